@@ -1,0 +1,169 @@
+/*
+ * brawl_oracle.h -- CPU restatement of BraWl's lattice-sampling hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA path
+ * is compared against (tests/, the smoke check and bench.py's CPU-baseline
+ * leg).  Nothing in the brawl_gb300 package links, loads or calls it.
+ *
+ * Parity status: pinned.  The restatement reproduces the reference's own
+ * golden outputs byte-for-byte (tests/99_ref/01_serial_metropolis,
+ * tests/99_ref/02_parallel_metropolis, tests/99_ref/03_serial_nested_sampling
+ * of the reference repository), and its Mersenne Twister is cross-checked
+ * word-for-word against the reference's src/mt19937ar.c compiled from source.
+ *
+ * Conventions shared with the reference (Fortran, column-major):
+ *   config(1, x, y, z) int8 on the doubled grid 2n1 x 2n2 x 2n3, stored with
+ *   x fastest: index = x + 2n1*(y + 2n2*z), all coordinates 0-based here.
+ *   V(a, b, shell) double in Ry, index = a + ns*(b + ns*shell), 0-based.
+ */
+#ifndef BRAWL_ORACLE_H
+#define BRAWL_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { BO_SC = 0, BO_BCC = 1, BO_FCC = 2 };
+
+/* ---- mt19937ar (src/mt19937ar.c) ---------------------------------------- */
+typedef struct {
+    uint32_t mt[624];
+    int mti;
+} bo_rng;
+
+void bo_rng_seed(bo_rng *r, uint32_t seed);
+uint32_t bo_rng_u32(bo_rng *r);
+double bo_rng_uniform(bo_rng *r);
+uint32_t bo_static_seed(int rank);
+
+/* ---- model --------------------------------------------------------------- */
+typedef struct {
+    int lattice;            /* BO_SC / BO_BCC / BO_FCC */
+    int n1, n2, n3;         /* conventional cells per direction */
+    int nsh;                /* interaction_range */
+    int ns;                 /* n_species */
+    const double *V;        /* V_ex, Ry */
+} bo_model;
+
+int bo_n_atoms(const bo_model *m);
+int bo_grid_size(const bo_model *m);
+int bo_max_shells(int lattice);
+int bo_shell_size(int lattice, int shell /* 1-based */);
+int bo_shell_offset(int lattice, int shell, int k, int d[3]);
+
+double bo_site_energy(const bo_model *m, const int8_t *cfg, int x, int y, int z);
+double bo_pair_energy(const bo_model *m, const int8_t *cfg, const int s1[3], const int s2[3]);
+double bo_total_energy(const bo_model *m, const int8_t *cfg);
+
+void bo_random_site(const bo_model *m, bo_rng *r, int site[3]);
+void bo_random_nbr(const bo_model *m, bo_rng *r, const int site[3], int nbr[3]);
+
+typedef struct {
+    int64_t trials;         /* monte_carlo_step calls */
+    int64_t evaluated;      /* trials whose two species differed */
+    int64_t draws;          /* 32-bit words drawn */
+    int64_t accepted;       /* accept == 1 (includes same-species trials) */
+    int64_t exp_tests;      /* trials that drew the acceptance uniform */
+} bo_counters;
+
+int bo_mc_step(const bo_model *m, int8_t *cfg, bo_rng *r, double beta,
+               int nbr_swap, bo_counters *c);
+int64_t bo_mc_run(const bo_model *m, int8_t *cfg, bo_rng *r, double beta,
+                  int64_t n_trials, int nbr_swap, bo_counters *c);
+/* Same trials, but also returns the per-trial accept flag and the delta-E
+ * (NaN for same-species trials), for trial-by-trial comparisons. */
+int64_t bo_mc_trace(const bo_model *m, int8_t *cfg, bo_rng *r, double beta,
+                    int64_t n_trials, int nbr_swap, int8_t *accept_out,
+                    double *de_out, bo_counters *c);
+
+/* initial_setup: conc has ns+1 entries with conc[0] = 0 (index 0..ns as in
+ * the reference); it is rewritten when numbers[] sums to n_atoms.  numbers
+ * may be NULL.  Returns 0, or -1 when the species counts cannot be made to
+ * sum to the number of sites. */
+int bo_initial_setup(const bo_model *m, double *conc, const int64_t *numbers,
+                     bo_rng *r, int8_t *cfg);
+
+/* ---- analytics ----------------------------------------------------------- */
+void bo_lattice_shells(const bo_model *m, const int8_t *cfg, int wc_range,
+                       double *shells);
+/* rho(i, j, l), index i + ns*(j + ns*l); counts (optional) get the raw
+ * integer pair counts in the same layout. */
+void bo_radial_densities(const bo_model *m, const int8_t *cfg, int wc_range,
+                         const double *shells, double *rho, int64_t *counts);
+
+/* ---- Metropolis simulated annealing (src/metropolis.F90:84-558) ---------- */
+typedef struct {
+    double T, delta_T;
+    int T_steps;
+    int64_t n_mc_steps, n_burn_in_steps;
+    int64_t n_sample_steps, n_sample_steps_asro, n_sample_steps_alro;
+    int64_t n_sample_steps_trajectory;
+    int burn_in, burn_in_start;
+    int calculate_energies, calculate_asro;
+    int nbr_swap;
+    int wc_range;
+} bo_anneal_params;
+
+typedef struct {
+    /* per temperature (T_steps) */
+    double *temperature, *energies_of_T, *C_of_T, *acceptance_of_T;
+    double *rho_of_T;           /* ns*ns*wc_range*T_steps (may be NULL) */
+    /* trajectory, written when n_sample_steps_trajectory divides the step;
+     * capacity in rows; rows filled returned in traj_rows */
+    int64_t traj_capacity;
+    int64_t traj_rows;
+    int64_t *traj_step;
+    double *traj_energy;        /* traj_capacity */
+    double *traj_asro;          /* traj_capacity * ns*ns*wc (may be NULL) */
+    /* configurations at start / end of each temperature (may be NULL) */
+    int8_t *initial_configs;    /* T_steps * grid */
+    int8_t *final_configs;      /* T_steps * grid */
+    double *shells;             /* wc_range */
+} bo_anneal_out;
+
+int bo_anneal(const bo_model *m, const bo_anneal_params *p, int8_t *cfg,
+              bo_rng *r, bo_anneal_out *o);
+
+/* ---- nested sampling (src/nested_sampling.f90:45-206) -------------------- */
+typedef struct {
+    int n_walkers, n_steps, n_iter;
+} bo_ns_params;
+
+/* Runs initialisation + n_iter iterations.  walkers: n_walkers*grid bytes of
+ * scratch (filled); energies: n_walkers; limits: n_iter (the ener_limit
+ * written at each iteration).  Returns 0. */
+int bo_ns_run(const bo_model *m, const bo_ns_params *p, double *conc,
+              const int64_t *numbers, bo_rng *r, int8_t *walkers,
+              double *energies, double *limits, int64_t *accepted_steps);
+
+/* One NS random walk of n_steps on one walker (inner loop of
+ * src/nested_sampling.f90:157-192).  Returns accepted steps. */
+int64_t bo_ns_walk(const bo_model *m, int8_t *cfg, bo_rng *r, double *energy,
+                   double ener_limit, int64_t n_steps, bo_counters *c);
+
+/* ---- Wang-Landau walker update (src/wang-landau.F90:515-632) ------------- */
+int bo_wl_bin_index(double energy, const double *bin_edges, int bins);
+
+typedef struct {
+    int bins;                   /* global number of bins */
+    int start_idx, end_idx;     /* 1-based window [start, end] */
+    int64_t n_trials;           /* mc_sweeps * n_atoms */
+    double wl_f;
+    int hist_period;            /* INT(0.02*REAL(n_atoms)) */
+} bo_wl_params;
+
+/* One walker's sweeps() trial loop.  lng: bins entries (global indexing),
+ * hist: window-local (end-start+1).  energy in/out is the walker's running
+ * e_unswapped (the reference recomputes it with full_energy at entry; the
+ * caller passes that value).  Returns accepted moves. */
+int64_t bo_wl_sweep(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
+                    bo_rng *r, const double *bin_edges, double *lng,
+                    double *hist, double *energy, bo_counters *c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
