@@ -1,0 +1,435 @@
+"""Benchmark: batched Metropolis swap trials on GB300 (one JSON line).
+
+Workload (the batched-replica configuration): 1024 independent bcc replicas,
+lattice edge L drawn per replica from {8, 12, 16, 24} (1024-27648 sites),
+4 equiatomic species, 6 coordination shells, V symmetric 4x4 per shell drawn
+uniform[-0.05, 0.05] eV from a fixed seed (converted to Ry), temperatures
+log-spaced 100-3000 K (one per replica), mt19937ar seed 110179 + 11 r per
+replica, random initial configurations drawn by initial_setup on the device.
+One step = `--sweeps-per-step` sweeps (N_r trials each) of every replica in
+one launch; 50 steps of 10 sweeps make the 500-sweep run.
+
+Reported:
+  value        trials/s with all state resident in HBM (device-timed)
+  e2e          trials/s through the C ABI with host buffers: every step
+               copies all replicas' configurations host->device, runs, and
+               copies them back (plus the accept counts)
+  roofline     algorithmic bytes per launch / kernel time, against the
+               measured HBM copy bandwidth
+  cpu_baseline the CPU oracle (a restatement of the reference's serial
+               Fortran, which needs gfortran/netCDF absent here) on all host
+               cores, on a bounded sample of the same replicas
+  plain_gpu    the one-chain-per-launch GPU path on a sample of replicas
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+RY_TO_EV = 13.605693122
+K_B_IN_RY = 8.167333262e-5 / 13.605693122990
+METRIC = "swap trials/s"
+WORKLOAD = "batched Metropolis: 1024 bcc replicas, L in {8,12,16,24}, 4 species, 6 shells"
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_workload(n_rep: int = 1024, seed: int = 20260, rank: int = 0):
+    rng = np.random.default_rng(seed)
+    Ls = rng.choice(np.array([8, 12, 16, 24]), size=n_rep)
+    ns, nsh = 4, 6
+    V = np.zeros((ns, ns, nsh))
+    for sh in range(nsh):
+        a = rng.uniform(-0.05, 0.05, size=(ns, ns))
+        V[:, :, sh] = np.triu(a) + np.triu(a, 1).T
+    V /= RY_TO_EV
+    r = np.arange(n_rep)
+    T = 100.0 * 30.0 ** (r / max(n_rep - 1, 1))
+    seeds = 110179 + 11 * (r + rank * n_rep)
+    conc = np.array([0.0, 0.25, 0.25, 0.25, 0.25])
+    return dict(L=Ls, V=V, T=T, seeds=seeds, conc=conc, ns=ns, nsh=nsh)
+
+
+def n_sites(L: int) -> int:
+    return 2 * L * L * L
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle port): one process per core, each owning one replica
+# ---------------------------------------------------------------------------
+def _cpu_worker(conn, replica: int, wl: dict):
+    from oracle import oracle as O
+    L = int(wl["L"][replica])
+    mod = O.OracleModel("bcc", L, L, L, wl["V"])
+    rng = O.OracleRng(int(wl["seeds"][replica]))
+    cfg, _ = mod.initial_setup(rng, wl["conc"])
+    beta = 1.0 / (float(wl["T"][replica]) * K_B_IN_RY)
+    conn.send("ready")
+    while True:
+        msg = conn.recv()
+        if msg is None:
+            break
+        t0 = time.perf_counter()
+        acc, _ = mod.mc_run(cfg, rng, beta, int(msg))
+        conn.send((int(msg), time.perf_counter() - t0))
+    conn.close()
+
+
+class CpuPool:
+    """Started with 'spawn' before any CUDA call."""
+
+    def __init__(self, n_procs: int, wl: dict):
+        ctx = mp.get_context("spawn")
+        self.conns, self.procs = [], []
+        # replicas spread over the four lattice sizes
+        order = np.argsort(wl["L"], kind="stable")
+        for k in range(n_procs):
+            replica = int(order[(k * len(order)) // n_procs])
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_cpu_worker, args=(b, replica, wl), daemon=True)
+            p.start()
+            self.conns.append(a)
+            self.procs.append(p)
+        for c in self.conns:
+            assert c.recv() == "ready"
+
+    def run(self, trials_each: int):
+        t0 = time.perf_counter()
+        for c in self.conns:
+            c.send(trials_each)
+        res = [c.recv() for c in self.conns]
+        wall = time.perf_counter() - t0
+        return sum(r[0] for r in res), wall
+
+    def close(self):
+        for c in self.conns:
+            try:
+                c.send(None)
+            except Exception:
+                pass
+        for p in self.procs:
+            p.join(timeout=5)
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_calibrate(pool: CpuPool, seconds: float) -> int:
+    n, wall = pool.run(20000)
+    per = max(wall, 1e-6) / 20000
+    return max(20000, int(seconds / per))
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.lines = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(device_index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def committed_traffic() -> dict | None:
+    """Per-trial DRAM traffic of the Metropolis kernel from the committed ncu
+    summary (profiles/metropolis_batched_traffic.json), if present."""
+    p = os.path.join(ROOT, "profiles", "metropolis_batched_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args, world, rank):
+    """The reference arm: the CPU implementation of the path (the oracle port
+    of the reference's serial Fortran) on all host cores."""
+    if rank != 0:
+        return 0
+    wl = make_workload(args.replicas)
+    cores = host_cores()
+    pool = CpuPool(cores, wl)
+    trials_each = cpu_calibrate(pool, 2.0)
+    for _ in range(args.warmup):
+        pool.run(trials_each)
+    tot, wall = 0, 0.0
+    for _ in range(args.steps):
+        n, w = pool.run(trials_each)
+        tot += n
+        wall += w
+    pool.close()
+    v = tot / wall
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "trials/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8+f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "replicas": args.replicas,
+                   "step": f"{cores} replicas x {trials_each} trials, one process per core"},
+        "cpu_baseline": {"value": v, "unit": "trials/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} replicas (spread over L) x {trials_each} trials per step"},
+        "e2e": {"value": v, "unit": "trials/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--replicas", type=int, default=1024)
+    ap.add_argument("--sweeps-per-step", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    wl = make_workload(args.replicas, rank=rank)
+    # CPU baseline workers first: spawned before any CUDA call
+    pool = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        pool = CpuPool(host_cores(), wl)
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import brawl_gb300 as B
+
+    setup_by_L = {L: B.Setup("bcc", L, L, L, wl["ns"], wl["nsh"]) for L in (8, 12, 16, 24)}
+    chains = []
+    for r in range(args.replicas):
+        L = int(wl["L"][r])
+        chains.append(dict(setup=setup_by_L[L], V=wl["V"], seed=int(wl["seeds"][r]),
+                           beta=1.0 / (float(wl["T"][r]) * K_B_IN_RY),
+                           species_concentrations=wl["conc"]))
+    batch = B.Batch(chains)
+    sites = np.array([n_sites(int(L)) for L in wl["L"]], dtype=np.int64)
+    trials = sites * args.sweeps_per_step
+    trials_per_step = int(trials.sum())
+
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def step_device():
+        batch.metropolis_async(trials, stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            step_device()
+        batch.sync()
+    c0 = batch.counters()
+
+    # ---- device-resident timed region -------------------------------------
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()                      # inputs < L2: flush between steps
+            starts[k].record(stream)
+            step_device()
+            ends[k].record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    batch.sync()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_s = sum(step_ms) / 1000.0
+    c1 = batch.counters()
+    if world > 1:
+        t = torch.tensor([dev_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t.item())
+    d = (c1 - c0).sum(axis=0)
+    T_all, T_eval, draws = int(d[0]), int(d[1]), int(d[2])
+    assert T_all == trials_per_step * args.steps, (T_all, trials_per_step * args.steps)
+    value = world * T_all / dev_s
+
+    # roofline: algorithmic bytes B = 2 T_all + (2 + 2z + 32z) T_eval + 4 D
+    z = 64
+    alg_bytes = 2 * T_all + (2 + 2 * z + 32 * z) * T_eval + 4 * draws
+    achieved_gbs = alg_bytes / dev_s / 1e9
+    peaks = measured_peaks()
+    traffic = None
+    tr = committed_traffic()
+    if tr and tr.get("dram_bytes_per_trial"):
+        traffic = float(tr["dram_bytes_per_trial"]) * T_all / args.steps
+
+    # ---- end to end through the C ABI with host buffers -------------------
+    grid_bytes = batch.grid_bytes
+    pinned = torch.empty(grid_bytes, dtype=torch.int8, pin_memory=True)
+    host_grids = pinned.numpy()
+    batch.get_configs(host_grids)
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch.set_configs(host_grids)          # h2d: every replica's config
+        acc = batch.metropolis(trials)         # launch + wait + accept counts (d2h)
+        batch.get_configs(host_grids)          # d2h: every replica's config
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * trials_per_step * e2e_steps / e2e_s
+    h2d = grid_bytes + 8 * args.replicas
+    d2h = grid_bytes + 8 * args.replicas * 9
+
+    # ---- plain one-chain-per-launch path on a sample -----------------------
+    sample = []
+    for L in (8, 12, 16, 24):
+        idx = np.nonzero(wl["L"] == L)[0]
+        sample += [int(i) for i in idx[:2]]
+    plain_chains = [chains[i] for i in sample]
+    pb = B.Batch(plain_chains)
+    ptrials = np.array([n_sites(int(wl["L"][i])) for i in sample], dtype=np.int64)
+    pb.metropolis_serial(ptrials // 10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pb.metropolis_serial(ptrials)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_value = float(ptrials.sum()) / plain_s
+    pb.close()
+
+    # ---- CPU baseline (oracle port) ------------------------------------------
+    cpu = None
+    if pool is not None:
+        each = cpu_calibrate(pool, args.cpu_seconds)
+        n, w = pool.run(each)
+        cores = len(pool.conns)
+        pool.close()
+        cpu = {"value": n / w, "unit": "trials/s", "cores": cores, "kind": "port",
+               "sample": f"{cores} replicas of the workload (spread over L), {each} trials each, "
+                         f"one process per core, {w:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "trials/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int8+f64",
+            "data": "synthetic (seeded replicas, V and temperatures)",
+            "config": {"workload": WORKLOAD, "replicas": args.replicas,
+                       "sweeps_per_step": args.sweeps_per_step,
+                       "trials_per_step": trials_per_step,
+                       "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "trials/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
+                         "traffic": traffic, "peak_source": peaks["source"],
+                         "algorithmic_bytes_per_step": alg_bytes / args.steps,
+                         "note": "latency-bound sequential chains; bytes are the canonical "
+                                 "algorithmic bytes per trial, mostly served from shared memory"},
+            "cpu_baseline": cpu,
+            "plain_gpu": {"value": plain_value, "unit": "trials/s",
+                          "sample": f"{len(sample)} replicas, 1 sweep each, one launch per replica"},
+            "batched_over_plain": value / plain_value,
+            "clocks": clk,
+            "gpu_launches": args.steps,
+            "counters": {"trials": T_all, "evaluated": T_eval, "draws": draws,
+                         "accepted": int(d[3]), "exp_tests": int(d[4]),
+                         "exact_path": int(d[5]), "exp_fp64": int(d[6]), "exp_cr": int(d[7])},
+            "wall_s_timed_region": t_wall,
+        }
+        print(json.dumps(line))
+    batch.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,400 @@
+"""brawl_gb300 -- GB300 (sm_103a) implementation of BraWl's lattice-sampling
+hot path, reached through the C ABI of include/brawl_gpu.h.
+
+The Python layer here is host logic only: it mirrors the reference's
+operator interface (total_energy, pair_energy, monte_carlo_step runs,
+initial_setup, radial_densities, the annealing driver) over the CUDA library
+libbrawl_gpu.so built in-tree by brawl_gb300.build.  There is no CPU
+fallback: every call fails loudly when the library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["load", "Setup", "Chain", "Batch", "BrawlError", "LATTICES", "K_B_IN_RY", "RY_TO_EV"]
+
+# src/constants.f90:41-49 (as written there)
+K_B_IN_EV = 8.167333262e-5
+K_B_IN_RY = 8.167333262e-5 / 13.605693122990
+RY_TO_EV = 13.605693122
+
+LATTICES = {"simple_cubic": 0, "sc": 0, "bcc": 1, "fcc": 2}
+NUM_COUNTERS = 8
+COUNTER_NAMES = ("trials", "evaluated", "draws", "accepted", "exp_tests", "exact_path",
+                 "exp_fp64", "exp_cr")
+
+
+class BrawlError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"brawl error {code}: {msg}")
+        self.code = code
+
+
+class _Setup(C.Structure):
+    _fields_ = [("lattice", C.c_int), ("n_1", C.c_int), ("n_2", C.c_int), ("n_3", C.c_int),
+                ("n_species", C.c_int), ("interaction_range", C.c_int)]
+
+
+class _ChainDesc(C.Structure):
+    _fields_ = [("setup", _Setup), ("V_ex", C.c_void_p), ("seed", C.c_uint32),
+                ("beta", C.c_double), ("nbr_swap", C.c_int),
+                ("species_concentrations", C.c_void_p), ("species_numbers", C.c_void_p),
+                ("config", C.c_void_p)]
+
+
+_LIB = None
+
+
+def load(rebuild: bool = False):
+    """The CUDA library, built if needed.  Raises when it cannot be loaded."""
+    global _LIB
+    if _LIB is not None and not rebuild:
+        return _LIB
+    path = _build.LIB
+    if rebuild or not os.path.exists(path):
+        _build.build(force=rebuild)
+    L = C.CDLL(path)
+    vp, i, i64, d, u32 = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_uint32
+    sig = {
+        "brawl_last_error": ([], C.c_char_p),
+        "brawl_version": ([], i),
+        "brawl_ctx_create": ([vp, vp, vp], i),
+        "brawl_ctx_destroy": ([vp], i),
+        "brawl_set_interactions": ([vp, vp], i),
+        "brawl_seed": ([vp, u32], i),
+        "brawl_f90_init_genrand": ([vp, i, i, u32, vp], i),
+        "brawl_rng_get": ([vp, vp], i),
+        "brawl_rng_set": ([vp, vp], i),
+        "brawl_genrand": ([vp, i64, vp], i),
+        "brawl_set_config": ([vp, vp], i),
+        "brawl_get_config": ([vp, vp], i),
+        "brawl_initial_setup": ([vp, vp, vp], i),
+        "brawl_total_energy": ([vp, vp], i),
+        "brawl_site_energy": ([vp, vp, vp], i),
+        "brawl_pair_energy": ([vp, vp, vp, vp], i),
+        "brawl_metropolis_run": ([vp, d, i64, i, vp], i),
+        "brawl_lattice_shells": ([vp, i, vp], i),
+        "brawl_radial_densities": ([vp, i, vp, vp], i),
+        "brawl_counters": ([vp, vp], i),
+        "brawl_batch_create": ([vp, i, vp], i),
+        "brawl_batch_destroy": ([vp], i),
+        "brawl_batch_size": ([vp, vp], i),
+        "brawl_batch_set_beta": ([vp, vp], i),
+        "brawl_batch_metropolis_run": ([vp, vp, vp], i),
+        "brawl_batch_metropolis_run_async": ([vp, vp, vp], i),
+        "brawl_batch_sync": ([vp], i),
+        "brawl_batch_metropolis_run_serial": ([vp, vp, vp], i),
+        "brawl_batch_total_energy": ([vp, vp], i),
+        "brawl_batch_get_config": ([vp, i, vp], i),
+        "brawl_batch_set_config": ([vp, i, vp], i),
+        "brawl_batch_rng_get": ([vp, i, vp], i),
+        "brawl_batch_get_configs": ([vp, vp], i),
+        "brawl_batch_set_configs": ([vp, vp], i),
+        "brawl_batch_counters": ([vp, vp], i),
+        "brawl_batch_radial_densities": ([vp, i, i, vp, vp], i),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _LIB = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise BrawlError(rc, load().brawl_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+class Setup:
+    """The subset of run_params (src/derived_types.f90:56-100) the path uses."""
+
+    def __init__(self, lattice, n_1, n_2, n_3, n_species, interaction_range):
+        self.lattice = LATTICES[lattice] if isinstance(lattice, str) else int(lattice)
+        self.n = (int(n_1), int(n_2), int(n_3))
+        self.n_species = int(n_species)
+        self.interaction_range = int(interaction_range)
+
+    @classmethod
+    def from_run_params(cls, p) -> "Setup":
+        return cls(p.lattice, p.n_1, p.n_2, p.n_3, p.n_species, p.interaction_range)
+
+    def c(self) -> _Setup:
+        return _Setup(self.lattice, *self.n, self.n_species, self.interaction_range)
+
+    @property
+    def grid_shape(self):
+        """(z, y, x): the C-ordered view of config(1, 2n1, 2n2, 2n3)."""
+        n1, n2, n3 = self.n
+        return (2 * n3, 2 * n2, 2 * n1)
+
+    @property
+    def n_atoms(self) -> int:
+        return (8, 2, 4)[self.lattice] * self.n[0] * self.n[1] * self.n[2]
+
+
+def _v_array(setup: Setup, V) -> np.ndarray:
+    V = np.asarray(V, dtype=np.float64)
+    shape = (setup.n_species, setup.n_species, setup.interaction_range)
+    if V.shape != shape:
+        raise ValueError(f"V_ex must have shape {shape}, got {V.shape}")
+    return np.ascontiguousarray(V.ravel(order="F"))
+
+
+class Chain:
+    """One simulation chain on the GPU (brawl_ctx): the reference's
+    single-process state (config, V_ex, the mt19937ar stream)."""
+
+    def __init__(self, setup: Setup, V):
+        self.setup = setup
+        self._V = _v_array(setup, V)
+        h = C.c_void_p()
+        s = setup.c()
+        _check(load().brawl_ctx_create(C.byref(s), _ptr(self._V), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().brawl_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- generator ----------------------------------------------------------
+    def seed(self, seed: int) -> None:
+        _check(load().brawl_seed(self._h, seed))
+
+    def f90_init_genrand(self, seedtime: int, my_rank: int, job_id: int = 0) -> int:
+        out = C.c_uint32()
+        _check(load().brawl_f90_init_genrand(self._h, seedtime, my_rank, job_id, C.byref(out)))
+        return out.value
+
+    def rng_state(self) -> np.ndarray:
+        st = np.zeros(625, dtype=np.uint32)
+        _check(load().brawl_rng_get(self._h, _ptr(st)))
+        return st
+
+    def set_rng_state(self, st) -> None:
+        st = np.ascontiguousarray(st, dtype=np.uint32)
+        _check(load().brawl_rng_set(self._h, _ptr(st)))
+
+    def genrand(self, n: int) -> np.ndarray:
+        out = np.zeros(n, dtype=np.float64)
+        _check(load().brawl_genrand(self._h, n, _ptr(out)))
+        return out
+
+    # -- configuration -------------------------------------------------------
+    def set_config(self, cfg: np.ndarray) -> None:
+        cfg = np.ascontiguousarray(cfg, dtype=np.int8)
+        if cfg.shape != self.setup.grid_shape:
+            raise ValueError(f"config must have shape {self.setup.grid_shape}")
+        _check(load().brawl_set_config(self._h, _ptr(cfg)))
+
+    def config(self) -> np.ndarray:
+        out = np.zeros(self.setup.grid_shape, dtype=np.int8)
+        _check(load().brawl_get_config(self._h, _ptr(out)))
+        return out
+
+    def initial_setup(self, species_concentrations, species_numbers=None) -> np.ndarray:
+        conc = np.ascontiguousarray(species_concentrations, dtype=np.float64).copy()
+        if conc.shape != (self.setup.n_species + 1,):
+            raise ValueError("species_concentrations needs n_species+1 entries ([0] = 0)")
+        nums = None
+        if species_numbers is not None:
+            nums = np.ascontiguousarray(species_numbers, dtype=np.int64)
+        _check(load().brawl_initial_setup(self._h, _ptr(conc), None if nums is None else _ptr(nums)))
+        return conc
+
+    # -- energies -------------------------------------------------------------
+    def total_energy(self) -> float:
+        e = C.c_double()
+        _check(load().brawl_total_energy(self._h, C.byref(e)))
+        return e.value
+
+    def site_energy(self, idx) -> float:
+        a = np.ascontiguousarray(idx, dtype=np.int32)
+        e = C.c_double()
+        _check(load().brawl_site_energy(self._h, _ptr(a), C.byref(e)))
+        return e.value
+
+    def pair_energy(self, idx1, idx2) -> float:
+        a = np.ascontiguousarray(idx1, dtype=np.int32)
+        b = np.ascontiguousarray(idx2, dtype=np.int32)
+        e = C.c_double()
+        _check(load().brawl_pair_energy(self._h, _ptr(a), _ptr(b), C.byref(e)))
+        return e.value
+
+    # -- sampling ---------------------------------------------------------------
+    def metropolis(self, beta: float, n_trials: int, nbr_swap: bool = False) -> int:
+        acc = C.c_int64()
+        _check(load().brawl_metropolis_run(self._h, float(beta), int(n_trials), int(bool(nbr_swap)),
+                                           C.byref(acc)))
+        return acc.value
+
+    def counters(self) -> dict:
+        c = np.zeros(NUM_COUNTERS, dtype=np.int64)
+        _check(load().brawl_counters(self._h, _ptr(c)))
+        return dict(zip(COUNTER_NAMES, (int(v) for v in c)))
+
+    # -- analytics ------------------------------------------------------------
+    def lattice_shells(self, wc_range: int) -> np.ndarray:
+        out = np.zeros(wc_range, dtype=np.float64)
+        _check(load().brawl_lattice_shells(self._h, wc_range, _ptr(out)))
+        return out
+
+    def radial_densities(self, shells) -> np.ndarray:
+        """rho shaped (wc_range, n_species, n_species): the C view of the
+        reference's rho(i, j, l)."""
+        shells = np.ascontiguousarray(shells, dtype=np.float64)
+        wc = shells.shape[0]
+        ns = self.setup.n_species
+        out = np.zeros((wc, ns, ns), dtype=np.float64)
+        _check(load().brawl_radial_densities(self._h, wc, _ptr(shells), _ptr(out)))
+        return out
+
+
+class Batch:
+    """Many independent chains (brawl_batch) that run in one launch."""
+
+    def __init__(self, chains: list[dict]):
+        """Each chain: dict(setup=Setup, V=array, seed=int, beta=float,
+        nbr_swap=bool, species_concentrations=array | None,
+        species_numbers=array | None, config=array | None)."""
+        n = len(chains)
+        descs = (_ChainDesc * n)()
+        self._keep = []
+        self.setups = []
+        for k, ch in enumerate(chains):
+            s = ch["setup"]
+            self.setups.append(s)
+            V = _v_array(s, ch["V"])
+            self._keep.append(V)
+            d = descs[k]
+            d.setup = s.c()
+            d.V_ex = V.ctypes.data
+            d.seed = int(ch.get("seed", 5489)) & 0xFFFFFFFF
+            d.beta = float(ch.get("beta", 0.0))
+            d.nbr_swap = int(bool(ch.get("nbr_swap", False)))
+            conc = ch.get("species_concentrations")
+            if conc is not None:
+                conc = np.ascontiguousarray(conc, dtype=np.float64)
+                self._keep.append(conc)
+                d.species_concentrations = conc.ctypes.data
+            nums = ch.get("species_numbers")
+            if nums is not None:
+                nums = np.ascontiguousarray(nums, dtype=np.int64)
+                self._keep.append(nums)
+                d.species_numbers = nums.ctypes.data
+            cfg = ch.get("config")
+            if cfg is not None:
+                cfg = np.ascontiguousarray(cfg, dtype=np.int8)
+                self._keep.append(cfg)
+                d.config = cfg.ctypes.data
+        h = C.c_void_p()
+        _check(load().brawl_batch_create(descs, n, C.byref(h)))
+        self._h = h
+        self.n = n
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().brawl_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_beta(self, beta) -> None:
+        b = np.ascontiguousarray(np.broadcast_to(np.asarray(beta, dtype=np.float64), (self.n,)))
+        _check(load().brawl_batch_set_beta(self._h, _ptr(b)))
+
+    def _trials(self, n_trials) -> np.ndarray:
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(n_trials, dtype=np.int64), (self.n,)))
+
+    def metropolis(self, n_trials) -> np.ndarray:
+        t = self._trials(n_trials)
+        acc = np.zeros(self.n, dtype=np.int64)
+        _check(load().brawl_batch_metropolis_run(self._h, _ptr(t), _ptr(acc)))
+        return acc
+
+    def metropolis_async(self, n_trials, stream: int | None = None) -> None:
+        self._pending = self._trials(n_trials)
+        _check(load().brawl_batch_metropolis_run_async(self._h, _ptr(self._pending),
+                                                       C.c_void_p(stream) if stream else None))
+
+    def sync(self) -> None:
+        _check(load().brawl_batch_sync(self._h))
+
+    def metropolis_serial(self, n_trials) -> np.ndarray:
+        t = self._trials(n_trials)
+        acc = np.zeros(self.n, dtype=np.int64)
+        _check(load().brawl_batch_metropolis_run_serial(self._h, _ptr(t), _ptr(acc)))
+        return acc
+
+    def total_energy(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.float64)
+        _check(load().brawl_batch_total_energy(self._h, _ptr(out)))
+        return out
+
+    def config(self, c: int) -> np.ndarray:
+        out = np.zeros(self.setups[c].grid_shape, dtype=np.int8)
+        _check(load().brawl_batch_get_config(self._h, c, _ptr(out)))
+        return out
+
+    def set_config(self, c: int, cfg) -> None:
+        cfg = np.ascontiguousarray(cfg, dtype=np.int8)
+        _check(load().brawl_batch_set_config(self._h, c, _ptr(cfg)))
+
+    def rng_state(self, c: int) -> np.ndarray:
+        st = np.zeros(625, dtype=np.uint32)
+        _check(load().brawl_batch_rng_get(self._h, c, _ptr(st)))
+        return st
+
+    @property
+    def grid_bytes(self) -> int:
+        return sum(int(np.prod(s.grid_shape)) for s in self.setups)
+
+    def get_configs(self, out: np.ndarray | None = None) -> np.ndarray:
+        """All chains' grids concatenated (int8, grid_bytes)."""
+        if out is None:
+            out = np.zeros(self.grid_bytes, dtype=np.int8)
+        assert out.dtype == np.int8 and out.size == self.grid_bytes and out.flags.c_contiguous
+        _check(load().brawl_batch_get_configs(self._h, _ptr(out)))
+        return out
+
+    def set_configs(self, grids: np.ndarray) -> None:
+        assert grids.dtype == np.int8 and grids.size == self.grid_bytes and grids.flags.c_contiguous
+        _check(load().brawl_batch_set_configs(self._h, _ptr(grids)))
+
+    def counters(self) -> np.ndarray:
+        out = np.zeros((self.n, NUM_COUNTERS), dtype=np.int64)
+        _check(load().brawl_batch_counters(self._h, _ptr(out)))
+        return out
+
+    def radial_densities(self, c: int, shells) -> np.ndarray:
+        shells = np.ascontiguousarray(shells, dtype=np.float64)
+        wc = shells.shape[0]
+        ns = self.setups[c].n_species
+        out = np.zeros((wc, ns, ns), dtype=np.float64)
+        _check(load().brawl_batch_radial_densities(self._h, c, wc, _ptr(shells), _ptr(out)))
+        return out

@@ -1,0 +1,963 @@
+// capi.cu -- the C ABI declared in include/brawl_gpu.h.
+//
+// A brawl_batch owns one device arena holding, per chain, the compact
+// lattice, the mt19937ar block, V_ex, its fixed-point image and the neighbour
+// entries, so a chain's whole state stays resident between calls.  A
+// brawl_ctx is a batch of one chain.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "../../include/brawl_gpu.h"
+#include "asro.cuh"
+#include "kernels.cuh"
+
+using namespace brawl;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                   \
+  do {                                                                                \
+    cudaError_t e_ = (x);                                                             \
+    if (e_ != cudaSuccess) {                                                          \
+      return fail(e_ == cudaErrorMemoryAllocation ? BRAWL_ENOMEM : BRAWL_ECUDA,       \
+                  std::string(#x) + ": " + cudaGetErrorString(e_));                   \
+    }                                                                                 \
+  } while (0)
+
+#define TRY(x)                 \
+  do {                         \
+    int r_ = (x);              \
+    if (r_ != BRAWL_OK) return r_; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// host-side model preparation
+// ---------------------------------------------------------------------------
+int make_geom(const brawl_setup& s, Geom& g) {
+  if (s.lattice < BRAWL_SIMPLE_CUBIC || s.lattice > BRAWL_FCC)
+    return fail(BRAWL_EINVAL, "Lattice type not yet implemented!");
+  if (s.n_1 < 1 || s.n_2 < 1 || s.n_3 < 1 || s.n_1 > 1024 || s.n_2 > 1024 || s.n_3 > 1024)
+    return fail(BRAWL_EINVAL, "n_1, n_2, n_3 must be in 1..1024");
+  if (s.n_species < 1 || s.n_species > kMaxSpecies)
+    return fail(BRAWL_EINVAL, "n_species must be in 1..15");
+  if (s.interaction_range < 1 || s.interaction_range > max_shells(s.lattice))
+    return fail(BRAWL_EINVAL, "Unsupported number of shells");
+  const int64_t sites = (int64_t)n_atoms(s.lattice, s.n_1, s.n_2, s.n_3);
+  if (sites > (int64_t)1 << 30) return fail(BRAWL_EINVAL, "lattice too large");
+  std::memset(&g, 0, sizeof(g));
+  g.lattice = s.lattice;
+  g.n1 = s.n_1;
+  g.n2 = s.n_2;
+  g.n3 = s.n_3;
+  g.nsh = s.interaction_range;
+  g.ns = s.n_species;
+  g.n_sites = (int32_t)sites;
+  g.z = shell_starts(s.lattice)[g.nsh];
+  if (s.lattice == kBcc) {
+    g.sz = s.n_1 * s.n_2;
+    g.sy = s.n_1;
+    g.ys = 1;
+    g.xs = 1;
+  } else if (s.lattice == kFcc) {
+    g.sz = 2 * s.n_2 * s.n_1;
+    g.sy = s.n_1;
+    g.ys = 0;
+    g.xs = 1;
+  } else {
+    g.sz = 4 * s.n_1 * s.n_2;
+    g.sy = 2 * s.n_1;
+    g.ys = 0;
+    g.xs = 0;
+  }
+  const int f = s.lattice == kSimpleCubic ? 1 : 2;  // sc wraps modulo n
+  g.W1 = f * s.n_1;
+  g.W2 = f * s.n_2;
+  g.W3 = f * s.n_3;
+  int dmax = 0;
+  const int8_t(*offs)[3] = shell_offsets(s.lattice);
+  for (int k = 0; k < g.z; ++k)
+    for (int a = 0; a < 3; ++a) dmax = std::max(dmax, std::abs((int)offs[k][a]));
+  g.fast_wrap = (s.lattice != kSimpleCubic) && std::min(g.W1, std::min(g.W2, g.W3)) >= dmax;
+  g.nbr_k = s.lattice == kSimpleCubic ? 6 : s.lattice == kBcc ? 8 : 12;
+  return BRAWL_OK;
+}
+
+struct Model {
+  Geom g;
+  std::vector<double> V;
+  std::vector<int32_t> F;
+  std::vector<uint32_t> entries;
+  std::vector<int16_t> sstart;
+  int S = 0;
+  int band = 0;
+};
+
+// Fixed-point image of V_ex for the fast tier.  S is the largest shift with
+// 4 z max|V| 2^S <= 2^30, so a swap's 2z terms (each a difference of two
+// entries) sum without overflow in int32.  band bounds, in quanta, the
+// distance between the fixed-point sum and the reference's FP64 value of
+// e_swapped - e_unswapped: one quantum per term for rounding V to the grid,
+// plus the worst case of the reference's own recursive FP64 sums (every term
+// passes through at most kmax + nsh - 1 roundings; |error| <= gamma_h *
+// sum|terms| for each of the two pair energies), plus two quanta of slack.
+int make_model(const brawl_setup& s, const double* V_ex, Model& m) {
+  TRY(make_geom(s, m.g));
+  if (!V_ex) return fail(BRAWL_EINVAL, "V_ex is NULL");
+  const Geom& g = m.g;
+  const int nv = g.ns * g.ns * g.nsh;
+  m.V.assign(V_ex, V_ex + nv);
+  double vmax = 0.0;
+  for (double v : m.V) {
+    if (!std::isfinite(v)) return fail(BRAWL_EINVAL, "V_ex contains a non-finite value");
+    vmax = std::max(vmax, std::fabs(v));
+  }
+  const int nsp = g.ns + 1;
+  m.F.assign((size_t)nsp * nsp * g.nsh, 0);
+  if (vmax > 0.0) {
+    m.S = (int)std::floor(std::log2(std::ldexp(1.0, 30) / (4.0 * g.z * vmax)));
+    m.S = std::max(-200, std::min(m.S, 200));
+    for (int a = 1; a <= g.ns; ++a)
+      for (int b = 1; b <= g.ns; ++b)
+        for (int sh = 0; sh < g.nsh; ++sh) {
+          double v = m.V[(a - 1) + g.ns * ((b - 1) + g.ns * sh)];
+          m.F[(a * nsp + b) * g.nsh + sh] = (int32_t)std::llrint(std::ldexp(v, m.S));
+        }
+    const int16_t* st = shell_starts(g.lattice);
+    int kmax = 0;
+    for (int sh = 0; sh < g.nsh; ++sh) kmax = std::max(kmax, (int)(st[sh + 1] - st[sh]));
+    const int h = kmax + g.nsh - 1;
+    const double fp = 4.0 * h * std::ldexp(1.0, -53) * g.z * vmax * std::ldexp(1.0, m.S) * 1.01;
+    m.band = 2 * g.z + 2 + (int)std::ceil(fp);
+  } else {
+    m.S = 0;
+    m.band = 0;
+  }
+  const int16_t* st = shell_starts(g.lattice);
+  const int8_t(*offs)[3] = shell_offsets(g.lattice);
+  m.sstart.assign(st, st + g.nsh + 1);
+  m.entries.resize(g.z);
+  for (int sh = 0; sh < g.nsh; ++sh)
+    for (int k = st[sh]; k < st[sh + 1]; ++k)
+      m.entries[k] = (uint32_t)(uint8_t)offs[k][0] | ((uint32_t)(uint8_t)offs[k][1] << 8) |
+                     ((uint32_t)(uint8_t)offs[k][2] << 16) | ((uint32_t)sh << 24);
+  return BRAWL_OK;
+}
+
+void set_beta(ChainJob& j, const Model& m, double beta) {
+  j.beta = beta;
+  const double q = std::ldexp(1.0, -m.S);
+  j.beta_q = (float)(beta * q);
+  double bb = beta * (double)m.band * q;
+  float bf = (float)bb;
+  if ((double)bf < bb) bf = std::nextafter(bf, INFINITY);
+  j.beta_band = bf;
+}
+
+// init_genrand (src/mt19937ar.c:63-78)
+void mt_seed_host(uint32_t seed, uint32_t* state) {
+  state[0] = seed;
+  for (int i = 1; i < kMTN; ++i)
+    state[i] = 1812433253u * (state[i - 1] ^ (state[i - 1] >> 30)) + (uint32_t)i;
+  state[kMTN] = kMTN;
+}
+
+// Species quotas and interval bounds of initial_setup
+// (src/initialise.F90:468-506, 534-535).
+int make_init_job(const Model& m, double* conc, const int64_t* numbers, InitJob& ij) {
+  const Geom& g = m.g;
+  const int ns = g.ns;
+  const int64_t n_atoms = g.n_sites;
+  int64_t count[kMaxSpecies];
+  int64_t sumnum = 0;
+  if (numbers)
+    for (int i = 0; i < ns; ++i) sumnum += numbers[i];
+  if (numbers && sumnum == n_atoms) {
+    for (int i = 0; i < ns; ++i) {
+      count[i] = numbers[i];
+      conc[i + 1] = (double)((float)count[i] / (float)n_atoms);
+    }
+  } else {
+    int64_t total = 0;
+    for (int i = 0; i < ns; ++i) {
+      const double prod = (double)(float)n_atoms * conc[i + 1];
+      if (!std::isfinite(prod)) return fail(BRAWL_EINVAL, "invalid species_concentrations");
+      count[i] = (int64_t)std::llround(prod);
+      total += count[i];
+    }
+    int64_t round_check = total - n_atoms;
+    const int64_t inc = (-round_check >= 0) ? 1 : -1;
+    int guard = 0;
+    while (round_check != 0) {
+      bool any = false;
+      for (int j = 0; j < ns; ++j) {
+        if (count[j] == 0 || round_check == 0) continue;
+        count[j] += inc;
+        round_check += inc;
+        any = true;
+      }
+      if (!any || ++guard > 1000000) break;
+    }
+  }
+  int64_t sum = 0;
+  for (int i = 0; i < ns; ++i) {
+    if (count[i] < 0) return fail(BRAWL_EINVAL, "negative species count");
+    sum += count[i];
+  }
+  if (sum != n_atoms) return fail(BRAWL_EINVAL, "Species counts do not sum to the number of lattice sites");
+  std::memset(&ij, 0, sizeof(ij));
+  ij.n_sites = g.n_sites;
+  ij.ns = ns;
+  double lo = 0.0;
+  for (int l = 1; l <= ns; ++l) {
+    // sum(c(0:l-1)) and sum(c(0:l)), sequential as gfortran's SUM
+    double a = 0.0;
+    for (int i = 0; i <= l - 1; ++i) a = a + conc[i];
+    double b = 0.0;
+    for (int i = 0; i <= l; ++i) b = b + conc[i];
+    lo = a;
+    // w*2^-32 >= lo  <=>  w >= ceil(lo*2^32);  w*2^-32 <= b  <=>  w <= floor(b*2^32)
+    double los = std::ceil(std::ldexp(lo, 32)), his = std::floor(std::ldexp(b, 32));
+    los = std::max(-1.0, std::min(los, 8589934592.0));
+    his = std::max(-1.0, std::min(his, 8589934592.0));
+    ij.lo_w[l - 1] = (int64_t)los;
+    ij.hi_w[l - 1] = (int64_t)his;
+    ij.counts[l - 1] = count[l - 1];
+    // a species whose quota is open must be reachable, or the loop never ends
+    if (count[l - 1] > 0 && ij.lo_w[l - 1] > ij.hi_w[l - 1])
+      return fail(BRAWL_EINVAL, "a species with atoms has an empty concentration interval");
+    if (count[l - 1] > 0 && (ij.hi_w[l - 1] < 0 || ij.lo_w[l - 1] > 4294967295LL))
+      return fail(BRAWL_EINVAL, "a species with atoms has an unreachable concentration interval");
+  }
+  return BRAWL_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// batch
+// ---------------------------------------------------------------------------
+struct brawl_batch {
+  std::vector<Model> models;
+  std::vector<ChainJob> jobs;            // host images (pointers into the arena)
+  std::vector<int> nbr_swap;
+  unsigned char* arena = nullptr;
+  ChainJob* d_jobs = nullptr;
+  EnergyJob* d_ejobs = nullptr;
+  AsroJob* d_ajob = nullptr;
+  unsigned long long* d_counters = nullptr;
+  int32_t* d_status = nullptr;
+  double* d_energy = nullptr;
+  double* d_site_e = nullptr;            // lazily sized scratch
+  size_t site_e_cap = 0;
+  int8_t* d_grid = nullptr;              // staging for one full grid
+  size_t grid_cap = 0;
+  int8_t* d_grids = nullptr;             // staging for every chain's grid
+  GridJob* d_gjobs = nullptr;
+  int64_t total_cells = 0;
+  void* d_scratch = nullptr;             // ASRO offsets and counts
+  size_t scratch_cap = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t smem_bytes = 0;
+  bool smem_lat = true;
+  std::vector<unsigned long long> last_counters;
+  int device = 0;
+};
+
+struct brawl_ctx {
+  brawl_batch* b;
+};
+
+namespace {
+
+int check_status(brawl_batch* b) {
+  std::vector<int32_t> st(b->jobs.size());
+  CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_status, st.size() * 4, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (size_t i = 0; i < st.size(); ++i)
+    if (st[i] != 0) {
+      int32_t zero = 0;
+      cudaMemcpy(b->d_status + i, &zero, 4, cudaMemcpyHostToDevice);
+      return fail(BRAWL_ESTATE, "device check failed on chain " + std::to_string(i) + " (code " +
+                                    std::to_string(st[i]) + ")");
+    }
+  return BRAWL_OK;
+}
+
+int ensure_grid(brawl_batch* b, size_t bytes) {
+  if (bytes <= b->grid_cap) return BRAWL_OK;
+  if (b->d_grid) cudaFree(b->d_grid);
+  b->d_grid = nullptr;
+  b->grid_cap = 0;
+  CUDA_TRY(cudaMalloc(&b->d_grid, bytes));
+  b->grid_cap = bytes;
+  return BRAWL_OK;
+}
+
+int upload_jobs(brawl_batch* b) {
+  CUDA_TRY(cudaMemcpyAsync(b->d_jobs, b->jobs.data(), b->jobs.size() * sizeof(ChainJob),
+                           cudaMemcpyHostToDevice, b->stream));
+  return BRAWL_OK;
+}
+
+int read_counters(brawl_batch* b, std::vector<unsigned long long>& out) {
+  out.resize(b->jobs.size() * kNumCounters);
+  CUDA_TRY(cudaMemcpyAsync(out.data(), b->d_counters, out.size() * 8, cudaMemcpyDeviceToHost,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int set_chain_config(brawl_batch* b, int c, const int8_t* config) {
+  const Geom& g = b->models[c].g;
+  const size_t grid = (size_t)8 * g.n1 * g.n2 * g.n3;
+  TRY(ensure_grid(b, grid));
+  CUDA_TRY(cudaMemcpyAsync(b->d_grid, config, grid, cudaMemcpyHostToDevice, b->stream));
+  launch_pack(g, b->d_grid, b->jobs[c].lat, b->d_status + c, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  int r = check_status(b);
+  if (r != BRAWL_OK) return fail(BRAWL_EINVAL, "config holds a species outside 1..n_species on an occupied site, or an atom on an empty site");
+  return BRAWL_OK;
+}
+
+int run_metropolis(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, bool serial,
+                   cudaStream_t stream, bool wait) {
+  const int n = (int)b->jobs.size();
+  for (int c = 0; c < n; ++c) {
+    if (n_trials[c] < 0) return fail(BRAWL_EINVAL, "n_trials < 0");
+    b->jobs[c].n_trials = n_trials[c];
+    b->jobs[c].nbr_swap = b->nbr_swap[c];
+  }
+  TRY(upload_jobs(b));
+  if (stream != b->stream) {
+    // order the job upload before the launch on the caller's stream
+    cudaEvent_t ev;
+    CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(ev, b->stream));
+    CUDA_TRY(cudaStreamWaitEvent(stream, ev, 0));
+    cudaEventDestroy(ev);
+  }
+  if (serial) {
+    for (int c = 0; c < n; ++c) {
+      launch_metropolis(b->d_jobs + c, 1, b->smem_lat, b->smem_bytes, stream);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaStreamSynchronize(stream));
+    }
+  } else {
+    launch_metropolis(b->d_jobs, n, b->smem_lat, b->smem_bytes, stream);
+    CUDA_TRY(cudaGetLastError());
+  }
+  if (!wait) return BRAWL_OK;
+  CUDA_TRY(cudaStreamSynchronize(stream));
+  std::vector<unsigned long long> cnt;
+  TRY(read_counters(b, cnt));
+  if (accepted)
+    for (int c = 0; c < n; ++c)
+      accepted[c] = (int64_t)(cnt[c * kNumCounters + kCntAccepted] -
+                              b->last_counters[c * kNumCounters + kCntAccepted]);
+  b->last_counters = cnt;
+  return check_status(b);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* brawl_last_error(void) { return g_err.c_str(); }
+int brawl_version(void) { return 10000; }
+
+int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch** out) {
+  if (!out || !chains || n_chains < 1) return fail(BRAWL_EINVAL, "no chains");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+    return fail(BRAWL_ECUDA, "no CUDA device");
+  brawl_batch* b = new brawl_batch();
+  auto cleanup = [&](int rc) {
+    brawl_batch_destroy(b);
+    return rc;
+  };
+  cudaGetDevice(&b->device);
+  b->models.resize(n_chains);
+  b->jobs.resize(n_chains);
+  b->nbr_swap.resize(n_chains);
+  for (int c = 0; c < n_chains; ++c) {
+    int r = make_model(chains[c].setup, chains[c].V_ex, b->models[c]);
+    if (r != BRAWL_OK) return cleanup(fail(r, "chain " + std::to_string(c) + ": " + g_err));
+    b->nbr_swap[c] = chains[c].nbr_swap ? 1 : 0;
+  }
+  // shared memory: lattice staged when every chain fits
+  int max_optin = 0;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  uint32_t need_smem = 0, need_gmem = 0;
+  for (auto& m : b->models) {
+    need_smem = std::max(need_smem, smem_layout(m.g, true).total);
+    need_gmem = std::max(need_gmem, smem_layout(m.g, false).total);
+  }
+  b->smem_lat = need_smem <= (uint32_t)max_optin;
+  b->smem_bytes = b->smem_lat ? need_smem : need_gmem;
+  if (b->smem_bytes > (uint32_t)max_optin)
+    return cleanup(fail(BRAWL_EINVAL, "interaction tables exceed shared memory"));
+  // arena layout
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  std::vector<size_t> off_lat(n_chains), off_rng(n_chains), off_V(n_chains), off_F(n_chains),
+      off_e(n_chains), off_s(n_chains);
+  size_t total = 0;
+  for (int c = 0; c < n_chains; ++c) {
+    const Model& m = b->models[c];
+    off_lat[c] = total;
+    total = al(total + m.g.n_sites);
+    off_rng[c] = total;
+    total = al(total + (kMTN + 1) * 4);
+    off_V[c] = total;
+    total = al(total + m.V.size() * 8);
+    off_F[c] = total;
+    total = al(total + m.F.size() * 4);
+    off_e[c] = total;
+    total = al(total + m.entries.size() * 4);
+    off_s[c] = total;
+    total = al(total + m.sstart.size() * 2);
+  }
+  const size_t off_jobs = total;
+  total = al(total + n_chains * sizeof(ChainJob));
+  const size_t off_ejobs = total;
+  total = al(total + n_chains * sizeof(EnergyJob));
+  const size_t off_ajob = total;
+  total = al(total + sizeof(AsroJob));
+  const size_t off_cnt = total;
+  total = al(total + (size_t)n_chains * kNumCounters * 8);
+  const size_t off_status = total;
+  total = al(total + (size_t)n_chains * 4);
+  const size_t off_energy = total;
+  total = al(total + (size_t)n_chains * 8);
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(fail(BRAWL_ECUDA, "stream create failed"));
+  cudaError_t e = cudaMalloc(&b->arena, total);
+  if (e != cudaSuccess) {
+    b->arena = nullptr;
+    return cleanup(fail(BRAWL_ENOMEM, std::string("arena: ") + cudaGetErrorString(e)));
+  }
+  std::vector<unsigned char> h(total, 0);
+  for (int c = 0; c < n_chains; ++c) {
+    const Model& m = b->models[c];
+    mt_seed_host(chains[c].seed, reinterpret_cast<uint32_t*>(&h[off_rng[c]]));
+    std::memcpy(&h[off_V[c]], m.V.data(), m.V.size() * 8);
+    std::memcpy(&h[off_F[c]], m.F.data(), m.F.size() * 4);
+    std::memcpy(&h[off_e[c]], m.entries.data(), m.entries.size() * 4);
+    std::memcpy(&h[off_s[c]], m.sstart.data(), m.sstart.size() * 2);
+    ChainJob& j = b->jobs[c];
+    std::memset(&j, 0, sizeof(j));
+    j.g = m.g;
+    j.nbr_swap = b->nbr_swap[c];
+    j.band = m.band;
+    set_beta(j, m, chains[c].beta);
+    j.lat = reinterpret_cast<int8_t*>(b->arena + off_lat[c]);
+    j.rng = reinterpret_cast<uint32_t*>(b->arena + off_rng[c]);
+    j.V = reinterpret_cast<const double*>(b->arena + off_V[c]);
+    j.F = reinterpret_cast<const int32_t*>(b->arena + off_F[c]);
+    j.entries = reinterpret_cast<const uint32_t*>(b->arena + off_e[c]);
+    j.shell_start = reinterpret_cast<const int16_t*>(b->arena + off_s[c]);
+    j.counters = reinterpret_cast<unsigned long long*>(b->arena + off_cnt) + c * kNumCounters;
+    j.status = reinterpret_cast<int32_t*>(b->arena + off_status) + c;
+  }
+  b->d_jobs = reinterpret_cast<ChainJob*>(b->arena + off_jobs);
+  b->d_ejobs = reinterpret_cast<EnergyJob*>(b->arena + off_ejobs);
+  b->d_ajob = reinterpret_cast<AsroJob*>(b->arena + off_ajob);
+  b->d_counters = reinterpret_cast<unsigned long long*>(b->arena + off_cnt);
+  b->d_status = reinterpret_cast<int32_t*>(b->arena + off_status);
+  b->d_energy = reinterpret_cast<double*>(b->arena + off_energy);
+  std::memcpy(&h[off_jobs], b->jobs.data(), n_chains * sizeof(ChainJob));
+  e = cudaMemcpy(b->arena, h.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
+  b->last_counters.assign((size_t)n_chains * kNumCounters, 0);
+  // configurations: given ones are packed, the others drawn by initial_setup
+  std::vector<InitJob> init;
+  for (int c = 0; c < n_chains; ++c) {
+    if (chains[c].config) {
+      int r = set_chain_config(b, c, chains[c].config);
+      if (r != BRAWL_OK) return cleanup(fail(r, "chain " + std::to_string(c) + ": " + g_err));
+    } else {
+      if (!chains[c].species_concentrations)
+        return cleanup(fail(BRAWL_EINVAL, "chain " + std::to_string(c) +
+                                              ": needs a config or species_concentrations"));
+      std::vector<double> conc(chains[c].species_concentrations,
+                               chains[c].species_concentrations + b->models[c].g.ns + 1);
+      InitJob ij;
+      int r = make_init_job(b->models[c], conc.data(), chains[c].species_numbers, ij);
+      if (r != BRAWL_OK) return cleanup(fail(r, "chain " + std::to_string(c) + ": " + g_err));
+      ij.lat = b->jobs[c].lat;
+      ij.rng = b->jobs[c].rng;
+      ij.counters = b->jobs[c].counters;
+      ij.status = b->jobs[c].status;
+      init.push_back(ij);
+    }
+  }
+  if (!init.empty()) {
+    InitJob* d_init = nullptr;
+    e = cudaMalloc(&d_init, init.size() * sizeof(InitJob));
+    if (e != cudaSuccess) return cleanup(fail(BRAWL_ENOMEM, cudaGetErrorString(e)));
+    cudaMemcpyAsync(d_init, init.data(), init.size() * sizeof(InitJob), cudaMemcpyHostToDevice,
+                    b->stream);
+    launch_initial_setup(d_init, (int)init.size(), b->stream);
+    e = cudaStreamSynchronize(b->stream);
+    cudaFree(d_init);
+    if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
+    int r = check_status(b);
+    if (r != BRAWL_OK) return cleanup(r);
+  }
+  {
+    std::vector<unsigned long long> cnt;
+    int r = read_counters(b, cnt);
+    if (r != BRAWL_OK) return cleanup(r);
+    b->last_counters = cnt;
+  }
+  *out = b;
+  return BRAWL_OK;
+}
+
+int brawl_batch_destroy(brawl_batch* b) {
+  if (!b) return BRAWL_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->arena) cudaFree(b->arena);
+  if (b->d_site_e) cudaFree(b->d_site_e);
+  if (b->d_grid) cudaFree(b->d_grid);
+  if (b->d_grids) cudaFree(b->d_grids);
+  if (b->d_gjobs) cudaFree(b->d_gjobs);
+  if (b->d_scratch) cudaFree(b->d_scratch);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return BRAWL_OK;
+}
+
+int brawl_batch_size(brawl_batch* b, int* n) {
+  if (!b || !n) return fail(BRAWL_EINVAL, "null argument");
+  *n = (int)b->jobs.size();
+  return BRAWL_OK;
+}
+
+int brawl_batch_set_beta(brawl_batch* b, const double* beta) {
+  if (!b || !beta) return fail(BRAWL_EINVAL, "null argument");
+  for (size_t c = 0; c < b->jobs.size(); ++c) set_beta(b->jobs[c], b->models[c], beta[c]);
+  return BRAWL_OK;
+}
+
+int brawl_batch_metropolis_run(brawl_batch* b, const int64_t* n_trials, int64_t* accepted) {
+  if (!b || !n_trials) return fail(BRAWL_EINVAL, "null argument");
+  return run_metropolis(b, n_trials, accepted, false, b->stream, true);
+}
+
+int brawl_batch_metropolis_run_async(brawl_batch* b, const int64_t* n_trials, void* stream) {
+  if (!b || !n_trials) return fail(BRAWL_EINVAL, "null argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+  return run_metropolis(b, n_trials, nullptr, false, s, false);
+}
+
+int brawl_batch_sync(brawl_batch* b) {
+  if (!b) return fail(BRAWL_EINVAL, "null argument");
+  CUDA_TRY(cudaDeviceSynchronize());
+  std::vector<unsigned long long> cnt;
+  TRY(read_counters(b, cnt));
+  b->last_counters = cnt;
+  return check_status(b);
+}
+
+int brawl_batch_metropolis_run_serial(brawl_batch* b, const int64_t* n_trials, int64_t* accepted) {
+  if (!b || !n_trials) return fail(BRAWL_EINVAL, "null argument");
+  return run_metropolis(b, n_trials, accepted, true, b->stream, true);
+}
+
+int brawl_batch_total_energy(brawl_batch* b, double* energies) {
+  if (!b || !energies) return fail(BRAWL_EINVAL, "null argument");
+  const int n = (int)b->jobs.size();
+  int64_t total_sites = 0;
+  for (int c = 0; c < n; ++c) total_sites += b->models[c].g.n_sites;
+  if ((size_t)total_sites * 8 > b->site_e_cap) {
+    if (b->d_site_e) cudaFree(b->d_site_e);
+    b->d_site_e = nullptr;
+    b->site_e_cap = 0;
+    CUDA_TRY(cudaMalloc(&b->d_site_e, (size_t)total_sites * 8));
+    b->site_e_cap = (size_t)total_sites * 8;
+  }
+  std::vector<EnergyJob> ej(n);
+  int64_t off = 0;
+  for (int c = 0; c < n; ++c) {
+    EnergyJob& j = ej[c];
+    j.g = b->models[c].g;
+    j.lat = b->jobs[c].lat;
+    j.V = b->jobs[c].V;
+    j.entries = b->jobs[c].entries;
+    j.shell_start = b->jobs[c].shell_start;
+    j.site_energy = b->d_site_e + off;
+    j.out = b->d_energy + c;
+    j.site_offset = off;
+    off += j.g.n_sites;
+  }
+  CUDA_TRY(cudaMemcpyAsync(b->d_ejobs, ej.data(), n * sizeof(EnergyJob), cudaMemcpyHostToDevice,
+                           b->stream));
+  launch_total_energy(b->d_ejobs, n, total_sites, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(energies, b->d_energy, n * 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_get_config(brawl_batch* b, int c, int8_t* config) {
+  if (!b || !config || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad argument");
+  const Geom& g = b->models[c].g;
+  const size_t grid = (size_t)8 * g.n1 * g.n2 * g.n3;
+  TRY(ensure_grid(b, grid));
+  launch_unpack(g, b->jobs[c].lat, b->d_grid, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(config, b->d_grid, grid, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_set_config(brawl_batch* b, int c, const int8_t* config) {
+  if (!b || !config || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad argument");
+  return set_chain_config(b, c, config);
+}
+
+static int ensure_grids(brawl_batch* b) {
+  if (b->d_grids) return BRAWL_OK;
+  const int n = (int)b->jobs.size();
+  std::vector<GridJob> gj(n);
+  int64_t off = 0;
+  for (int c = 0; c < n; ++c) {
+    gj[c].g = b->models[c].g;
+    gj[c].lat = b->jobs[c].lat;
+    gj[c].grid_offset = off;
+    gj[c].status = b->jobs[c].status;
+    off += (int64_t)8 * gj[c].g.n1 * gj[c].g.n2 * gj[c].g.n3;
+  }
+  CUDA_TRY(cudaMalloc(&b->d_grids, (size_t)off));
+  CUDA_TRY(cudaMalloc(&b->d_gjobs, n * sizeof(GridJob)));
+  CUDA_TRY(cudaMemcpy(b->d_gjobs, gj.data(), n * sizeof(GridJob), cudaMemcpyHostToDevice));
+  b->total_cells = off;
+  return BRAWL_OK;
+}
+
+int brawl_batch_get_configs(brawl_batch* b, int8_t* configs) {
+  if (!b || !configs) return fail(BRAWL_EINVAL, "null argument");
+  TRY(ensure_grids(b));
+  launch_unpack_batch(b->d_gjobs, (int)b->jobs.size(), b->total_cells, b->d_grids, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(configs, b->d_grids, (size_t)b->total_cells, cudaMemcpyDeviceToHost,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_set_configs(brawl_batch* b, const int8_t* configs) {
+  if (!b || !configs) return fail(BRAWL_EINVAL, "null argument");
+  TRY(ensure_grids(b));
+  CUDA_TRY(cudaMemcpyAsync(b->d_grids, configs, (size_t)b->total_cells, cudaMemcpyHostToDevice,
+                           b->stream));
+  launch_pack_batch(b->d_gjobs, (int)b->jobs.size(), b->total_cells, b->d_grids, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  int r = check_status(b);
+  if (r != BRAWL_OK) return fail(BRAWL_EINVAL, "a config holds a species outside 1..n_species on an occupied site, or an atom on an empty site");
+  return BRAWL_OK;
+}
+
+int brawl_batch_rng_get(brawl_batch* b, int c, uint32_t state[625]) {
+  if (!b || !state || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad argument");
+  CUDA_TRY(cudaMemcpyAsync(state, b->jobs[c].rng, (kMTN + 1) * 4, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_counters(brawl_batch* b, int64_t* counters) {
+  if (!b || !counters) return fail(BRAWL_EINVAL, "null argument");
+  std::vector<unsigned long long> cnt;
+  TRY(read_counters(b, cnt));
+  for (size_t i = 0; i < cnt.size(); ++i) counters[i] = (int64_t)cnt[i];
+  return BRAWL_OK;
+}
+
+int brawl_batch_radial_densities(brawl_batch* b, int c, int wc_range, const double* shells,
+                                 double* rho) {
+  if (!b || !shells || !rho || c < 0 || c >= (int)b->jobs.size() || wc_range < 1 || wc_range > 64)
+    return fail(BRAWL_EINVAL, "bad argument");
+  const Geom& g = b->models[c].g;
+  AsroPlan plan;
+  TRY(make_asro_plan(g, wc_range, shells, plan) == 0 ? BRAWL_OK
+                                                     : fail(BRAWL_EINVAL, "bad ASRO plan"));
+  const int nsp = g.ns + 1;
+  const size_t n_counts = (size_t)nsp * nsp * plan.n_class + nsp;
+  const size_t bytes = plan.offsets.size() * 4 + 256 + n_counts * 8;
+  if (bytes > b->scratch_cap) {
+    if (b->d_scratch) cudaFree(b->d_scratch);
+    b->d_scratch = nullptr;
+    b->scratch_cap = 0;
+    CUDA_TRY(cudaMalloc(&b->d_scratch, bytes));
+    b->scratch_cap = bytes;
+  }
+  unsigned char* s = reinterpret_cast<unsigned char*>(b->d_scratch);
+  uint32_t* d_offs = reinterpret_cast<uint32_t*>(s);
+  unsigned long long* d_cnt =
+      reinterpret_cast<unsigned long long*>(s + (plan.offsets.size() * 4 + 255) / 256 * 256);
+  CUDA_TRY(cudaMemcpyAsync(d_offs, plan.offsets.data(), plan.offsets.size() * 4,
+                           cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaMemsetAsync(d_cnt, 0, n_counts * 8, b->stream));
+  AsroJob aj;
+  aj.g = g;
+  aj.lat = b->jobs[c].lat;
+  aj.offsets = d_offs;
+  aj.n_offsets = (int)plan.offsets.size();
+  aj.n_class = plan.n_class;
+  aj.counts = d_cnt;
+  aj.species_counts = d_cnt + (size_t)nsp * nsp * plan.n_class;
+  CUDA_TRY(cudaMemcpyAsync(b->d_ajob, &aj, sizeof(aj), cudaMemcpyHostToDevice, b->stream));
+  launch_asro(b->d_ajob, g, plan.n_class, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  std::vector<unsigned long long> cnt(n_counts);
+  CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_cnt, n_counts * 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  finish_asro(g, wc_range, plan, cnt.data(), rho);
+  return BRAWL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// single chain
+// ---------------------------------------------------------------------------
+int brawl_ctx_create(const brawl_setup* setup, const double* V_ex, brawl_ctx** out) {
+  if (!setup || !out) return fail(BRAWL_EINVAL, "null argument");
+  *out = nullptr;
+  Geom g;
+  TRY(make_geom(*setup, g));
+  // an empty lattice until set_config / initial_setup: all sites species 1
+  std::vector<int8_t> grid((size_t)8 * setup->n_1 * setup->n_2 * setup->n_3, 0);
+  {
+    const int W1 = 2 * g.n1, W2 = 2 * g.n2;
+    for (size_t t = 0; t < grid.size(); ++t) {
+      int x = (int)(t % W1), y = (int)((t / W1) % W2), z = (int)(t / ((size_t)W1 * W2));
+      bool occ = g.lattice == kBcc   ? (((x & 1) == (z & 1)) && ((y & 1) == (z & 1)))
+                 : g.lattice == kFcc ? (((x + y + z) & 1) == 0)
+                                     : true;
+      grid[t] = occ ? 1 : 0;
+    }
+  }
+  brawl_chain_desc d;
+  std::memset(&d, 0, sizeof(d));
+  d.setup = *setup;
+  d.V_ex = V_ex;
+  d.seed = 5489u;
+  d.beta = 0.0;
+  d.config = grid.data();
+  brawl_batch* b = nullptr;
+  TRY(brawl_batch_create(&d, 1, &b));
+  *out = new brawl_ctx{b};
+  return BRAWL_OK;
+}
+
+int brawl_ctx_destroy(brawl_ctx* ctx) {
+  if (!ctx) return BRAWL_OK;
+  brawl_batch_destroy(ctx->b);
+  delete ctx;
+  return BRAWL_OK;
+}
+
+int brawl_set_interactions(brawl_ctx* ctx, const double* V_ex) {
+  if (!ctx || !V_ex) return fail(BRAWL_EINVAL, "null argument");
+  brawl_batch* b = ctx->b;
+  brawl_setup s = {b->models[0].g.lattice, b->models[0].g.n1, b->models[0].g.n2, b->models[0].g.n3,
+                   b->models[0].g.ns, b->models[0].g.nsh};
+  Model m;
+  TRY(make_model(s, V_ex, m));
+  ChainJob& j = b->jobs[0];
+  CUDA_TRY(cudaMemcpyAsync(const_cast<double*>(j.V), m.V.data(), m.V.size() * 8,
+                           cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(const_cast<int32_t*>(j.F), m.F.data(), m.F.size() * 4,
+                           cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  const double beta = j.beta;
+  b->models[0] = m;
+  j.band = m.band;
+  set_beta(j, m, beta);
+  return BRAWL_OK;
+}
+
+int brawl_seed(brawl_ctx* ctx, uint32_t seed) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  uint32_t st[kMTN + 1];
+  mt_seed_host(seed, st);
+  return brawl_rng_set(ctx, st);
+}
+
+int brawl_f90_init_genrand(brawl_ctx* ctx, int seedtime, int my_rank, uint32_t job_id,
+                           uint32_t* seed_out) {
+  // src/mt19937ar.c:127-142
+  uint32_t seed;
+  if (seedtime) {
+    seed = (uint32_t)time(nullptr);
+    seed += 11u * (uint32_t)my_rank;
+    seed += job_id;
+    if (seed % 2 == 0) seed += 1;
+  } else {
+    seed = 110179u + 11u * (uint32_t)my_rank;
+  }
+  if (seed_out) *seed_out = seed;
+  return brawl_seed(ctx, seed);
+}
+
+int brawl_rng_get(brawl_ctx* ctx, uint32_t state[625]) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_rng_get(ctx->b, 0, state);
+}
+
+int brawl_rng_set(brawl_ctx* ctx, const uint32_t state[625]) {
+  if (!ctx || !state) return fail(BRAWL_EINVAL, "null argument");
+  if (state[kMTN] > (uint32_t)kMTN) {
+    // mti == N+1 means "never seeded": the reference then seeds with 5489
+    if (state[kMTN] == (uint32_t)kMTN + 1) return brawl_seed(ctx, 5489u);
+    return fail(BRAWL_EINVAL, "mti out of range");
+  }
+  brawl_batch* b = ctx->b;
+  CUDA_TRY(cudaMemcpyAsync(b->jobs[0].rng, state, (kMTN + 1) * 4, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_genrand(brawl_ctx* ctx, int64_t n, double* out) {
+  if (!ctx || (n > 0 && !out) || n < 0) return fail(BRAWL_EINVAL, "bad argument");
+  // The stream is advanced on the host from the device state: the draws the
+  // host needs (clone choices, exchange shuffles) are few.
+  uint32_t st[kMTN + 1];
+  TRY(brawl_rng_get(ctx, st));
+  int pos = (int)st[kMTN];
+  for (int64_t i = 0; i < n; ++i) {
+    if (pos >= kMTN) {
+      for (int k = 0; k < kMTN; ++k) {
+        uint32_t y = (st[k] & 0x80000000u) | (st[(k + 1) % kMTN] & 0x7fffffffu);
+        st[k] = st[(k + kMTM) % kMTN] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      }
+      pos = 0;
+    }
+    uint32_t y = st[pos++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    out[i] = (double)y * (1.0 / 4294967296.0);
+  }
+  st[kMTN] = (uint32_t)pos;
+  return brawl_rng_set(ctx, st);
+}
+
+int brawl_set_config(brawl_ctx* ctx, const int8_t* config) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_set_config(ctx->b, 0, config);
+}
+
+int brawl_get_config(brawl_ctx* ctx, int8_t* config) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_get_config(ctx->b, 0, config);
+}
+
+int brawl_initial_setup(brawl_ctx* ctx, double* conc, const int64_t* numbers) {
+  if (!ctx || !conc) return fail(BRAWL_EINVAL, "null argument");
+  brawl_batch* b = ctx->b;
+  std::vector<double> c(conc, conc + b->models[0].g.ns + 1);
+  InitJob ij;
+  TRY(make_init_job(b->models[0], c.data(), numbers, ij));
+  ij.lat = b->jobs[0].lat;
+  ij.rng = b->jobs[0].rng;
+  ij.counters = b->jobs[0].counters;
+  ij.status = b->jobs[0].status;
+  InitJob* d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, sizeof(InitJob)));
+  cudaMemcpyAsync(d, &ij, sizeof(ij), cudaMemcpyHostToDevice, b->stream);
+  launch_initial_setup(d, 1, b->stream);
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(BRAWL_ECUDA, cudaGetErrorString(e));
+  TRY(check_status(b));
+  std::copy(c.begin(), c.end(), conc);
+  return BRAWL_OK;
+}
+
+int brawl_total_energy(brawl_ctx* ctx, double* energy) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_total_energy(ctx->b, energy);
+}
+
+static int site_from_idx(const Geom& g, const int idx[4], int& x, int& y, int& z) {
+  if (idx[0] != 1) return fail(BRAWL_EINVAL, "basis index must be 1");
+  x = idx[1] - 1;
+  y = idx[2] - 1;
+  z = idx[3] - 1;
+  if (x < 0 || y < 0 || z < 0 || x >= 2 * g.n1 || y >= 2 * g.n2 || z >= 2 * g.n3)
+    return fail(BRAWL_EINVAL, "site outside the lattice");
+  bool occ = g.lattice == kBcc   ? (((x & 1) == (z & 1)) && ((y & 1) == (z & 1)))
+             : g.lattice == kFcc ? (((x + y + z) & 1) == 0)
+                                 : true;
+  if (!occ) return fail(BRAWL_EINVAL, "site is not a lattice site");
+  return BRAWL_OK;
+}
+
+int brawl_site_energy(brawl_ctx* ctx, const int idx[4], double* energy) {
+  if (!ctx || !idx || !energy) return fail(BRAWL_EINVAL, "null argument");
+  brawl_batch* b = ctx->b;
+  int x, y, z;
+  TRY(site_from_idx(b->models[0].g, idx, x, y, z));
+  EnergyJob j;
+  std::memset(&j, 0, sizeof(j));
+  j.g = b->models[0].g;
+  j.lat = b->jobs[0].lat;
+  j.V = b->jobs[0].V;
+  j.entries = b->jobs[0].entries;
+  j.shell_start = b->jobs[0].shell_start;
+  CUDA_TRY(cudaMemcpyAsync(b->d_ejobs, &j, sizeof(j), cudaMemcpyHostToDevice, b->stream));
+  launch_site_energy(b->d_ejobs, x, y, z, b->d_energy, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(energy, b->d_energy, 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_pair_energy(brawl_ctx* ctx, const int idx1[4], const int idx2[4], double* energy) {
+  double e1, e2;
+  TRY(brawl_site_energy(ctx, idx1, &e1));
+  TRY(brawl_site_energy(ctx, idx2, &e2));
+  *energy = e1 + e2;
+  return BRAWL_OK;
+}
+
+int brawl_metropolis_run(brawl_ctx* ctx, double beta, int64_t n_trials, int nbr_swap,
+                         int64_t* accepted) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  brawl_batch* b = ctx->b;
+  set_beta(b->jobs[0], b->models[0], beta);
+  b->nbr_swap[0] = nbr_swap ? 1 : 0;
+  return run_metropolis(b, &n_trials, accepted, false, b->stream, true);
+}
+
+int brawl_lattice_shells(brawl_ctx* ctx, int wc_range, double* shells) {
+  if (!ctx || !shells || wc_range < 1) return fail(BRAWL_EINVAL, "bad argument");
+  lattice_shells_host(ctx->b->models[0].g, wc_range, shells);
+  return BRAWL_OK;
+}
+
+int brawl_radial_densities(brawl_ctx* ctx, int wc_range, const double* shells, double* rho) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_radial_densities(ctx->b, 0, wc_range, shells, rho);
+}
+
+int brawl_counters(brawl_ctx* ctx, int64_t* counters) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_counters(ctx->b, counters);
+}
+
+}  // extern "C"

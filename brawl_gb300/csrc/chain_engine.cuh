@@ -1,0 +1,391 @@
+// chain_engine.cuh -- the per-chain, warp-cooperative pieces of BraWl's
+// sampling hot path on sm_103a.
+//
+// One chain (replica, walker) is owned by one warp.  Its lattice lives as a
+// compact uint8 array of occupied sites (shared memory when it fits), its
+// mt19937ar state as 624 words in shared memory, and every trial follows the
+// reference's sequential proposal order on that chain's own stream:
+//
+//   * site draws        -- *_random_site, src/random_site.f90:74-193
+//                          (z, x, y for fcc/bcc; x, y, z for simple cubic),
+//                          computed exactly with integer multiply-high
+//   * swap energy       -- pair_energy before/after the swap,
+//                          src/bw_hamiltonian.f90:99-114
+//   * decision          -- monte_carlo_step_lattice, src/metropolis.F90:751-813
+//
+// Energies are decided in two tiers.  The fast tier sums the swap's energy
+// change as exact int32 fixed point (V_ex scaled by 2^S and rounded), spread
+// over the 32 lanes and reduced with one redux.sync; its distance from the
+// reference's FP64 value is bounded by `band` quanta (fixed-point rounding
+// plus the worst-case rounding of the reference's own FP64 sums).  Only when
+// a decision falls inside that band does the warp recompute the four site
+// energies in the reference's exact FP64 order (one lane per shell sum,
+// neighbours added in list order, shells added left to right, then
+// site1 + site2 and e_swapped - e_unswapped).
+#pragma once
+
+#include <cstdint>
+
+#include "exact_fp.cuh"
+#include "lattice_tables.h"
+
+namespace brawl {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMTN = 624;
+constexpr int kMTM = 397;
+constexpr int kMaxZ = 168;           // neighbour entries of bcc with 10 shells
+constexpr int kMaxLaneEntries = 11;  // ceil(2 * kMaxZ / 32)
+constexpr int kMaxSpecies = 15;      // species codes 1..15 (int8 storage)
+
+enum Counter : int {
+  kCntTrials = 0,    // monte_carlo_step calls (or WL/NS steps)
+  kCntEvaluated,     // trials whose two species differed
+  kCntDraws,         // 32-bit words consumed from the chain's stream
+  kCntAccepted,      // accept == 1
+  kCntExpTests,      // trials that drew the acceptance uniform
+  kCntExactPath,     // trials decided with the FP64 reference-order sums
+  kCntExpFp64,       // exp/log decisions that needed the FP64 libm value
+  kCntExpCr,         // ... and the double-double value
+  kNumCounters
+};
+
+enum Status : int {
+  kStatusOk = 0,
+  kStatusRngInvariant = 1,   // stream position left its block (internal error)
+  kStatusBadSpecies = 2,     // a species code outside 1..ns was met
+};
+
+struct Geom {
+  int32_t lattice, n1, n2, n3;
+  int32_t nsh, ns, n_sites, z;
+  int32_t sy, sz, xs, ys;     // compact index: z*sz + (y>>ys)*sy + (x>>xs)
+  int32_t W1, W2, W3;         // neighbour wrap modulus per axis
+  int32_t fast_wrap;          // one conditional add/sub wraps every offset
+  int32_t nbr_k;              // nearest-neighbour count (6/8/12)
+  int32_t pad;
+};
+
+// One chain's work order for a launch.  Plain data, shared with the host.
+struct ChainJob {
+  Geom g;
+  int32_t nbr_swap;
+  int32_t band;               // decision band of the fixed-point tier, quanta
+  double beta;
+  float beta_q;               // beta * 2^-S (float)
+  float beta_band;            // beta * band * 2^-S, rounded up (float)
+  int64_t n_trials;
+  int8_t* lat;                // compact species array, n_sites bytes
+  uint32_t* rng;              // mt[624], then the stream position
+  const double* V;            // V_ex(a, b, shell), a fastest, ns*ns*nsh
+  const int32_t* F;           // fixed-point V: F[(a*(ns+1) + b)*nsh + shell]
+  const uint32_t* entries;    // z packed neighbour entries (dx,dy,dz,shell)
+  const int16_t* shell_start; // nsh + 1 entry offsets
+  unsigned long long* counters;
+  int32_t* status;
+};
+
+// ---------------------------------------------------------------------------
+// mt19937ar (src/mt19937ar.c:82-125), warp-cooperative
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t mt_temper(uint32_t y) {
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return y;
+}
+
+__device__ __forceinline__ uint32_t mt_mix(uint32_t a, uint32_t b, uint32_t c) {
+  // c ^ (y >> 1) ^ mag01[y & 1] with y = (a & UPPER) | (b & LOWER)
+  uint32_t y = (a & 0x80000000u) | (b & 0x7fffffffu);
+  return c ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+}
+
+// Regenerates the 624-word block in place with the whole warp, in three
+// phases that respect the recurrence's dependencies: words [0,227) read
+// only old words, [227,454) read new words of the first phase, and
+// [454,624) read new words of the second phase (word 623 also reads the new
+// word 0, as the reference's last step does).  Each phase reads all of its
+// inputs before any lane writes.
+__device__ __forceinline__ void mt_twist_warp(uint32_t* mt, int lane) {
+  const int bounds[4] = {0, kMTN - kMTM, 2 * (kMTN - kMTM), kMTN};
+#pragma unroll
+  for (int ph = 0; ph < 3; ++ph) {
+    const int lo = bounds[ph], hi = bounds[ph + 1];
+    uint32_t nv[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      int k = lo + lane + 32 * i;
+      nv[i] = 0;
+      if (k < hi) {
+        int k1 = k + 1 == kMTN ? 0 : k + 1;
+        int km = k + kMTM;
+        km = km >= kMTN ? km - kMTN : km;
+        nv[i] = mt_mix(mt[k], mt[k1], mt[km]);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      int k = lo + lane + 32 * i;
+      if (k < hi) mt[k] = nv[i];
+    }
+    __syncwarp();
+  }
+}
+
+// Makes n words (n <= 32) available at positions pos..pos+n-1 and returns
+// word pos+lane in lanes < n.  When fewer than n words remain in the block
+// the remaining ones are captured first, the block is regenerated and pos
+// becomes negative (the captured words sit at negative positions).  The
+// caller must then consume at least the captured words, which holds for
+// every caller: a trial never consumes fewer than n-1 of n peeked words and
+// a block is only regenerated when at most n-1 remain.
+__device__ __forceinline__ uint32_t mt_peek(uint32_t* mt, int& pos, int n, int lane) {
+  int avail = kMTN - pos;
+  uint32_t w = 0;
+  if (avail >= n) {
+    if (lane < n) w = mt_temper(mt[pos + lane]);
+  } else {
+    if (lane < avail) w = mt_temper(mt[pos + lane]);
+    __syncwarp();
+    mt_twist_warp(mt, lane);
+    if (lane >= avail && lane < n) w = mt_temper(mt[lane - avail]);
+    pos -= kMTN;
+  }
+  return w;
+}
+
+// ---------------------------------------------------------------------------
+// lattice addressing
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int compact_index(const Geom& g, int x, int y, int z) {
+  return z * g.sz + (y >> g.ys) * g.sy + (x >> g.xs);
+}
+
+// inverse of compact_index
+__device__ __forceinline__ void decode_site(const Geom& g, int idx, int& x, int& y, int& z) {
+  if (g.lattice == kBcc) {
+    z = idx / g.sz;
+    int r = idx - z * g.sz;
+    int yh = r / g.sy, xh = r - yh * g.sy;
+    int p = z & 1;
+    y = 2 * yh + p;
+    x = 2 * xh + p;
+  } else if (g.lattice == kFcc) {
+    z = idx / g.sz;
+    int r = idx - z * g.sz;
+    y = r / g.sy;
+    int xh = r - y * g.sy;
+    x = 2 * xh + ((y + z) & 1);
+  } else {
+    z = idx / g.sz;
+    int r = idx - z * g.sz;
+    y = r / g.sy;
+    x = r - y * g.sy;
+  }
+}
+
+__device__ __forceinline__ int wrap_fast(int c, int W) {
+  c = c < 0 ? c + W : c;
+  return c >= W ? c - W : c;
+}
+
+// General rule: an axis with a zero offset keeps the site's own index (the
+// reference uses site_i directly there), otherwise modulo(i + d, W).
+__device__ __forceinline__ int wrap_general(int c, int d, int W) {
+  if (d == 0) return c;
+  int t = (c + d) % W;
+  return t < 0 ? t + W : t;
+}
+
+__device__ __forceinline__ int neighbour_index(const Geom& g, int x, int y, int z, int dx,
+                                               int dy, int dz) {
+  int nx, ny, nz;
+  if (g.fast_wrap) {
+    nx = wrap_fast(x + dx, g.W1);
+    ny = wrap_fast(y + dy, g.W2);
+    nz = wrap_fast(z + dz, g.W3);
+  } else {
+    nx = wrap_general(x, dx, g.W1);
+    ny = wrap_general(y, dy, g.W2);
+    nz = wrap_general(z, dz, g.W3);
+  }
+  return compact_index(g, nx, ny, nz);
+}
+
+__device__ __forceinline__ uint32_t umulhi32(uint32_t w, uint32_t k) { return __umulhi(w, k); }
+
+// floor(u * k) for u = w * 2^-32 and small k is exactly (w * k) >> 32.
+__device__ __forceinline__ void draw_site(const Geom& g, uint32_t w0, uint32_t w1, uint32_t w2,
+                                          int& x, int& y, int& z) {
+  if (g.lattice == kBcc) {
+    z = (int)umulhi32(w0, 2u * g.n3);
+    int p = z & 1;
+    x = 2 * (int)umulhi32(w1, (uint32_t)g.n1) + p;
+    y = 2 * (int)umulhi32(w2, (uint32_t)g.n2) + p;
+  } else if (g.lattice == kFcc) {
+    z = (int)umulhi32(w0, 2u * g.n3);
+    x = (int)umulhi32(w1, 2u * g.n1);
+    y = 2 * (int)umulhi32(w2, (uint32_t)g.n2) + ((x + z) & 1);
+  } else {
+    x = (int)umulhi32(w0, 2u * g.n1);
+    y = (int)umulhi32(w1, 2u * g.n2);
+    z = (int)umulhi32(w2, 2u * g.n3);
+  }
+}
+
+// Nearest-neighbour vectors of the nbr_swap proposals (the reference's
+// sc_nbrs, bcc_nbrs and fcc_nbrs, src/random_site.f90:29-61), by lattice code.
+static __constant__ int8_t cNbrSwap[3][12][3] = {
+    {{0, 0, 1}, {0, 1, 0}, {1, 0, 0}, {0, 0, -1}, {0, -1, 0}, {-1, 0, 0}},
+    {{1, 1, 1}, {1, 1, -1}, {1, -1, 1}, {1, -1, -1}, {-1, 1, 1}, {-1, 1, -1}, {-1, -1, 1},
+     {-1, -1, -1}},
+    {{0, 1, 1}, {0, 1, -1}, {0, -1, 1}, {0, -1, -1}, {1, 1, 0}, {1, -1, 0}, {1, 0, 1},
+     {1, 0, -1}, {-1, 1, 0}, {-1, -1, 0}, {-1, 0, 1}, {-1, 0, -1}}};
+
+// Nearest neighbour chosen by one draw, n = floor(k*u)
+// (src/random_site.f90:97-225); wraps on the doubled grid for every lattice.
+__device__ __forceinline__ void draw_nbr(const Geom& g, uint32_t w, int x, int y, int z,
+                                         int& nx, int& ny, int& nz) {
+  const int k = (int)umulhi32(w, (uint32_t)g.nbr_k);
+  const int8_t* v = cNbrSwap[g.lattice][k];
+  nx = wrap_general(x, v[0], 2 * g.n1);
+  ny = wrap_general(y, v[1], 2 * g.n2);
+  nz = wrap_general(z, v[2], 2 * g.n3);
+}
+
+__device__ __forceinline__ void unpack_entry(uint32_t e, int& dx, int& dy, int& dz, int& sh) {
+  dx = (int)(int8_t)(e & 0xffu);
+  dy = (int)(int8_t)((e >> 8) & 0xffu);
+  dz = (int)(int8_t)((e >> 16) & 0xffu);
+  sh = (int)(e >> 24);
+}
+
+struct SitePair {
+  int ax, ay, az, ai;  // site 1 (rdm1)
+  int bx, by, bz, bi;  // site 2 (rdm2)
+  int sa, sb;          // species before the swap
+};
+
+// ---------------------------------------------------------------------------
+// Fast tier: exact fixed-point energy change of swapping the two sites.
+// Lane entries: entry e in [0, 2z) belongs to site 1 for e < z and to site 2
+// otherwise; lane l owns entries l, l+32, ...
+// ---------------------------------------------------------------------------
+struct LaneEntries {
+  uint32_t e[kMaxLaneEntries];  // packed (dx,dy,dz,shell)
+  uint32_t site2_mask;          // bit j: entry j belongs to site 2
+  int n;
+};
+
+__device__ __forceinline__ void load_lane_entries(const uint32_t* ents, int z, int lane,
+                                                  LaneEntries& le) {
+  le.n = 0;
+  le.site2_mask = 0;
+#pragma unroll
+  for (int j = 0; j < kMaxLaneEntries; ++j) {
+    int e = lane + 32 * j;
+    le.e[j] = 0;
+    if (e < 2 * z) {
+      int k = e < z ? e : e - z;
+      le.e[j] = ents[k];
+      if (e >= z) le.site2_mask |= 1u << j;
+      le.n = j + 1;
+    }
+  }
+}
+
+__device__ __forceinline__ int fixed_delta(const Geom& g, const int8_t* lat, const int32_t* F,
+                                           const LaneEntries& le, const SitePair& p) {
+  const int nsp = g.ns + 1;
+  const int nsh = g.nsh;
+  int acc = 0;
+#pragma unroll
+  for (int j = 0; j < kMaxLaneEntries; ++j) {
+    if (j < le.n) {
+      const bool b = (le.site2_mask >> j) & 1u;
+      int dx, dy, dz, sh;
+      unpack_entry(le.e[j], dx, dy, dz, sh);
+      const int cx = b ? p.bx : p.ax, cy = b ? p.by : p.ay, cz = b ? p.bz : p.az;
+      const int own = b ? p.bi : p.ai, other = b ? p.ai : p.bi;
+      const int so = b ? p.sb : p.sa, sn = b ? p.sa : p.sb;
+      const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
+      const int s_before = lat[ni];
+      const int s_after = ni == other ? so : (ni == own ? sn : s_before);
+      acc += F[(sn * nsp + s_after) * nsh + sh] - F[(so * nsp + s_before) * nsh + sh];
+    }
+  }
+  return __reduce_add_sync(kFull, acc);
+}
+
+// ---------------------------------------------------------------------------
+// Exact tier: the reference's FP64 pair energies before and after the swap.
+// Chain c in [0, 4*nsh): evaluation c / nsh (0: site 1 before, 1: site 2
+// before, 2: site 1 after, 3: site 2 after), shell c % nsh.
+// ---------------------------------------------------------------------------
+__device__ inline void exact_pair_energies(const Geom& g, const int8_t* lat, const double* V,
+                                           const uint32_t* ents, const int16_t* sstart,
+                                           const SitePair& p, int lane, double& e_un,
+                                           double& e_sw) {
+  const int nsh = g.nsh, ns = g.ns;
+  const int nc = 4 * nsh;
+  double part[2] = {0.0, 0.0};
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int c = lane + 32 * r;
+    if (c < nc) {
+      const int ev = c / nsh, sh = c - ev * nsh;
+      const bool on2 = ev & 1, after = ev >= 2;
+      const int cx = on2 ? p.bx : p.ax, cy = on2 ? p.by : p.ay, cz = on2 ? p.bz : p.az;
+      const int own = on2 ? p.bi : p.ai, other = on2 ? p.ai : p.bi;
+      const int s_own_before = on2 ? p.sb : p.sa;
+      const int s_own_after = on2 ? p.sa : p.sb;
+      const int cs = after ? s_own_after : s_own_before;
+      double sum = 0.0;
+      for (int k = sstart[sh]; k < sstart[sh + 1]; ++k) {
+        int dx, dy, dz, shk;
+        unpack_entry(ents[k], dx, dy, dz, shk);
+        const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
+        int s = lat[ni];
+        if (after) {
+          if (ni == other) s = s_own_before;        // the partner now holds our old species
+          else if (ni == own) s = s_own_after;
+        }
+        sum = __dadd_rn(sum, V[(cs - 1) + ns * ((s - 1) + ns * sh)]);
+      }
+      part[r] = sum;
+    }
+  }
+  double e[4];
+#pragma unroll
+  for (int ev = 0; ev < 4; ++ev) {
+    double acc = 0.0;
+    for (int sh = 0; sh < nsh; ++sh) {
+      const int c = ev * nsh + sh;
+      double v = c < 32 ? __shfl_sync(kFull, part[0], c) : __shfl_sync(kFull, part[1], c - 32);
+      acc = sh == 0 ? v : __dadd_rn(acc, v);
+    }
+    e[ev] = acc;
+  }
+  e_un = __dadd_rn(e[0], e[1]);
+  e_sw = __dadd_rn(e[2], e[3]);
+}
+
+// FP32 filter of u < exp(-beta*dE) for a fixed-point dE > band.
+// Returns 1 accept, 0 reject, -1 undecided.
+__device__ __forceinline__ int fast_exp_decision(const ChainJob& J, int dE, uint32_t w) {
+  float xf = -__fmul_rn(J.beta_q, __int2float_rn(dE));
+  float D = fabsf(xf) * 2.0e-7f + J.beta_band * 1.0001f;
+  float M = 1.1f * D + 7.0e-7f;
+  if (!(M < 0.01f)) return -1;
+  if (xf < -40.0f) return w != 0u ? 0 : -1;
+  float thr = __fmul_rn(expf(xf), 4294967296.0f);
+  float wf = __uint2float_rn(w);
+  if (wf < __fmul_rn(thr, 1.0f - M)) return 1;
+  if (wf > __fmul_rn(thr, 1.0f + M)) return 0;
+  return -1;
+}
+
+}  // namespace brawl

@@ -1,0 +1,244 @@
+// lattice_ops.cu -- initial configurations, total energies and layout
+// conversions for batches of chains.
+#include "kernels.cuh"
+
+namespace brawl {
+
+// ---------------------------------------------------------------------------
+// initial_setup (src/initialise.F90:434-617).  The reference visits the
+// occupied sites in z, y, x order -- exactly the compact index order -- and
+// for each draws u until a species with quota left contains u in its
+// interval [sum(c(0:l-1)), sum(c(0:l))]; every species whose interval holds
+// u and whose quota is open is written in turn (the last one wins) and each
+// such write uses up one of its quota.  The interval tests are done exactly
+// on the 32-bit word: lo <= u <=> w >= lo_w, u <= hi <=> w <= hi_w.
+// One warp per chain; all lanes follow the same control flow so the whole
+// warp can regenerate the mt19937ar block when needed.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32) initial_setup_kernel(const InitJob* __restrict__ jobs) {
+  __shared__ uint32_t mt[kMTN];
+  __shared__ int64_t check[kMaxSpecies];
+  const InitJob& J = jobs[blockIdx.x];
+  const int lane = threadIdx.x;
+  for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
+  if (lane < kMaxSpecies) check[lane] = 0;
+  int pos = (int)J.rng[kMTN];
+  __syncwarp();
+  unsigned long long draws = 0;
+  const int ns = J.ns;
+  for (int site = 0; site < J.n_sites; ++site) {
+    int s = 0;
+    while (s == 0) {
+      const uint32_t w = __shfl_sync(kFull, mt_peek(mt, pos, 1, lane), 0);
+      pos += 1;
+      ++draws;
+      const int64_t wl = (int64_t)w;
+      for (int l = 0; l < ns; ++l) {
+        if (wl >= J.lo_w[l] && wl <= J.hi_w[l]) {
+          if (check[l] < J.counts[l]) {
+            s = l + 1;
+            __syncwarp();
+            if (lane == 0) check[l] += 1;
+            __syncwarp();
+          }
+        }
+      }
+      if (draws > (unsigned long long)J.n_sites * 4096ull + 1000000ull) {
+        // a quota that can never be met (the host validates the counts, so
+        // this only guards against a corrupted job)
+        if (lane == 0) *J.status = kStatusBadSpecies;
+        return;
+      }
+    }
+    if (lane == 0) J.lat[site] = (int8_t)s;
+  }
+  __syncwarp();
+  for (int i = lane; i < kMTN; i += 32) J.rng[i] = mt[i];
+  if (lane == 0) {
+    J.rng[kMTN] = (uint32_t)pos;
+    J.counters[kCntDraws] += draws;
+  }
+}
+
+void launch_initial_setup(const InitJob* d_jobs, int n_jobs, cudaStream_t stream) {
+  if (n_jobs > 0) initial_setup_kernel<<<n_jobs, 32, 0, stream>>>(d_jobs);
+}
+
+// ---------------------------------------------------------------------------
+// Site energies in the reference's order: each shell sum starts from 0.0
+// and adds V_ex(species, neighbour, shell) in list order; the shell sums are
+// added left to right (src/bw_hamiltonian.f90:898-1262, 1712-1910,
+// 2059-2106).  Grid-stride over (chain, site) pairs.
+// ---------------------------------------------------------------------------
+__device__ double site_energy_ref(const Geom& g, const int8_t* lat, const double* V,
+                                  const uint32_t* ents, const int16_t* sstart, int x, int y,
+                                  int z) {
+  const int cs = lat[compact_index(g, x, y, z)];
+  double total = 0.0;
+  for (int sh = 0; sh < g.nsh; ++sh) {
+    double e = 0.0;
+    for (int k = sstart[sh]; k < sstart[sh + 1]; ++k) {
+      int dx, dy, dz, shk;
+      unpack_entry(ents[k], dx, dy, dz, shk);
+      const int s = lat[neighbour_index(g, x, y, z, dx, dy, dz)];
+      e = __dadd_rn(e, V[(cs - 1) + g.ns * ((s - 1) + g.ns * sh)]);
+    }
+    total = sh == 0 ? e : __dadd_rn(total, e);
+  }
+  return total;
+}
+
+__global__ void site_energies_kernel(const EnergyJob* __restrict__ jobs, int n_jobs,
+                                     int64_t total_sites) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total_sites;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    // locate the chain by binary search on the site prefix
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].site_offset <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const EnergyJob& J = jobs[lo];
+    const int idx = (int)(t - J.site_offset);
+    int x, y, z;
+    decode_site(J.g, idx, x, y, z);
+    J.site_energy[idx] = site_energy_ref(J.g, J.lat, J.V, J.entries, J.shell_start, x, y, z);
+  }
+}
+
+// energy = energy + e(site) over sites in order, then 0.5 * energy.
+__global__ void sum_sites_kernel(const EnergyJob* __restrict__ jobs, int n_jobs) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_jobs) return;
+  const EnergyJob& J = jobs[c];
+  double energy = 0.0;
+  for (int i = 0; i < J.g.n_sites; ++i) energy = __dadd_rn(energy, J.site_energy[i]);
+  *J.out = __dmul_rn(0.5, energy);
+}
+
+void launch_total_energy(const EnergyJob* d_jobs, int n_jobs, int64_t total_sites,
+                         cudaStream_t stream) {
+  if (n_jobs <= 0) return;
+  int64_t blocks = (total_sites + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  site_energies_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_sites);
+  sum_sites_kernel<<<(n_jobs + 31) / 32, 32, 0, stream>>>(d_jobs, n_jobs);
+}
+
+__global__ void one_site_energy_kernel(const EnergyJob* __restrict__ job, int x, int y, int z,
+                                       double* out) {
+  *out = site_energy_ref(job->g, job->lat, job->V, job->entries, job->shell_start, x, y, z);
+}
+
+void launch_site_energy(const EnergyJob* d_job, int x, int y, int z, double* out,
+                        cudaStream_t stream) {
+  one_site_energy_kernel<<<1, 1, 0, stream>>>(d_job, x, y, z, out);
+}
+
+// ---------------------------------------------------------------------------
+// Layout conversions.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool occupied(const Geom& g, int x, int y, int z) {
+  if (g.lattice == kBcc) return ((x & 1) == (z & 1)) && ((y & 1) == (z & 1));
+  if (g.lattice == kFcc) return ((x + y + z) & 1) == 0;
+  return true;
+}
+
+__global__ void pack_kernel(Geom g, const int8_t* __restrict__ grid, int8_t* __restrict__ lat,
+                            int32_t* status) {
+  const int W1 = 2 * g.n1, W2 = 2 * g.n2, W3 = 2 * g.n3;
+  const int64_t total = (int64_t)W1 * W2 * W3;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(t % W1), y = (int)((t / W1) % W2), z = (int)(t / ((int64_t)W1 * W2));
+    const int8_t s = grid[t];
+    if (occupied(g, x, y, z)) {
+      lat[compact_index(g, x, y, z)] = s;
+      if (s < 1 || s > g.ns) *status = kStatusBadSpecies;
+    } else if (s != 0) {
+      *status = kStatusBadSpecies;
+    }
+  }
+}
+
+__global__ void unpack_kernel(Geom g, const int8_t* __restrict__ lat, int8_t* __restrict__ grid) {
+  const int W1 = 2 * g.n1, W2 = 2 * g.n2, W3 = 2 * g.n3;
+  const int64_t total = (int64_t)W1 * W2 * W3;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(t % W1), y = (int)((t / W1) % W2), z = (int)(t / ((int64_t)W1 * W2));
+    grid[t] = occupied(g, x, y, z) ? lat[compact_index(g, x, y, z)] : (int8_t)0;
+  }
+}
+
+void launch_pack(const Geom& g, const int8_t* d_grid, int8_t* d_lat, int32_t* d_status,
+                 cudaStream_t stream) {
+  const int64_t total = (int64_t)8 * g.n1 * g.n2 * g.n3;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  pack_kernel<<<blocks, 256, 0, stream>>>(g, d_grid, d_lat, d_status);
+}
+
+void launch_unpack(const Geom& g, const int8_t* d_lat, int8_t* d_grid, cudaStream_t stream) {
+  const int64_t total = (int64_t)8 * g.n1 * g.n2 * g.n3;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  unpack_kernel<<<blocks, 256, 0, stream>>>(g, d_lat, d_grid);
+}
+
+__device__ __forceinline__ int find_grid_job(const GridJob* jobs, int n, int64_t t) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].grid_offset <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void pack_batch_kernel(const GridJob* __restrict__ jobs, int n_jobs, int64_t total,
+                                  const int8_t* __restrict__ grids) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const GridJob& J = jobs[find_grid_job(jobs, n_jobs, t)];
+    const int64_t c = t - J.grid_offset;
+    const int W1 = 2 * J.g.n1, W2 = 2 * J.g.n2;
+    const int x = (int)(c % W1), y = (int)((c / W1) % W2), z = (int)(c / ((int64_t)W1 * W2));
+    const int8_t s = grids[t];
+    if (occupied(J.g, x, y, z)) {
+      J.lat[compact_index(J.g, x, y, z)] = s;
+      if (s < 1 || s > J.g.ns) *J.status = kStatusBadSpecies;
+    } else if (s != 0) {
+      *J.status = kStatusBadSpecies;
+    }
+  }
+}
+
+__global__ void unpack_batch_kernel(const GridJob* __restrict__ jobs, int n_jobs, int64_t total,
+                                    int8_t* __restrict__ grids) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const GridJob& J = jobs[find_grid_job(jobs, n_jobs, t)];
+    const int64_t c = t - J.grid_offset;
+    const int W1 = 2 * J.g.n1, W2 = 2 * J.g.n2;
+    const int x = (int)(c % W1), y = (int)((c / W1) % W2), z = (int)(c / ((int64_t)W1 * W2));
+    grids[t] = occupied(J.g, x, y, z) ? J.lat[compact_index(J.g, x, y, z)] : (int8_t)0;
+  }
+}
+
+void launch_pack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells,
+                       const int8_t* d_grids, cudaStream_t stream) {
+  int64_t blocks = (total_cells + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (n_jobs > 0) pack_batch_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_cells, d_grids);
+}
+
+void launch_unpack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells, int8_t* d_grids,
+                         cudaStream_t stream) {
+  int64_t blocks = (total_cells + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (n_jobs > 0) unpack_batch_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_cells, d_grids);
+}
+
+}  // namespace brawl

@@ -1,0 +1,99 @@
+"""Host driver of the Metropolis simulated annealing over the GPU chain.
+
+Mirrors metropolis_simulated_annealing (src/metropolis.F90:84-558): per
+temperature, the optional burn-in, the sample at step 0, n_sweeps blocks of
+n_sweep_steps swap trials on the device, and after each block the energy
+(total_energy), the ASRO sample (radial_densities) and the trajectory rows.
+The per-temperature averages use the reference's arithmetic: E and E^2
+accumulated in FP64 sample by sample, n_save_* = floor(real/real) in single
+precision, C clamped at zero.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import K_B_IN_RY, Chain
+
+
+def _f32_floor_div(a: int, b: int) -> int:
+    return int(np.floor(np.float32(a) / np.float32(b)))
+
+
+def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs: bool = True):
+    """Runs the annealing on a chain whose configuration and stream are
+    already set (initial_setup or a read configuration).  `metropolis` is a
+    MetropolisParams (brawl_gb300.inputs).  Returns per-temperature arrays and
+    the trajectory, with the keys the reference writes to its outputs."""
+    m = metropolis
+    ns = chain.setup.n_species
+    n_atoms = chain.setup.n_atoms
+    shells = chain.lattice_shells(wc_range)
+    n_save_energy = _f32_floor_div(m.n_mc_steps, m.n_sample_steps)
+    n_save_asro = _f32_floor_div(m.n_mc_steps, m.n_sample_steps_asro)
+    Ts = m.T_steps
+    out = {
+        "shells": shells,
+        "temperature": np.zeros(Ts), "energies_of_T": np.zeros(Ts), "C_of_T": np.zeros(Ts),
+        "acceptance_of_T": np.zeros(Ts), "rho_of_T": np.zeros((Ts, wc_range, ns, ns)),
+        "traj_step": [], "traj_energy": [], "traj_asro": [],
+        "initial_configs": [], "final_configs": [],
+    }
+    asro = np.zeros((wc_range, ns, ns))
+    for j in range(Ts):
+        r_dens = np.zeros((wc_range, ns, ns))
+        step_E = 0.0
+        step_Esq = 0.0
+        temp = m.T + float(j) * m.delta_T
+        sim_temp = temp * K_B_IN_RY
+        beta = 1.0 / sim_temp if sim_temp != 0.0 else float("inf")
+        out["temperature"][j] = temp
+        burn = m.burn_in_start if j == 0 else m.burn_in
+        if burn and m.n_burn_in_steps > 0:
+            chain.metropolis(beta, m.n_burn_in_steps, m.nbr_swap)
+        current_energy = 0.0
+        if m.calculate_energies:
+            current_energy = chain.total_energy()
+        if m.calculate_asro:
+            asro = chain.radial_densities(shells)
+        out["traj_step"].append(0)
+        out["traj_energy"].append(current_energy)
+        out["traj_asro"].append(asro.copy())
+        if record_configs:
+            out["initial_configs"].append(chain.config())
+        n_sweeps = m.n_mc_steps // m.n_sample_steps
+        n_sweep_steps = m.n_mc_steps // n_sweeps
+        accepted = 0
+        for i in range(1, n_sweeps + 1):
+            accepted += chain.metropolis(beta, n_sweep_steps, m.nbr_swap)
+            step_n = i * n_sweep_steps
+            if m.calculate_energies:
+                current_energy = chain.total_energy()
+                step_E = step_E + current_energy
+                step_Esq = step_Esq + current_energy * current_energy
+            if m.calculate_asro and step_n % m.n_sample_steps_asro == 0:
+                asro = chain.radial_densities(shells)
+                r_dens = r_dens + asro
+            if step_n % m.n_sample_steps_trajectory == 0:
+                out["traj_step"].append(step_n)
+                out["traj_energy"].append(current_energy)
+                out["traj_asro"].append(asro.copy())
+        # acceptance/real(n_mc_steps): the sum of 0/1 results is exact in FP64
+        out["acceptance_of_T"][j] = float(accepted) / float(np.float32(m.n_mc_steps))
+        if m.calculate_energies:
+            ne = float(n_save_energy)
+            out["energies_of_T"][j] = step_E / ne / float(n_atoms)
+            mean = step_E / ne
+            C = (step_Esq / ne - mean * mean) / (sim_temp * temp) / float(n_atoms)
+            if C < 0.0:
+                C = 0.0
+            if temp <= 0.0:
+                C = 0.0
+            out["C_of_T"][j] = C
+        if m.calculate_asro:
+            out["rho_of_T"][j] = r_dens / float(n_save_asro)
+        if record_configs:
+            out["final_configs"].append(chain.config())
+    out["traj_step"] = np.array(out["traj_step"], dtype=np.int64)
+    out["traj_energy"] = np.array(out["traj_energy"])
+    out["traj_asro"] = np.array(out["traj_asro"])
+    return out

@@ -1,0 +1,178 @@
+/*
+ * brawl_gpu.h -- C ABI of the GB300 (sm_103a) implementation of BraWl's
+ * lattice-sampling hot path.
+ *
+ * The entry points replace, call for call, the procedures that BraWl's
+ * Fortran host reaches through its procedure pointers and its one existing
+ * C binding.  Each declaration names the reference interface it replaces
+ * (paths relative to the BraWl repository root).  Everything is plain C:
+ * pointers, sizes and int status codes; no CUDA or C++ types cross the
+ * boundary, and every call is synchronous unless its name ends in _async.
+ *
+ * Data layouts are the reference's own (Fortran, column-major):
+ *   config  int8  config(1, 2*n_1, 2*n_2, 2*n_3), x fastest; empty sites 0,
+ *                 species 1..n_species (src/initialise.F90:286-298)
+ *   V_ex    double V_ex(n_species, n_species, interaction_range) in Ry
+ *                 (src/shared_data.f90:37, read by src/io.f90:389-402)
+ *   sites   int[4] (b, i, j, k), 1-based, as returned by *_random_site
+ *   rho     double rho(n_species, n_species, wc_range)
+ *
+ * Errors: the reference stops the program (e.g. src/initialise.F90:168,
+ * :205, :237); these functions return a status instead and leave their
+ * outputs untouched.  brawl_last_error() describes the most recent failure
+ * on the calling thread.
+ */
+#ifndef BRAWL_GPU_H
+#define BRAWL_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define BRAWL_OK 0
+#define BRAWL_EINVAL 1        /* unsupported lattice / shells / sizes / species */
+#define BRAWL_ENOMEM 2        /* device memory exhausted */
+#define BRAWL_ECUDA 3         /* CUDA runtime failure (no device, launch error) */
+#define BRAWL_ETIMEDOUT 4     /* a serving request did not finish in time */
+#define BRAWL_ECANCELLED 5    /* a serving request was cancelled */
+#define BRAWL_ESTATE 6        /* a device-side consistency check failed */
+
+/* ---- lattice codes (setup%lattice, src/initialise.F90:157-243) ----------- */
+#define BRAWL_SIMPLE_CUBIC 0  /* interaction_range 1-2 */
+#define BRAWL_BCC 1           /* interaction_range 1-10 */
+#define BRAWL_FCC 2           /* interaction_range 1-6 */
+
+/* The subset of run_params (src/derived_types.f90:56-100) the path needs. */
+typedef struct brawl_setup {
+    int lattice;              /* BRAWL_SIMPLE_CUBIC / BRAWL_BCC / BRAWL_FCC */
+    int n_1, n_2, n_3;        /* conventional cells per direction */
+    int n_species;            /* 1..15 */
+    int interaction_range;    /* coordination shells in the Hamiltonian */
+} brawl_setup;
+
+/* Counters returned per chain (all 64-bit):
+ *   [0] trials  [1] trials whose species differed  [2] 32-bit words drawn
+ *   [3] accepted  [4] trials that drew the acceptance uniform
+ *   [5] trials decided with the FP64 reference-order sums
+ *   [6] exp/log decisions that needed the FP64 libm value
+ *   [7] ... and the double-double value */
+#define BRAWL_NUM_COUNTERS 8
+
+const char *brawl_last_error(void);
+int brawl_version(void);
+
+/* ====================================================================== */
+/* Single chain: one simulation as the reference runs it in one process. */
+/* ====================================================================== */
+typedef struct brawl_ctx brawl_ctx;
+
+/* initialise_function_pointers + initialise_interaction + read_exchange
+ * (src/initialise.F90:153-257, :267-273; src/io.f90:389-402): validates the
+ * lattice and shell count and keeps V_ex on the device. */
+int brawl_ctx_create(const brawl_setup *setup, const double *V_ex, brawl_ctx **out);
+int brawl_ctx_destroy(brawl_ctx *ctx);
+/* Replace V_ex (same shape). */
+int brawl_set_interactions(brawl_ctx *ctx, const double *V_ex);
+
+/* init_genrand(seed) (src/mt19937ar.c:63-78) on the chain's own stream. */
+int brawl_seed(brawl_ctx *ctx, uint32_t seed);
+/* f90_init_genrand (src/mt19937ar.c:127-142): static seed 110179+11*rank or
+ * a time-based one; returns the seed used. */
+int brawl_f90_init_genrand(brawl_ctx *ctx, int seedtime, int my_rank, uint32_t job_id,
+                           uint32_t *seed_out);
+/* The generator state as the reference holds it: mt[624] then mti. */
+int brawl_rng_get(brawl_ctx *ctx, uint32_t state[625]);
+int brawl_rng_set(brawl_ctx *ctx, const uint32_t state[625]);
+/* n calls of genrand() (src/mt19937ar.c:121-125) from the chain's stream. */
+int brawl_genrand(brawl_ctx *ctx, int64_t n, double *out);
+
+/* config in and out, reference layout (see above). */
+int brawl_set_config(brawl_ctx *ctx, const int8_t *config);
+int brawl_get_config(brawl_ctx *ctx, int8_t *config);
+
+/* initial_setup (src/initialise.F90:434-617) on the device, consuming the
+ * chain's stream exactly as the reference does.  species_concentrations has
+ * n_species+1 entries with [0] = 0 (the reference's 0:n_species array) and
+ * is rewritten, as the reference rewrites it, when species_numbers (may be
+ * NULL) sums to the number of atoms. */
+int brawl_initial_setup(brawl_ctx *ctx, double *species_concentrations,
+                        const int64_t *species_numbers);
+
+/* total_energy (src/bw_hamiltonian.f90:58-81), bit-identical. */
+int brawl_total_energy(brawl_ctx *ctx, double *energy);
+/* nbr_energy of one site (the setup%nbr_energy pointer,
+ * src/derived_types.f90:90-98), 1-based (b, i, j, k). */
+int brawl_site_energy(brawl_ctx *ctx, const int idx[4], double *energy);
+/* pair_energy (src/bw_hamiltonian.f90:99-114). */
+int brawl_pair_energy(brawl_ctx *ctx, const int idx1[4], const int idx2[4], double *energy);
+
+/* n_trials calls of monte_carlo_step_lattice (nbr_swap = 0) or
+ * monte_carlo_step_nbr (nbr_swap = 1) at inverse temperature beta
+ * (src/metropolis.F90:751-891).  accepted (may be NULL) receives the sum of
+ * their accept results, i.e. what the reference adds to `acceptance`. */
+int brawl_metropolis_run(brawl_ctx *ctx, double beta, int64_t n_trials, int nbr_swap,
+                         int64_t *accepted);
+
+/* lattice_shells (src/analytics.f90:205-275) of the current config. */
+int brawl_lattice_shells(brawl_ctx *ctx, int wc_range, double *shells);
+/* radial_densities (src/analytics.f90:293-404), bit-identical. */
+int brawl_radial_densities(brawl_ctx *ctx, int wc_range, const double *shells, double *rho);
+
+/* Cumulative counters of this chain (BRAWL_NUM_COUNTERS values). */
+int brawl_counters(brawl_ctx *ctx, int64_t *counters);
+
+/* ====================================================================== */
+/* Batches: many independent chains (replicas, temperatures, walkers) of  */
+/* uneven lattice, species and shell counts, run together -- the          */
+/* reference's MPI replica ensemble (src/comms.F90:122-160) on one GPU.   */
+/* ====================================================================== */
+typedef struct brawl_batch brawl_batch;
+
+typedef struct brawl_chain_desc {
+    brawl_setup setup;
+    const double *V_ex;                    /* copied at create */
+    uint32_t seed;                         /* init_genrand seed of this chain */
+    double beta;                           /* 1/(k_B T) in 1/Ry */
+    int nbr_swap;
+    const double *species_concentrations;  /* n_species+1 ([0] = 0) */
+    const int64_t *species_numbers;        /* n_species or NULL */
+    const int8_t *config;                  /* start config, or NULL for initial_setup */
+} brawl_chain_desc;
+
+/* Seeds every chain, then sets its configuration (copying `config`, or by
+ * initial_setup on the device when config is NULL). */
+int brawl_batch_create(const brawl_chain_desc *chains, int n_chains, brawl_batch **out);
+int brawl_batch_destroy(brawl_batch *batch);
+int brawl_batch_size(brawl_batch *batch, int *n_chains);
+/* New inverse temperatures, one per chain. */
+int brawl_batch_set_beta(brawl_batch *batch, const double *beta);
+/* n_trials[c] Metropolis trials on every chain c, all chains in one launch.
+ * accepted (may be NULL) receives each chain's accept sum for this call. */
+int brawl_batch_metropolis_run(brawl_batch *batch, const int64_t *n_trials, int64_t *accepted);
+/* Same, queued on `stream` (a cudaStream_t, or NULL for the batch's own
+ * stream) without waiting; brawl_batch_sync waits for it. */
+int brawl_batch_metropolis_run_async(brawl_batch *batch, const int64_t *n_trials, void *stream);
+int brawl_batch_sync(brawl_batch *batch);
+/* The plain path: chains run one at a time, one launch per chain. */
+int brawl_batch_metropolis_run_serial(brawl_batch *batch, const int64_t *n_trials,
+                                      int64_t *accepted);
+int brawl_batch_total_energy(brawl_batch *batch, double *energies);
+int brawl_batch_get_config(brawl_batch *batch, int chain, int8_t *config);
+int brawl_batch_set_config(brawl_batch *batch, int chain, const int8_t *config);
+/* Every chain's config at once: the reference-layout grids of all chains
+ * concatenated in chain order (the host side of the ensemble). */
+int brawl_batch_get_configs(brawl_batch *batch, int8_t *configs);
+int brawl_batch_set_configs(brawl_batch *batch, const int8_t *configs);
+int brawl_batch_rng_get(brawl_batch *batch, int chain, uint32_t state[625]);
+int brawl_batch_counters(brawl_batch *batch, int64_t *counters /* n_chains * 8 */);
+int brawl_batch_radial_densities(brawl_batch *batch, int chain, int wc_range,
+                                 const double *shells, double *rho);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BRAWL_GPU_H */

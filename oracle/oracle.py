@@ -22,10 +22,11 @@ LATTICE_IDS = {"simple_cubic": SC, "sc": SC, "bcc": BCC, "fcc": FCC}
 
 def build(ref: bool = False) -> None:
     """Compile liboracle.so (and, with ref=True, the reference's own
-    mt19937ar.c into _ref/) with the committed Makefile."""
+    mt19937ar.c into _ref/ where its sources are present) with the committed
+    Makefile."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref-if-present"], check=True)
 
 
 class Rng(C.Structure):

@@ -1,0 +1,281 @@
+"""GPU parity of the Metropolis path against the reference goldens and the
+oracle, through the C ABI (bit-exact: configurations, energies, streams,
+accept counts)."""
+import zlib
+
+import numpy as np
+import pytest
+
+import brawl_gb300 as B
+from brawl_gb300 import inputs as I
+from brawl_gb300 import metropolis as MET
+from brawl_gb300 import output as OUT
+from oracle import oracle as O
+from tests import golden_io as G
+
+pytestmark = pytest.mark.gpu
+
+RY_TO_EV = 13.605693122
+
+
+def random_V(rng, ns, nsh, scale_ev=0.05):
+    """Symmetric V_ex per shell, uniform[-scale, scale] eV, in Ry."""
+    V = np.zeros((ns, ns, nsh))
+    for sh in range(nsh):
+        a = rng.uniform(-scale_ev, scale_ev, size=(ns, ns))
+        V[:, :, sh] = np.triu(a) + np.triu(a, 1).T
+    return V / RY_TO_EV
+
+
+def equi_numbers(n_atoms, ns):
+    base = np.full(ns, n_atoms // ns, dtype=np.int64)
+    base[: n_atoms - base.sum()] += 1
+    return base
+
+
+def conc_vector(ns):
+    c = np.zeros(ns + 1)
+    c[1:] = 1.0 / ns
+    return c
+
+
+# ---------------------------------------------------------------------------
+# goldens through the GPU
+# ---------------------------------------------------------------------------
+MET = [("01_serial_metropolis", 0)] + [("02_parallel_metropolis", r) for r in range(4)]
+
+
+@pytest.mark.parametrize("test,rank", MET)
+def test_golden_anneal_on_gpu(test, rank):
+    p, V = G.load_inputs(test)
+    m = I.read_metropolis_file(G.path(test, "metropolis.inp"))
+    ch = B.Chain(B.Setup.from_run_params(p), V)
+    seed = ch.f90_init_genrand(0, rank)
+    assert seed == 110179 + 11 * rank
+    ch.initial_setup(p.species_concentrations, p.numbers_or_none())
+    out = MET.simulated_annealing(ch, m, p.wc_range)
+    tag = "proc_%04d" % rank
+    assert np.array_equal(out["initial_configs"][0],
+                          G.config_zyx(test, tag + "_initial_config_at_0300.0.npz"))
+    assert np.array_equal(out["final_configs"][0],
+                          G.config_zyx(test, tag + "_final_config_at_0300.0.npz"))
+    lines = [OUT.energy_trajectory_header()] + [
+        OUT.energy_trajectory_line(s, e) for s, e in zip(out["traj_step"], out["traj_energy"])]
+    assert lines == G.text(test, tag + "_energy_trajectory_at_T_0300.0.dat")
+    lines = [OUT.asro_trajectory_header()] + [
+        OUT.asro_trajectory_line(s, a) for s, a in zip(out["traj_step"], out["traj_asro"])]
+    assert lines == G.text(test, tag + "_asro_trajectory_at_T_0300.0.dat")
+    rho = G.npz(test, tag + "_rho_of_T.npz")
+    assert np.array_equal(rho["rho_data"], out["rho_of_T"])
+    assert np.array_equal(rho["r_data"], out["shells"])
+    assert np.array_equal(rho["U_data"], out["energies_of_T"])
+    if test.startswith("02"):
+        diag = OUT.diagnostics_lines(out["temperature"], out["energies_of_T"], out["C_of_T"],
+                                     out["acceptance_of_T"])
+        assert diag == G.text(test, tag + "_energy_diagnostics.dat")
+
+
+# ---------------------------------------------------------------------------
+# trial-level parity with the oracle
+# ---------------------------------------------------------------------------
+SYSTEMS = [
+    # lattice, n, ns, nsh, T, trials, nbr_swap
+    ("fcc", (4, 4, 4), 2, 2, 300.0, 60000, False),
+    ("fcc", (3, 4, 5), 5, 6, 1500.0, 40000, False),
+    ("bcc", (4, 4, 4), 4, 6, 100.0, 60000, False),
+    ("bcc", (3, 5, 4), 3, 10, 800.0, 30000, False),
+    ("bcc", (6, 6, 6), 4, 4, 3000.0, 40000, True),
+    ("fcc", (2, 2, 2), 3, 6, 500.0, 20000, False),   # neighbours wrap more than once
+    ("bcc", (1, 2, 1), 2, 10, 500.0, 5000, False),   # offsets reach the site itself
+    ("simple_cubic", (3, 3, 3), 2, 2, 400.0, 20000, False),
+    ("simple_cubic", (2, 3, 4), 3, 1, 50.0, 20000, True),
+    ("fcc", (4, 4, 4), 4, 3, 5.0, 30000, False),     # nearly every uphill move rejected
+]
+
+
+def _oracle_run(lattice, n, V, seed, T, trials, nbr_swap, conc, nums):
+    mod = O.OracleModel(lattice, *n, V)
+    r = O.OracleRng(seed)
+    cfg, conc2 = mod.initial_setup(r, conc, nums)
+    beta = 1.0 / (T * B.K_B_IN_RY)
+    acc, c = mod.mc_run(cfg, r, beta, trials, nbr_swap)
+    return mod, cfg, r, acc, c, beta
+
+
+@pytest.mark.parametrize("system", SYSTEMS, ids=lambda s: f"{s[0]}-{s[1]}-s{s[2]}-sh{s[3]}-T{s[4]}")
+def test_metropolis_matches_oracle(system):
+    lattice, n, ns, nsh, T, trials, nbr = system
+    rng = np.random.default_rng(zlib.crc32(repr(system).encode()))
+    V = random_V(rng, ns, nsh)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    nums = equi_numbers(setup.n_atoms, ns)
+    seed = int(rng.integers(1, 2**31))
+    mod, cfg, r, acc, c, beta = _oracle_run(lattice, n, V, seed, T, trials, nbr, conc_vector(ns), nums)
+    ch = B.Chain(setup, V)
+    ch.seed(seed)
+    ch.initial_setup(conc_vector(ns), nums)
+    # split the run in uneven chunks: state must carry across calls
+    acc_gpu = 0
+    for chunk in (trials // 3, trials // 7, trials - trials // 3 - trials // 7):
+        acc_gpu += ch.metropolis(beta, chunk, nbr)
+    assert acc_gpu == acc
+    assert np.array_equal(ch.config(), cfg)
+    cnt = ch.counters()
+    assert cnt["trials"] == c.trials and cnt["evaluated"] == c.evaluated
+    assert cnt["accepted"] == c.accepted and cnt["exp_tests"] == c.exp_tests
+    # the streams continue identically
+    assert np.array_equal(ch.genrand(1500), np.array([r.uniform() for _ in range(1500)]))
+    assert ch.total_energy() == mod.total_energy(cfg)
+
+
+def test_all_moves_on_the_exact_tier():
+    """With every V equal, every swap's dE is exactly zero: each evaluated
+    trial needs the FP64 reference-order sums (dE == 0 draws, exp(-0) = 1)."""
+    setup = B.Setup("fcc", 3, 3, 3, 3, 3)
+    V = np.full((3, 3, 3), 0.0123)
+    nums = equi_numbers(setup.n_atoms, 3)
+    mod, cfg, r, acc, c, beta = _oracle_run("fcc", (3, 3, 3), V, 99, 300.0, 5000, False,
+                                            conc_vector(3), nums)
+    ch = B.Chain(setup, V)
+    ch.seed(99)
+    ch.initial_setup(conc_vector(3), nums)
+    assert ch.metropolis(beta, 5000) == acc
+    assert np.array_equal(ch.config(), cfg)
+    cnt = ch.counters()
+    assert cnt["exact_path"] == cnt["evaluated"] > 0
+
+
+def test_zero_interactions_and_infinite_beta():
+    """V = 0: dE is +0 exactly, the move draws and exp(-beta*0) decides; at
+    T = 0 beta is +inf and -inf*0 is NaN, so every such move is rejected."""
+    setup = B.Setup("bcc", 3, 3, 3, 2, 2)
+    V = np.zeros((2, 2, 2))
+    nums = equi_numbers(setup.n_atoms, 2)
+    for beta in (1000.0, float("inf")):
+        mod = O.OracleModel("bcc", 3, 3, 3, V)
+        r = O.OracleRng(7)
+        cfg, _ = mod.initial_setup(r, conc_vector(2), nums)
+        acc, c = mod.mc_run(cfg, r, beta, 3000)
+        ch = B.Chain(setup, V)
+        ch.seed(7)
+        ch.initial_setup(conc_vector(2), nums)
+        assert ch.metropolis(beta, 3000) == acc
+        assert np.array_equal(ch.config(), cfg)
+
+
+def test_batch_equals_individual_and_serial():
+    """Chains of different lattices, sizes, species and shells run together
+    in one launch give exactly what each gives alone (and what the oracle
+    gives); the one-chain-per-launch path gives the same."""
+    rng = np.random.default_rng(5)
+    specs = [("bcc", (4, 4, 4), 4, 6), ("fcc", (3, 3, 3), 2, 2), ("bcc", (6, 5, 4), 3, 10),
+             ("fcc", (5, 5, 5), 5, 3), ("simple_cubic", (3, 3, 3), 2, 2), ("bcc", (2, 2, 2), 4, 5)]
+    chains, expect = [], []
+    for k, (lat, n, ns, nsh) in enumerate(specs):
+        V = random_V(rng, ns, nsh)
+        T = float(rng.uniform(100, 3000))
+        setup = B.Setup(lat, *n, ns, nsh)
+        nums = equi_numbers(setup.n_atoms, ns)
+        seed = 110179 + 11 * k
+        beta = 1.0 / (T * B.K_B_IN_RY)
+        chains.append(dict(setup=setup, V=V, seed=seed, beta=beta,
+                           species_concentrations=conc_vector(ns), species_numbers=nums))
+        trials = 7 * setup.n_atoms
+        mod, cfg, r, acc, c, _ = _oracle_run(lat, n, V, seed, T, trials, False, conc_vector(ns), nums)
+        expect.append((trials, cfg, acc, mod.total_energy(cfg)))
+    trials = np.array([e[0] for e in expect])
+    b = B.Batch(chains)
+    acc = b.metropolis(trials)
+    energies = b.total_energy()
+    b2 = B.Batch(chains)
+    acc2 = b2.metropolis_serial(trials)
+    for k, (t, cfg, a, e) in enumerate(expect):
+        assert acc[k] == a and acc2[k] == a
+        assert np.array_equal(b.config(k), cfg) and np.array_equal(b2.config(k), cfg)
+        assert energies[k] == e
+
+
+def test_initial_setup_modes_match_oracle():
+    rng = np.random.default_rng(11)
+    for lat, n, ns in (("fcc", (4, 3, 2), 5), ("bcc", (5, 5, 5), 3), ("simple_cubic", (2, 2, 3), 4)):
+        setup = B.Setup(lat, *n, ns, 1)
+        V = random_V(rng, ns, 1)
+        conc = np.zeros(ns + 1)
+        conc[1:] = rng.dirichlet(np.ones(ns))
+        for nums in (None, equi_numbers(setup.n_atoms, ns)):
+            mod = O.OracleModel(lat, *n, V)
+            r = O.OracleRng(1234)
+            cfg, conc_o = mod.initial_setup(r, conc, nums)
+            ch = B.Chain(setup, V)
+            ch.seed(1234)
+            conc_g = ch.initial_setup(conc, nums)
+            assert np.array_equal(ch.config(), cfg)
+            assert np.array_equal(conc_g, conc_o)
+            assert np.array_equal(ch.genrand(10), np.array([r.uniform() for _ in range(10)]))
+
+
+def test_energies_match_oracle():
+    rng = np.random.default_rng(3)
+    for lat, n, ns, nsh in (("bcc", (5, 4, 3), 4, 10), ("fcc", (4, 4, 4), 5, 6),
+                            ("simple_cubic", (3, 4, 2), 3, 2)):
+        V = random_V(rng, ns, nsh)
+        setup = B.Setup(lat, *n, ns, nsh)
+        mod = O.OracleModel(lat, *n, V)
+        r = O.OracleRng(42)
+        cfg, _ = mod.initial_setup(r, conc_vector(ns), equi_numbers(setup.n_atoms, ns))
+        ch = B.Chain(setup, V)
+        ch.set_config(cfg)
+        assert ch.total_energy() == mod.total_energy(cfg)
+        occ = np.argwhere(cfg != 0)[:20]
+        for z, y, x in occ:
+            idx = (1, x + 1, y + 1, z + 1)
+            assert ch.site_energy(idx) == mod.site_energy(cfg, x, y, z)
+        (z1, y1, x1), (z2, y2, x2) = occ[0], occ[-1]
+        assert ch.pair_energy((1, x1 + 1, y1 + 1, z1 + 1), (1, x2 + 1, y2 + 1, z2 + 1)) == \
+            mod.pair_energy(cfg, (x1, y1, z1), (x2, y2, z2))
+
+
+@pytest.mark.parametrize("lat,n,ns,wc", [("fcc", (4, 4, 4), 5, 3), ("bcc", (4, 4, 4), 4, 2),
+                                         ("bcc", (6, 7, 8), 3, 6), ("fcc", (2, 3, 2), 2, 8),
+                                         ("simple_cubic", (3, 3, 3), 2, 4),
+                                         ("bcc", (12, 12, 12), 4, 3)])
+def test_radial_densities_match_oracle(lat, n, ns, wc):
+    rng = np.random.default_rng(17)
+    V = random_V(rng, ns, 1)
+    setup = B.Setup(lat, *n, ns, 1)
+    mod = O.OracleModel(lat, *n, V)
+    r = O.OracleRng(77)
+    cfg, _ = mod.initial_setup(r, conc_vector(ns), equi_numbers(setup.n_atoms, ns))
+    shells = mod.lattice_shells(cfg, wc)
+    rho_o, _ = mod.radial_densities(cfg, shells)
+    ch = B.Chain(setup, V)
+    ch.set_config(cfg)
+    assert np.array_equal(ch.lattice_shells(wc), shells)
+    rho_g = ch.radial_densities(shells)
+    assert np.array_equal(rho_g, rho_o)
+
+
+def test_rng_interface_matches_reference_generator():
+    setup = B.Setup("fcc", 2, 2, 2, 2, 1)
+    ch = B.Chain(setup, np.zeros((2, 2, 1)))
+    for seed in (110179, 5489, 1, 4294967295):
+        ch.seed(seed)
+        r = O.OracleRng(seed)
+        assert np.array_equal(ch.genrand(2000), np.array([r.uniform() for _ in range(2000)]))
+    st = ch.rng_state()
+    ch.set_rng_state(st)
+    assert st[624] <= 624
+
+
+def test_invalid_inputs_return_status():
+    with pytest.raises(B.BrawlError) as e:
+        B.Chain(B.Setup("fcc", 2, 2, 2, 2, 7), np.zeros((2, 2, 7)))
+    assert e.value.code == 1
+    with pytest.raises(B.BrawlError):
+        B.Chain(B.Setup("bcc", 2, 2, 2, 2, 11), np.zeros((2, 2, 11)))
+    ch = B.Chain(B.Setup("fcc", 2, 2, 2, 2, 1), np.zeros((2, 2, 1)))
+    bad = np.zeros(ch.setup.grid_shape, dtype=np.int8)
+    with pytest.raises(B.BrawlError):
+        ch.set_config(bad)          # occupied sites must hold a species
+    with pytest.raises(B.BrawlError):
+        ch.initial_setup(np.array([0.0, 0.0, 0.0]))   # counts cannot reach n_atoms

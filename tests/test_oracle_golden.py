@@ -19,8 +19,8 @@ def test_mt19937_matches_reference_source():
     r = O.OracleRng(5489)
     words = [r.u32() for _ in range(10000)]
     assert words[9999] == 4123659995  # 10000th output for seed 5489
-    if os.path.exists("/root/reference/src/mt19937ar.c"):
-        O.build(ref=True)
+    O.build(ref=True)
+    if os.path.exists(O.REF_MT_PATH):
         for seed in (110179, 110190, 5489, 1):
             ref = O.reference_mt_words(seed, 3000)
             r = O.OracleRng(seed)
