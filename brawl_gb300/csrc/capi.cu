@@ -94,6 +94,48 @@ int make_geom(const brawl_setup& s, Geom& g) {
   return BRAWL_OK;
 }
 
+// Halo staging of an fcc/bcc lattice (halo_engine.cuh): halo widths from the
+// largest compact-index step of any entry at either parity; usable when the
+// images of a site are unique (2h <= N per axis), the pair-distance test is
+// exact (offsets within n per axis) and the difference table is staged.
+void make_halo(const Geom& g, HaloGeom& H, bool& ok) {
+  std::memset(&H, 0, sizeof(H));
+  ok = false;
+  if (g.lattice != kBcc && g.lattice != kFcc) return;
+  const int8_t(*offs)[3] = shell_offsets(g.lattice);
+  int hx = 0, hy = 0, hz = 0, dmx = 0, dmy = 0, dmz = 0;
+  for (int k = 0; k < g.z; ++k) {
+    const int dx = offs[k][0], dy = offs[k][1], dz = offs[k][2];
+    dmx = std::max(dmx, std::abs(dx));
+    dmy = std::max(dmy, std::abs(dy));
+    dmz = std::max(dmz, std::abs(dz));
+    for (int par = 0; par < 2; ++par) {
+      const int ddx = (par + dx) >> 1;
+      const int ddy = g.lattice == kBcc ? ((par + dy) >> 1) : dy;
+      hx = std::max(hx, std::abs(ddx));
+      hy = std::max(hy, std::abs(ddy));
+      hz = std::max(hz, std::abs(dz));
+    }
+  }
+  H.NX = g.n1;
+  H.NY = g.lattice == kBcc ? g.n2 : 2 * g.n2;
+  H.NZ = 2 * g.n3;
+  H.hx = hx;
+  H.hy = hy;
+  H.hz = hz;
+  H.SY = H.NX + 2 * hx;
+  H.SZ = (H.NY + 2 * hy) * H.SY;
+  const int64_t padded = (int64_t)(H.NZ + 2 * hz) * H.SZ;
+  H.origin = hz * H.SZ + hy * H.SY + hx;
+  H.dmx = dmx;
+  H.dmy = dmy;
+  H.dmz = dmz;
+  if (padded > (int64_t)1 << 30) return;
+  H.padded = (int32_t)padded;
+  ok = 2 * hx <= H.NX && 2 * hy <= H.NY && 2 * hz <= H.NZ && dmx <= g.n1 && dmy <= g.n2 &&
+       dmz <= g.n3 && smem_layout(g, false).use_D;
+}
+
 struct Model {
   Geom g;
   std::vector<double> V;
@@ -132,7 +174,7 @@ int make_model(const brawl_setup& s, const double* V_ex, Model& m) {
       for (int b = 1; b <= g.ns; ++b)
         for (int sh = 0; sh < g.nsh; ++sh) {
           double v = m.V[(a - 1) + g.ns * ((b - 1) + g.ns * sh)];
-          m.F[(a * nsp + b) * g.nsh + sh] = (int32_t)std::llrint(std::ldexp(v, m.S));
+          m.F[(a * g.nsh + sh) * nsp + b] = (int32_t)std::llrint(std::ldexp(v, m.S));
         }
     const int16_t* st = shell_starts(g.lattice);
     int kmax = 0;
@@ -143,6 +185,17 @@ int make_model(const brawl_setup& s, const double* V_ex, Model& m) {
   } else {
     m.S = 0;
     m.band = 0;
+  }
+  // D (see fixed_delta) follows F when it is small enough to stage
+  if (smem_layout(g, false).use_D) {
+    const size_t nF = m.F.size();
+    m.F.resize(nF + (size_t)nsp * nsp * g.nsh * nsp, 0);
+    for (int so = 1; so <= g.ns; ++so)
+      for (int sn = 1; sn <= g.ns; ++sn)
+        for (int sh = 0; sh < g.nsh; ++sh)
+          for (int b = 1; b <= g.ns; ++b)
+            m.F[nF + ((size_t)(so * nsp + sn) * g.nsh + sh) * nsp + b] =
+                m.F[(sn * g.nsh + sh) * nsp + b] - m.F[(so * g.nsh + sh) * nsp + b];
   }
   const int16_t* st = shell_starts(g.lattice);
   const int8_t(*offs)[3] = shell_offsets(g.lattice);
@@ -163,6 +216,7 @@ void set_beta(ChainJob& j, const Model& m, double beta) {
   float bf = (float)bb;
   if ((double)bf < bb) bf = std::nextafter(bf, INFINITY);
   j.beta_band = bf;
+  j.beta_q_l2 = (float)(beta * q * 1.4426950408889634);
 }
 
 // init_genrand (src/mt19937ar.c:63-78)
@@ -271,6 +325,14 @@ struct brawl_batch {
   cudaStream_t stream = nullptr;
   uint32_t smem_bytes = 0;
   bool smem_lat = true;
+  bool use_D = true;
+  int max_z = 0;
+  // chains run by the halo kernel, and its shared-memory size / unrolling
+  std::vector<int> halo;
+  uint32_t halo_smem = 0;
+  int halo_max_z = 0;
+  std::vector<ChainJob> staged;          // jobs in launch order
+  int n_halo_launch = 0;
   std::vector<unsigned long long> last_counters;
   int device = 0;
 };
@@ -305,8 +367,23 @@ int ensure_grid(brawl_batch* b, size_t bytes) {
   return BRAWL_OK;
 }
 
+// Jobs go to the device in launch order: halo chains first, then the rest,
+// each group by decreasing trial count so the longest chains start first.
 int upload_jobs(brawl_batch* b) {
-  CUDA_TRY(cudaMemcpyAsync(b->d_jobs, b->jobs.data(), b->jobs.size() * sizeof(ChainJob),
+  const int n = (int)b->jobs.size();
+  std::vector<int> order(n);
+  for (int c = 0; c < n; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    if (b->halo[x] != b->halo[y]) return b->halo[x] > b->halo[y];
+    return b->jobs[x].n_trials > b->jobs[y].n_trials;
+  });
+  b->staged.resize(n);
+  b->n_halo_launch = 0;
+  for (int k = 0; k < n; ++k) {
+    b->staged[k] = b->jobs[order[k]];
+    b->n_halo_launch += b->halo[order[k]];
+  }
+  CUDA_TRY(cudaMemcpyAsync(b->d_jobs, b->staged.data(), n * sizeof(ChainJob),
                            cudaMemcpyHostToDevice, b->stream));
   return BRAWL_OK;
 }
@@ -348,14 +425,22 @@ int run_metropolis(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, b
     CUDA_TRY(cudaStreamWaitEvent(stream, ev, 0));
     cudaEventDestroy(ev);
   }
+  const int nh = b->n_halo_launch;
   if (serial) {
-    for (int c = 0; c < n; ++c) {
-      launch_metropolis(b->d_jobs + c, 1, b->smem_lat, b->smem_bytes, stream);
+    for (int k = 0; k < n; ++k) {
+      if (k < nh)
+        launch_metropolis_halo(b->d_jobs + k, 1, b->halo_smem, b->halo_max_z, stream);
+      else
+        launch_metropolis(b->d_jobs + k, 1, b->smem_lat, b->use_D, b->smem_bytes, b->max_z,
+                          stream);
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(cudaStreamSynchronize(stream));
     }
   } else {
-    launch_metropolis(b->d_jobs, n, b->smem_lat, b->smem_bytes, stream);
+    if (nh > 0) launch_metropolis_halo(b->d_jobs, nh, b->halo_smem, b->halo_max_z, stream);
+    if (n - nh > 0)
+      launch_metropolis(b->d_jobs + nh, n - nh, b->smem_lat, b->use_D, b->smem_bytes, b->max_z,
+                        stream);
     CUDA_TRY(cudaGetLastError());
   }
   if (!wait) return BRAWL_OK;
@@ -401,9 +486,28 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
   int max_optin = 0;
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
   uint32_t need_smem = 0, need_gmem = 0;
-  for (auto& m : b->models) {
-    need_smem = std::max(need_smem, smem_layout(m.g, true).total);
-    need_gmem = std::max(need_gmem, smem_layout(m.g, false).total);
+  for (size_t c = 0; c < b->models.size(); ++c) {
+    HaloGeom H;
+    bool ok;
+    make_halo(b->models[c].g, H, ok);
+    if (ok && halo_layout(b->models[c].g, H).total <= (uint32_t)max_optin) continue;
+    need_smem = std::max(need_smem, smem_layout(b->models[c].g, true).total);
+    need_gmem = std::max(need_gmem, smem_layout(b->models[c].g, false).total);
+  }
+  b->halo.assign(n_chains, 0);
+  for (int c = 0; c < n_chains; ++c) {
+    const Model& m = b->models[c];
+    HaloGeom H;
+    bool ok;
+    make_halo(m.g, H, ok);
+    if (ok && halo_layout(m.g, H).total <= (uint32_t)max_optin) {
+      b->halo[c] = 1;
+      b->halo_smem = std::max(b->halo_smem, halo_layout(m.g, H).total);
+      b->halo_max_z = std::max(b->halo_max_z, (int)m.g.z);
+      continue;
+    }
+    b->max_z = std::max(b->max_z, (int)m.g.z);
+    if (!smem_layout(m.g, false).use_D) b->use_D = false;
   }
   b->smem_lat = need_smem <= (uint32_t)max_optin;
   b->smem_bytes = b->smem_lat ? need_smem : need_gmem;
@@ -459,6 +563,11 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
     ChainJob& j = b->jobs[c];
     std::memset(&j, 0, sizeof(j));
     j.g = m.g;
+    {
+      bool ok;
+      make_halo(m.g, j.hg, ok);
+      j.halo = b->halo[c];
+    }
     j.nbr_swap = b->nbr_swap[c];
     j.band = m.band;
     set_beta(j, m, chains[c].beta);

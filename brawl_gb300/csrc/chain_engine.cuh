@@ -66,19 +66,34 @@ struct Geom {
   int32_t pad;
 };
 
+// Halo layout of an fcc/bcc lattice staged in shared memory (see
+// halo_engine.cuh).
+struct HaloGeom {
+  int32_t NX, NY, NZ;     // compact extents
+  int32_t hx, hy, hz;     // halo widths
+  int32_t SY, SZ;         // padded strides (x stride 1)
+  int32_t padded;         // padded byte count
+  int32_t origin;         // hz*SZ + hy*SY + hx
+  int32_t dmx, dmy, dmz;  // largest |offset| component per axis (doubled grid)
+  int32_t pad;
+};
+
 // One chain's work order for a launch.  Plain data, shared with the host.
 struct ChainJob {
   Geom g;
+  HaloGeom hg;
   int32_t nbr_swap;
   int32_t band;               // decision band of the fixed-point tier, quanta
   double beta;
   float beta_q;               // beta * 2^-S (float)
   float beta_band;            // beta * band * 2^-S, rounded up (float)
+  float beta_q_l2;            // beta * 2^-S * log2(e) (float)
+  int32_t halo;               // 1: staged with a halo (halo kernel)
   int64_t n_trials;
   int8_t* lat;                // compact species array, n_sites bytes
   uint32_t* rng;              // mt[624], then the stream position
   const double* V;            // V_ex(a, b, shell), a fastest, ns*ns*nsh
-  const int32_t* F;           // fixed-point V: F[(a*(ns+1) + b)*nsh + shell]
+  const int32_t* F;           // fixed-point F then D tables (see fixed_delta)
   const uint32_t* entries;    // z packed neighbour entries (dx,dy,dz,shell)
   const int16_t* shell_start; // nsh + 1 entry offsets
   unsigned long long* counters;
@@ -108,7 +123,7 @@ __device__ __forceinline__ uint32_t mt_mix(uint32_t a, uint32_t b, uint32_t c) {
 // [454,624) read new words of the second phase (word 623 also reads the new
 // word 0, as the reference's last step does).  Each phase reads all of its
 // inputs before any lane writes.
-__device__ __forceinline__ void mt_twist_warp(uint32_t* mt, int lane) {
+static __device__ __noinline__ void mt_twist_warp(uint32_t* mt, int lane) {
   const int bounds[4] = {0, kMTN - kMTM, 2 * (kMTN - kMTM), kMTN};
 #pragma unroll
   for (int ph = 0; ph < 3; ++ph) {
@@ -271,51 +286,144 @@ struct SitePair {
 
 // ---------------------------------------------------------------------------
 // Fast tier: exact fixed-point energy change of swapping the two sites.
-// Lane entries: entry e in [0, 2z) belongs to site 1 for e < z and to site 2
-// otherwise; lane l owns entries l, l+32, ...
+//
+// Lanes 0-15 work on site 1 and lanes 16-31 on site 2; lane l owns the
+// site's neighbour entries (l & 15) + 16 j.  Neighbour addresses come from
+// three small per-axis tables in shared memory that map an unwrapped
+// coordinate t in [-kHalo, 2n + kHalo) straight to its wrapped contribution
+// to the compact index, so one neighbour costs three table loads and two
+// adds whatever the lattice and however far it wraps.  (For simple cubic an
+// axis with a zero offset keeps the site's own index, which the reference's
+// modulo-n wrap does not; those entries read identity tables instead.)
 // ---------------------------------------------------------------------------
-struct LaneEntries {
-  uint32_t e[kMaxLaneEntries];  // packed (dx,dy,dz,shell)
-  uint32_t site2_mask;          // bit j: entry j belongs to site 2
-  int n;
+constexpr int kHalo = 6;  // every neighbour offset component is within +-5
+
+struct AxisTables {
+  const int32_t* tx[2];  // [0] wrapping, [1] identity (simple-cubic zero offsets)
+  const int32_t* ty[2];
+  const int32_t* tz[2];
 };
 
-__device__ __forceinline__ void load_lane_entries(const uint32_t* ents, int z, int lane,
-                                                  LaneEntries& le) {
-  le.n = 0;
-  le.site2_mask = 0;
+// Fixed-point tables of the fast tier, in one int32 region of shared memory
+// (all indices below are element offsets into it):
+//   F[(a * nsh + shell) * (ns+1) + b]        = round(V_ex(a, b, shell) * 2^S)
+//   D[((so * (ns+1) + sn) * nsh + shell) * (ns+1) + b]
+//                                            = F(sn, b, shell) - F(so, b, shell)
+// D is the change of one neighbour term when its centre changes from so to
+// sn; only the partner site (whose own species changes too) needs F.
+template <int NJ>
+struct LanePlan {
+  int32_t ax[NJ], ay[NJ], az[NJ];  // element offsets of the entry's axis-table slot
+  int32_t shp[NJ];                 // shell * (ns + 1)
+  uint32_t valid;                  // bit j: entry j exists
+};
+
+template <int NJ>
+__device__ __forceinline__ void make_lane_plan(const Geom& g, const uint32_t* ents,
+                                               const int32_t* tabs_base, const AxisTables& T,
+                                               int lane, LanePlan<NJ>& P) {
+  const int sub = lane & 15;
+  const int nsp = g.ns + 1;
+  P.valid = 0;
 #pragma unroll
-  for (int j = 0; j < kMaxLaneEntries; ++j) {
-    int e = lane + 32 * j;
-    le.e[j] = 0;
-    if (e < 2 * z) {
-      int k = e < z ? e : e - z;
-      le.e[j] = ents[k];
-      if (e >= z) le.site2_mask |= 1u << j;
-      le.n = j + 1;
+  for (int j = 0; j < NJ; ++j) {
+    const int k = sub + 16 * j;
+    int dx = 0, dy = 0, dz = 0, sh = 0;
+    if (k < g.z) {
+      unpack_entry(ents[k], dx, dy, dz, sh);
+      P.valid |= 1u << j;
     }
+    const bool sc = g.lattice == kSimpleCubic;
+    const int ix = sc && dx == 0 ? 1 : 0;
+    const int iy = sc && dy == 0 ? 1 : 0;
+    const int iz = sc && dz == 0 ? 1 : 0;
+    P.ax[j] = (int32_t)(T.tx[ix] - tabs_base) + dx + kHalo;
+    P.ay[j] = (int32_t)(T.ty[iy] - tabs_base) + dy + kHalo;
+    P.az[j] = (int32_t)(T.tz[iz] - tabs_base) + dz + kHalo;
+    P.shp[j] = sh * nsp;
   }
 }
 
-__device__ __forceinline__ int fixed_delta(const Geom& g, const int8_t* lat, const int32_t* F,
-                                           const LaneEntries& le, const SitePair& p) {
+// Sum over this lane's entries of the change of its neighbour terms; the
+// warp total (returned in every lane) is the fixed-point swap delta.
+// Shared memory is addressed through the dynamic shared-memory symbols
+// themselves (element offsets, not pointers), so every access is a plain
+// 32-bit shared load the compiler can schedule freely.  I_off is the start
+// of the int32 region (axis tables, F, D) in int32 units; lat_off the byte
+// offset of the staged lattice (used when kSmemLat).
+//
+// This tier assumes neither site is a neighbour of the other (nor of
+// itself): `near` returns whether any lane met the partner, and the caller
+// then recomputes the trial with fixed_delta_general.
+template <int NJ, bool kSmemLat, bool kUseD>
+__device__ __forceinline__ int fixed_delta(const Geom& g, const int8_t* lat_g, int lat_off,
+                                           int I_off, int F_off, int D_off,
+                                           const LanePlan<NJ>& P, const SitePair& p, int lane,
+                                           bool& near) {
+  extern __shared__ int32_t s_i32[];
+  extern __shared__ int8_t s_i8[];
+  const bool h = lane >= 16;
+  const int cx = h ? p.bx : p.ax, cy = h ? p.by : p.ay, cz = h ? p.bz : p.az;
+  const int other = h ? p.ai : p.bi;
+  const int so = h ? p.sb : p.sa, sn = h ? p.sa : p.sb;
   const int nsp = g.ns + 1;
-  const int nsh = g.nsh;
+  const int rowD = I_off + D_off + (so * nsp + sn) * g.nsh * nsp;
+  const int rowN = I_off + F_off + sn * g.nsh * nsp;
+  const int rowO = I_off + F_off + so * g.nsh * nsp;
+  const int bx = I_off + cx, by = I_off + cy, bz = I_off + cz;
   int acc = 0;
+  bool hit = false;
 #pragma unroll
-  for (int j = 0; j < kMaxLaneEntries; ++j) {
-    if (j < le.n) {
-      const bool b = (le.site2_mask >> j) & 1u;
-      int dx, dy, dz, sh;
-      unpack_entry(le.e[j], dx, dy, dz, sh);
-      const int cx = b ? p.bx : p.ax, cy = b ? p.by : p.ay, cz = b ? p.bz : p.az;
-      const int own = b ? p.bi : p.ai, other = b ? p.ai : p.bi;
-      const int so = b ? p.sb : p.sa, sn = b ? p.sa : p.sb;
-      const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
-      const int s_before = lat[ni];
-      const int s_after = ni == other ? so : (ni == own ? sn : s_before);
-      acc += F[(sn * nsp + s_after) * nsh + sh] - F[(so * nsp + s_before) * nsh + sh];
-    }
+  for (int j = 0; j < NJ; ++j) {
+    const int ni = s_i32[P.ax[j] + bx] + s_i32[P.ay[j] + by] + s_i32[P.az[j] + bz];
+    const int s_before = kSmemLat ? (int)s_i8[lat_off + ni] : (int)lat_g[ni];
+    const int t = kUseD ? s_i32[rowD + P.shp[j] + s_before]
+                        : s_i32[rowN + P.shp[j] + s_before] - s_i32[rowO + P.shp[j] + s_before];
+    hit |= ni == other;
+    acc += ((P.valid >> j) & 1u) ? t : 0;
+  }
+  near = __any_sync(kFull, hit);
+  return __reduce_add_sync(kFull, acc);
+}
+
+// The same sum for any pair, including neighbouring sites and sites that
+// are their own neighbours on tiny lattices (the partner's term uses its new
+// species, a site's own term its new species).  Out of line and rebuilt
+// from the entry table so the hot loop's registers stay where they are.
+// tl0..tl2 are the axis-table lengths (the tables sit at the start of I).
+template <bool kSmemLat>
+__device__ __noinline__ int fixed_delta_general(int lattice, int ns, int nsh, int z,
+                                                const int8_t* lat_g, int lat_off,
+                                                int I_off, int F_off, int ents_off, int tl0,
+                                                int tl1, int tl2, int ax, int ay, int az, int ai,
+                                                int bx_, int by_, int bz_, int bi, int sa, int sb,
+                                                int lane) {
+  extern __shared__ int32_t s_i32[];
+  extern __shared__ int8_t s_i8[];
+  extern __shared__ uint32_t s_u32[];
+  const bool h = lane >= 16;
+  const int cx = h ? bx_ : ax, cy = h ? by_ : ay, cz = h ? bz_ : az;
+  const int own = h ? bi : ai, other = h ? ai : bi;
+  const int so = h ? sb : sa, sn = h ? sa : sb;
+  const int nsp = ns + 1;
+  const int rowN = I_off + F_off + sn * nsh * nsp;
+  const int rowO = I_off + F_off + so * nsh * nsp;
+  const bool sc = lattice == kSimpleCubic;
+  const int xw = I_off, xi = I_off + tl0;
+  const int yw = I_off + 2 * tl0, yi = yw + tl1;
+  const int zw = I_off + 2 * (tl0 + tl1), zi = zw + tl2;
+  int acc = 0;
+  for (int k = lane & 15; k < z; k += 16) {
+    int dx, dy, dz, sh;
+    unpack_entry(s_u32[ents_off / 4 + k], dx, dy, dz, sh);
+    const int tx = (sc && dx == 0) ? xi : xw;
+    const int ty = (sc && dy == 0) ? yi : yw;
+    const int tz = (sc && dz == 0) ? zi : zw;
+    const int ni = s_i32[tx + cx + dx + kHalo] + s_i32[ty + cy + dy + kHalo] +
+                   s_i32[tz + cz + dz + kHalo];
+    const int s_before = kSmemLat ? (int)s_i8[lat_off + ni] : (int)lat_g[ni];
+    const int s_after = ni == other ? so : (ni == own ? sn : s_before);
+    acc += s_i32[rowN + sh * nsp + s_after] - s_i32[rowO + sh * nsp + s_before];
   }
   return __reduce_add_sync(kFull, acc);
 }
@@ -325,7 +433,14 @@ __device__ __forceinline__ int fixed_delta(const Geom& g, const int8_t* lat, con
 // Chain c in [0, 4*nsh): evaluation c / nsh (0: site 1 before, 1: site 2
 // before, 2: site 1 after, 3: site 2 after), shell c % nsh.
 // ---------------------------------------------------------------------------
-__device__ inline void exact_pair_energies(const Geom& g, const int8_t* lat, const double* V,
+// Lattice accessors: species of canonical compact site i.
+struct CompactLat {
+  const int8_t* p;
+  __device__ __forceinline__ int operator()(int i) const { return p[i]; }
+};
+
+template <class Lat>
+__device__ inline void exact_pair_energies(const Geom& g, const Lat& lat, const double* V,
                                            const uint32_t* ents, const int16_t* sstart,
                                            const SitePair& p, int lane, double& e_un,
                                            double& e_sw) {
@@ -348,7 +463,7 @@ __device__ inline void exact_pair_energies(const Geom& g, const int8_t* lat, con
         int dx, dy, dz, shk;
         unpack_entry(ents[k], dx, dy, dz, shk);
         const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
-        int s = lat[ni];
+        int s = lat(ni);
         if (after) {
           if (ni == other) s = s_own_before;        // the partner now holds our old species
           else if (ni == own) s = s_own_after;
@@ -383,6 +498,23 @@ __device__ __forceinline__ int fast_exp_decision(const ChainJob& J, int dE, uint
   if (xf < -40.0f) return w != 0u ? 0 : -1;
   float thr = __fmul_rn(expf(xf), 4294967296.0f);
   float wf = __uint2float_rn(w);
+  if (wf < __fmul_rn(thr, 1.0f - M)) return 1;
+  if (wf > __fmul_rn(thr, 1.0f + M)) return 0;
+  return -1;
+}
+
+// The same filter in the base-2 domain: x2 = -beta*q*log2(e)*dE, 2^x2 with
+// exp2f (<= 2 ulp).  The argument's float rounding (3 roundings, relative
+// 1.8e-7 of |x2|, i.e. 1.25e-7 |x2| relative on 2^x2), the band term and the
+// libm's own error are covered by M.
+__device__ __forceinline__ int fast_exp2_decision(float beta_q_l2, float beta_band, int dE,
+                                                  uint32_t w) {
+  const float x2 = -__fmul_rn(beta_q_l2, __int2float_rn(dE));
+  const float M = fabsf(x2) * 1.5e-7f + beta_band * 1.01f + 8.0e-7f;
+  if (!(M < 0.01f)) return -1;
+  if (x2 < -57.5f) return w != 0u ? 0 : -1;
+  const float thr = __fmul_rn(exp2f(x2), 4294967296.0f);
+  const float wf = __uint2float_rn(w);
   if (wf < __fmul_rn(thr, 1.0f - M)) return 1;
   if (wf > __fmul_rn(thr, 1.0f + M)) return 0;
   return -1;

@@ -1,0 +1,244 @@
+// halo_engine.cuh -- the fast per-trial machinery for fcc and bcc chains
+// whose lattice fits in shared memory with a periodic halo.
+//
+// Lattice.  The compact lattice (Z, Y', X') = (z, y >> ys, x >> xs) is
+// staged with a halo of (hz, hy, hx) cells on each side holding the periodic
+// images, so every neighbour of a site is base(site) + delta[j] with no
+// wrapping: delta depends only on the entry and on the site's parity (the
+// x >> 1 of the compact layout).  A swap writes the two sites and their
+// images (at most 8 copies each).
+//
+// Stream.  mt19937ar words are consumed from a ring of two tempered blocks
+// (tbuf); a block is generated (twist + temper) when the consumer gets
+// within a trial of the end of the generated words, so a trial reads its
+// words with plain shared loads.  The state written back is the reference's
+// (mt[624], mti): when consumption is still in the older block, that block's
+// untempered words are recovered by inverting the tempering.
+#pragma once
+
+#include "chain_engine.cuh"
+
+namespace brawl {
+
+
+// ---------------------------------------------------------------------------
+// tempered ring
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t mt_untemper(uint32_t y) {
+  // inverse of mt_temper, step by step from the last
+  y ^= y >> 18;
+  y ^= (y << 15) & 0xefc60000u;
+  // y ^= (y << 7) & 0x9d2c5680: recover 7 bits at a time
+  uint32_t t = y;
+  t = y ^ ((t << 7) & 0x9d2c5680u);
+  t = y ^ ((t << 7) & 0x9d2c5680u);
+  t = y ^ ((t << 7) & 0x9d2c5680u);
+  t = y ^ ((t << 7) & 0x9d2c5680u);
+  y = t;
+  // y ^= y >> 11
+  t = y ^ (y >> 11);
+  y = y ^ (t >> 11);
+  return y;
+}
+
+// Ring of two tempered blocks in tbuf[0, 1248), plus a mirror of the first
+// 8 words at tbuf[1248, 1256) so a trial's words never wrap.  `idx` is the
+// ring slot of the next word, `avail` the generated words not yet consumed
+// (0..1248), `next_half` the half the next generated block goes to; mt holds
+// the newest generated block, untempered.
+constexpr int kRing = 2 * kMTN;
+constexpr int kRingMirror = 8;
+
+struct Ring {
+  int idx;
+  int avail;
+  int next_half;
+};
+
+// Twists mt in place and tempers the new block into the ring half next_half.
+__device__ __noinline__ void ring_generate(uint32_t* mt, uint32_t* tbuf, int next_half,
+                                           int lane) {
+  mt_twist_warp(mt, lane);
+  uint32_t* dst = tbuf + next_half * kMTN;
+  for (int i = lane; i < kMTN; i += 32) dst[i] = mt_temper(mt[i]);
+  if (next_half == 0 && lane < kRingMirror) tbuf[kRing + lane] = mt_temper(mt[lane]);
+  __syncwarp();
+}
+
+// The block in mt is current with mti = pos0 (0..624): temper it into half 0.
+__device__ __forceinline__ void ring_init(const uint32_t* mt, uint32_t* tbuf, int pos0, int lane,
+                                          Ring& R) {
+  for (int i = lane; i < kMTN; i += 32) tbuf[i] = mt_temper(mt[i]);
+  if (lane < kRingMirror) tbuf[kRing + lane] = mt_temper(mt[lane]);
+  R.idx = pos0;
+  R.avail = kMTN - pos0;
+  R.next_half = 1;
+  __syncwarp();
+}
+
+// Makes n <= 8 words available from R.idx.  A block is only generated when
+// fewer than n remain, so the half it overwrites has been consumed.
+__device__ __forceinline__ void ring_ensure(uint32_t* mt, uint32_t* tbuf, Ring& R, int n,
+                                            int lane) {
+  if (R.avail < n) {
+    ring_generate(mt, tbuf, R.next_half, lane);
+    R.avail += kMTN;
+    R.next_half ^= 1;
+  }
+}
+
+__device__ __forceinline__ void ring_consume(Ring& R, int n) {
+  R.idx += n;
+  R.idx = R.idx >= kRing ? R.idx - kRing : R.idx;
+  R.avail -= n;
+}
+
+// Writes (mt, mti) in the reference's form.  If the next word lies in the
+// block before the newest one, that block is recovered by untempering.
+__device__ inline void ring_writeback(const uint32_t* mt, const uint32_t* tbuf, const Ring& R,
+                                      uint32_t* out, int lane) {
+  if (R.avail <= kMTN) {
+    for (int i = lane; i < kMTN; i += 32) out[i] = mt[i];
+    if (lane == 0) out[kMTN] = (uint32_t)(kMTN - R.avail);
+  } else {
+    const int older = R.next_half;  // the half after the newest is the older one
+    for (int i = lane; i < kMTN; i += 32) out[i] = mt_untemper(tbuf[older * kMTN + i]);
+    if (lane == 0) out[kMTN] = (uint32_t)(kRing - R.avail);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// halo lattice
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int halo_index(const HaloGeom& H, int Z, int Yp, int Xp) {
+  return H.origin + Z * H.SZ + Yp * H.SY + Xp;
+}
+
+// Fills the padded lattice from the compact one (every padded cell reads its
+// canonical cell).
+__device__ inline void halo_fill(const Geom& g, const HaloGeom& H, const int8_t* lat_c,
+                                 int8_t* lat_p, int lane) {
+  const int PX = H.NX + 2 * H.hx, PY = H.NY + 2 * H.hy, PZ = H.NZ + 2 * H.hz;
+  const int total = PX * PY * PZ;
+  for (int t = lane; t < total; t += 32) {
+    const int px = t % PX, py = (t / PX) % PY, pz = t / (PX * PY);
+    int X = px - H.hx, Y = py - H.hy, Z = pz - H.hz;
+    X = X < 0 ? X + H.NX : (X >= H.NX ? X - H.NX : X);
+    Y = Y < 0 ? Y + H.NY : (Y >= H.NY ? Y - H.NY : Y);
+    Z = Z < 0 ? Z + H.NZ : (Z >= H.NZ ? Z - H.NZ : Z);
+    lat_p[pz * H.SZ + py * H.SY + px] = lat_c[Z * g.sz + Y * g.sy + X];
+  }
+}
+
+// Copies the interior back to the compact lattice.
+__device__ inline void halo_store(const Geom& g, const HaloGeom& H, const int8_t* lat_p,
+                                  int8_t* lat_c, int lane) {
+  for (int t = lane; t < g.n_sites; t += 32) {
+    const int Z = t / g.sz, r = t - Z * g.sz, Y = r / g.sy, X = r - Y * g.sy;
+    lat_c[t] = lat_p[halo_index(H, Z, Y, X)];
+  }
+}
+
+// Writes species s at canonical (Z, Y', X') and at its images; lanes 8k..8k+7
+// handle site k (k = 0, 1) through the 8 combinations of images per axis.
+__device__ __forceinline__ void halo_write_pair(const HaloGeom& H, int8_t* lat_p, int lane,
+                                                int Za, int Ya, int Xa, int sa_new, int Zb,
+                                                int Yb, int Xb, int sb_new) {
+  if (lane < 16) {
+    const bool b = lane >= 8;
+    const int combo = lane & 7;
+    int Z = b ? Zb : Za, Y = b ? Yb : Ya, X = b ? Xb : Xa;
+    const int s = b ? sb_new : sa_new;
+    bool ok = true;
+    if (combo & 1) {
+      if (X < H.hx) X += H.NX;
+      else if (X >= H.NX - H.hx) X -= H.NX;
+      else ok = false;
+    }
+    if (combo & 2) {
+      if (Y < H.hy) Y += H.NY;
+      else if (Y >= H.NY - H.hy) Y -= H.NY;
+      else ok = false;
+    }
+    if (combo & 4) {
+      if (Z < H.hz) Z += H.NZ;
+      else if (Z >= H.NZ - H.hz) Z -= H.NZ;
+      else ok = false;
+    }
+    if (ok) lat_p[halo_index(H, Z, Y, X)] = (int8_t)s;
+  }
+  __syncwarp();
+}
+
+// Conservative test that site b may be within the interaction range of site
+// a (minimum-image displacement within the largest offsets on every axis).
+__device__ __forceinline__ bool pair_near(const Geom& g, const HaloGeom& H, int ax, int ay,
+                                          int az, int bx, int by, int bz) {
+  int dx = bx - ax, dy = by - ay, dz = bz - az;
+  const int W1 = 2 * g.n1, W2 = 2 * g.n2, W3 = 2 * g.n3;
+  dx = dx > g.n1 ? dx - W1 : (dx < -g.n1 ? dx + W1 : dx);
+  dy = dy > g.n2 ? dy - W2 : (dy < -g.n2 ? dy + W2 : dy);
+  dz = dz > g.n3 ? dz - W3 : (dz < -g.n3 ? dz + W3 : dz);
+  return abs(dx) <= H.dmx && abs(dy) <= H.dmy && abs(dz) <= H.dmz;
+}
+
+// Per-lane entry plan of the halo tier: for entry j of this lane's site, the
+// padded-index delta for the site's parity (0/1) and shell * (ns+1).
+template <int NJ>
+struct HaloPlan {
+  int32_t d0[NJ], d1[NJ];
+  int32_t shp[NJ];
+  uint32_t valid;
+};
+
+template <int NJ>
+__device__ __forceinline__ void make_halo_plan(const Geom& g, const HaloGeom& H,
+                                               const uint32_t* ents, int lane, HaloPlan<NJ>& P) {
+  const int sub = lane & 15;
+  P.valid = 0;
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int k = sub + 16 * j;
+    int dx = 0, dy = 0, dz = 0, sh = 0;
+    if (k < g.z) {
+      unpack_entry(ents[k], dx, dy, dz, sh);
+      P.valid |= 1u << j;
+    }
+#pragma unroll
+    for (int par = 0; par < 2; ++par) {
+      // parity: bcc the shared parity of x, y, z; fcc the parity of x
+      const int ddx = (par + dx) >> 1;                       // x is always halved
+      const int ddy = g.lattice == kBcc ? ((par + dy) >> 1) : dy;
+      const int dd = dz * H.SZ + ddy * H.SY + ddx;
+      if (par == 0) P.d0[j] = dd;
+      else P.d1[j] = dd;
+    }
+    P.shp[j] = sh * (g.ns + 1);
+  }
+}
+
+// Fixed-point swap delta for a pair that is not near: neighbours never
+// include the partner or the site itself.
+template <int NJ>
+__device__ __forceinline__ int halo_delta(const Geom& g, int lat_off, int D_off_abs,
+                                          const HaloPlan<NJ>& P, int base_a, int base_b, int par_a,
+                                          int par_b, int sa, int sb, int lane) {
+  extern __shared__ int32_t s_i32[];
+  extern __shared__ int8_t s_i8[];
+  const bool h = lane >= 16;
+  const int base = lat_off + (h ? base_b : base_a);
+  const bool par = h ? par_b : par_a;
+  const int so = h ? sb : sa, sn = h ? sa : sb;
+  const int nsp = g.ns + 1;
+  const int rowD = D_off_abs + (so * nsp + sn) * g.nsh * nsp;
+  int acc = 0;
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int s = s_i8[base + (par ? P.d1[j] : P.d0[j])];
+    const int t = s_i32[rowD + P.shp[j] + s];
+    acc += ((P.valid >> j) & 1u) ? t : 0;
+  }
+  return __reduce_add_sync(kFull, acc);
+}
+
+}  // namespace brawl

@@ -10,28 +10,78 @@
 namespace brawl {
 
 // Shared-memory layout of one chain's CTA, identical on host and device.
+// The int32 region I holds the six axis tables, then F, then (when small
+// enough) D.
 struct SmemLayout {
-  uint32_t mt, F, V, ents, sstart, lat, total;
+  uint32_t mt, V, ents, sstart, I, lat, total;
+  uint32_t tab_len[3];        // 2n + 2*kHalo per axis
+  int32_t F_off, D_off;       // element offsets in I
+  int32_t use_D;
 };
 
 __host__ __device__ inline uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 
+constexpr uint32_t kMaxDBytes = 12 * 1024;
+
 __host__ __device__ inline SmemLayout smem_layout(const Geom& g, bool lattice_in_smem) {
   SmemLayout L;
   const uint32_t nsp = (uint32_t)g.ns + 1;
+  const uint32_t nF = nsp * (uint32_t)g.nsh * nsp;
+  const uint32_t nD = nsp * nsp * (uint32_t)g.nsh * nsp;
   L.mt = 0;
-  L.F = L.mt + kMTN * 4;
-  L.V = align_up(L.F + nsp * nsp * (uint32_t)g.nsh * 4, 16);
+  L.V = align_up(L.mt + kMTN * 4, 16);
   L.ents = L.V + (uint32_t)(g.ns * g.ns * g.nsh) * 8;
   L.sstart = L.ents + (uint32_t)g.z * 4;
-  L.lat = align_up(L.sstart + (uint32_t)(g.nsh + 1) * 2, 16);
+  L.I = align_up(L.sstart + (uint32_t)(g.nsh + 1) * 2, 16);
+  L.tab_len[0] = 2 * (uint32_t)g.n1 + 2 * kHalo;
+  L.tab_len[1] = 2 * (uint32_t)g.n2 + 2 * kHalo;
+  L.tab_len[2] = 2 * (uint32_t)g.n3 + 2 * kHalo;
+  const uint32_t ntab = 2 * (L.tab_len[0] + L.tab_len[1] + L.tab_len[2]);
+  L.use_D = nD * 4 <= kMaxDBytes ? 1 : 0;
+  L.F_off = (int32_t)ntab;
+  L.D_off = (int32_t)(ntab + nF);
+  const uint32_t nI = ntab + nF + (L.use_D ? nD : 0);
+  L.lat = align_up(L.I + nI * 4, 16);
   L.total = lattice_in_smem ? align_up(L.lat + (uint32_t)g.n_sites, 16) : L.lat;
   return L;
 }
 
-// Metropolis swap trials, one warp (CTA) per chain.
-void launch_metropolis(const ChainJob* d_jobs, int n_jobs, bool lattice_in_smem,
-                       uint32_t smem_bytes, cudaStream_t stream);
+// Shared-memory layout of a chain staged with a halo (halo_engine.cuh).
+struct HaloLayout {
+  uint32_t mt, tbuf, V, ents, sstart, I, lat, total;
+  int32_t F_off, D_off;
+};
+
+constexpr int kTbufWords = 2 * kMTN + 8;
+
+__host__ __device__ inline HaloLayout halo_layout(const Geom& g, const HaloGeom& H) {
+  HaloLayout L;
+  const uint32_t nsp = (uint32_t)g.ns + 1;
+  const uint32_t nF = nsp * (uint32_t)g.nsh * nsp;
+  const uint32_t nD = nsp * nsp * (uint32_t)g.nsh * nsp;
+  L.mt = 0;
+  L.tbuf = align_up(kMTN * 4, 16);
+  L.V = align_up(L.tbuf + kTbufWords * 4, 16);
+  L.ents = L.V + (uint32_t)(g.ns * g.ns * g.nsh) * 8;
+  L.sstart = L.ents + (uint32_t)g.z * 4;
+  L.I = align_up(L.sstart + (uint32_t)(g.nsh + 1) * 2, 16);
+  L.F_off = 0;
+  L.D_off = (int32_t)nF;
+  L.lat = align_up(L.I + (nF + nD) * 4, 16);
+  L.total = align_up(L.lat + (uint32_t)H.padded, 16);
+  return L;
+}
+
+int lane_entries_for(int max_z);
+
+// Metropolis swap trials for chains staged with a halo (fcc/bcc that fit).
+void launch_metropolis_halo(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z,
+                            cudaStream_t stream);
+
+// Metropolis swap trials, one warp (CTA) per chain; max_z is the largest
+// neighbour count in the batch (it selects the unrolling of the fast tier).
+void launch_metropolis(const ChainJob* d_jobs, int n_jobs, bool lattice_in_smem, bool use_D,
+                       uint32_t smem_bytes, int max_z, cudaStream_t stream);
 
 // initial_setup (src/initialise.F90:434-617) on the device, one warp per
 // chain.  Per chain: counts[ns] species quotas, lo_w/hi_w[ns] the interval

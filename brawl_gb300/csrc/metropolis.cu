@@ -1,16 +1,85 @@
 // metropolis.cu -- Metropolis-Kawasaki swap trials for a batch of chains.
 //
 // Each CTA is one warp and owns one chain for the whole launch: it stages the
-// chain's lattice (compact uint8), its mt19937ar block and its interaction
-// tables in shared memory, runs n_trials of monte_carlo_step_lattice
-// (src/metropolis.F90:751-813) or monte_carlo_step_nbr (:829-891) in the
-// reference's order, and writes the state back.  A batch of one chain is the
-// plain one-chain-per-launch path; a batch of many is the batched path.
+// chain's lattice (compact uint8), its mt19937ar block, its interaction
+// tables and the per-axis wrap tables in shared memory, runs n_trials of
+// monte_carlo_step_lattice (src/metropolis.F90:751-813) or
+// monte_carlo_step_nbr (:829-891) in the reference's order, and writes the
+// state back.  A batch of one chain is the plain one-chain-per-launch path; a
+// batch of many is the batched path.
 #include "kernels.cuh"
 
 namespace brawl {
 
-template <bool kSmemLat>
+// Builds the wrapping and identity axis tables (see AxisTables).
+__device__ inline void build_axis_tables(const Geom& g, int32_t* tabs, const SmemLayout& L,
+                                         int lane, AxisTables& T) {
+  // tabs: the start of the int32 region I
+  int32_t* base = tabs;
+  const int n[3] = {g.n1, g.n2, g.n3};
+  const int W[3] = {g.W1, g.W2, g.W3};
+  for (int a = 0; a < 3; ++a) {
+    const int len = (int)L.tab_len[a];
+    int32_t* wrap = base;
+    int32_t* ident = base + len;
+    for (int i = lane; i < len; i += 32) {
+      const int t = i - kHalo;
+      int w = t % W[a];
+      w = w < 0 ? w + W[a] : w;
+      int vw, vi;
+      const int ti = t < 0 ? 0 : (t >= 2 * n[a] ? 2 * n[a] - 1 : t);
+      if (a == 0) {
+        vw = w >> g.xs;
+        vi = ti >> g.xs;
+      } else if (a == 1) {
+        vw = (w >> g.ys) * g.sy;
+        vi = (ti >> g.ys) * g.sy;
+      } else {
+        vw = w * g.sz;
+        vi = ti * g.sz;
+      }
+      wrap[i] = vw;
+      ident[i] = vi;
+    }
+    if (a == 0) {
+      T.tx[0] = wrap;
+      T.tx[1] = ident;
+    } else if (a == 1) {
+      T.ty[0] = wrap;
+      T.ty[1] = ident;
+    } else {
+      T.tz[0] = wrap;
+      T.tz[1] = ident;
+    }
+    base += 2 * len;
+  }
+}
+
+// The reference-order FP64 decision for one trial (rare: only when the
+// fixed-point value is within the band).  Kept out of line so the hot loop
+// stays small; reads the job from global memory.  Returns bit 0 accept,
+// bit 1 the acceptance uniform was drawn, bit 2 the FP64 libm tier was
+// needed, bit 3 the double-double tier.
+__device__ __noinline__ int exact_decision(const ChainJob* __restrict__ Jg, const int8_t* lat,
+                                           const double* V, const uint32_t* ents,
+                                           const int16_t* sstart, int ax, int ay, int az, int ai,
+                                           int bx, int by, int bz, int bi, int sa, int sb,
+                                           int lane, uint32_t wu) {
+  const Geom g = Jg->g;
+  SitePair p;
+  p.ax = ax; p.ay = ay; p.az = az; p.ai = ai;
+  p.bx = bx; p.by = by; p.bz = bz; p.bi = bi;
+  p.sa = sa; p.sb = sb;
+  double e_un, e_sw;
+  exact_pair_energies(g, CompactLat{lat}, V, ents, sstart, p, lane, e_un, e_sw);
+  const double delta_e = __dsub_rn(e_sw, e_un);
+  if (delta_e < 0.0) return 1;
+  DecideStats st = {0u, 0u};
+  const int acc = u_lt_exp(wu, __dmul_rn(-Jg->beta, delta_e), st);
+  return acc | 2 | (st.fp64 ? 4 : 0) | (st.cr ? 8 : 0);
+}
+
+template <int NJ, bool kSmemLat, bool kUseD>
 __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restrict__ jobs) {
   extern __shared__ __align__(16) unsigned char smem[];
   const ChainJob J = jobs[blockIdx.x];
@@ -18,7 +87,7 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
   const int lane = threadIdx.x;
   const SmemLayout L = smem_layout(g, kSmemLat);
   uint32_t* mt = reinterpret_cast<uint32_t*>(smem + L.mt);
-  int32_t* F = reinterpret_cast<int32_t*>(smem + L.F);
+  int32_t* I = reinterpret_cast<int32_t*>(smem + L.I);
   double* V = reinterpret_cast<double*>(smem + L.V);
   uint32_t* ents = reinterpret_cast<uint32_t*>(smem + L.ents);
   int16_t* sstart = reinterpret_cast<int16_t*>(smem + L.sstart);
@@ -26,9 +95,9 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
 
   // ---- stage state ------------------------------------------------------
   const int nsp = g.ns + 1;
-  const int nF = nsp * nsp * g.nsh, nV = g.ns * g.ns * g.nsh;
+  const int nF = nsp * nsp * g.nsh * (L.use_D ? 1 + nsp : 1), nV = g.ns * g.ns * g.nsh;
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
-  for (int i = lane; i < nF; i += 32) F[i] = J.F[i];
+  for (int i = lane; i < nF; i += 32) I[L.F_off + i] = J.F[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
   for (int i = lane; i < g.z; i += 32) ents[i] = J.entries[i];
   for (int i = lane; i <= g.nsh; i += 32) sstart[i] = J.shell_start[i];
@@ -39,16 +108,22 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
     for (int i = lane; i < n16; i += 32) dst[i] = src[i];
     for (int i = (n16 << 4) + lane; i < g.n_sites; i += 32) lat[i] = J.lat[i];
   }
+  AxisTables T;
+  build_axis_tables(g, I, L, lane, T);
   int pos = (int)J.rng[kMTN];
   __syncwarp();
 
-  LaneEntries le;
-  load_lane_entries(ents, g.z, lane, le);
+  LanePlan<NJ> P;
+  make_lane_plan<NJ>(g, ents, I, T, lane, P);
+  const int lat_off = (int)L.lat, I_off = (int)(L.I / 4);
+  // an entry can map a site onto itself only when a wrap period is within
+  // the offsets' reach
+  const bool self_map = g.W1 <= kHalo || g.W2 <= kHalo || g.W3 <= kHalo;
 
   const int n_peek = J.nbr_swap ? 5 : 7;
   const int n_base = J.nbr_swap ? 4 : 6;
   unsigned long long c_eval = 0, c_draws = 0, c_acc = 0, c_exp = 0, c_exact = 0;
-  DecideStats st = {0u, 0u};
+  unsigned int c_fp64 = 0, c_cr = 0;
   int status = kStatusOk;
 
   for (int64_t t = 0; t < J.n_trials; ++t) {
@@ -68,13 +143,18 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
     p.sa = lat[p.ai];
     p.sb = lat[p.bi];
     int consumed = n_base;
-    int accept;
-    if (p.sa == p.sb) {
-      // same species: accepted without an energy evaluation or a draw
-      accept = 1;
-    } else {
+    int accept = 1;  // same species: accepted without an energy evaluation or a draw
+    if (p.sa != p.sb) {
       ++c_eval;
-      const int dE = fixed_delta(g, lat, F, le, p);
+      bool near;
+      int dE = fixed_delta<NJ, kSmemLat, kUseD>(g, lat, lat_off, I_off, L.F_off, L.D_off, P, p,
+                                                lane, near);
+      if (near || self_map)
+        dE = fixed_delta_general<kSmemLat>(g.lattice, g.ns, g.nsh, g.z, lat, lat_off, I_off,
+                                           L.F_off, (int)L.ents,
+                                           (int)L.tab_len[0], (int)L.tab_len[1],
+                                           (int)L.tab_len[2], p.ax, p.ay, p.az, p.ai, p.bx, p.by,
+                                           p.bz, p.bi, p.sa, p.sb, lane);
       const uint32_t wu = __shfl_sync(kFull, w, n_base);
       accept = -1;
       if (dE < -J.band) {
@@ -86,16 +166,12 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
       if (accept < 0) {
         // decision inside the band: the reference's FP64 sums, in its order
         ++c_exact;
-        double e_un, e_sw;
-        exact_pair_energies(g, lat, V, ents, sstart, p, lane, e_un, e_sw);
-        const double delta_e = __dsub_rn(e_sw, e_un);
-        if (delta_e < 0.0) {
-          consumed = n_base;
-          accept = 1;
-        } else {
-          consumed = n_base + 1;
-          accept = u_lt_exp(wu, __dmul_rn(-J.beta, delta_e), st);
-        }
+        const int r = exact_decision(jobs + blockIdx.x, lat, V, ents, sstart, p.ax, p.ay, p.az,
+                                     p.ai, p.bx, p.by, p.bz, p.bi, p.sa, p.sb, lane, wu);
+        accept = r & 1;
+        consumed = (r & 2) ? n_base + 1 : n_base;
+        c_fp64 += (r >> 2) & 1;
+        c_cr += (r >> 3) & 1;
       }
       if (consumed > n_base) ++c_exp;
       if (accept && lane == 0) {
@@ -130,23 +206,46 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
     c[kCntAccepted] += c_acc;
     c[kCntExpTests] += c_exp;
     c[kCntExactPath] += c_exact;
-    c[kCntExpFp64] += st.fp64;
-    c[kCntExpCr] += st.cr;
+    c[kCntExpFp64] += c_fp64;
+    c[kCntExpCr] += c_cr;
     if (status != kStatusOk) *J.status = status;
   }
 }
 
-void launch_metropolis(const ChainJob* d_jobs, int n_jobs, bool lattice_in_smem,
-                       uint32_t smem_bytes, cudaStream_t stream) {
-  if (n_jobs <= 0) return;
-  if (lattice_in_smem) {
-    cudaFuncSetAttribute(metropolis_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem_bytes);
-    metropolis_kernel<true><<<n_jobs, 32, smem_bytes, stream>>>(d_jobs);
+template <int NJ, bool kSmemLat, bool kUseD>
+static void launch_one(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes,
+                       cudaStream_t stream) {
+  cudaFuncSetAttribute(metropolis_kernel<NJ, kSmemLat, kUseD>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  metropolis_kernel<NJ, kSmemLat, kUseD><<<n_jobs, 32, smem_bytes, stream>>>(d_jobs);
+}
+
+template <int NJ>
+static void launch_nj(const ChainJob* d_jobs, int n_jobs, bool smem_lat, bool use_D,
+                      uint32_t smem_bytes, cudaStream_t stream) {
+  if (smem_lat) {
+    if (use_D) launch_one<NJ, true, true>(d_jobs, n_jobs, smem_bytes, stream);
+    else launch_one<NJ, true, false>(d_jobs, n_jobs, smem_bytes, stream);
   } else {
-    cudaFuncSetAttribute(metropolis_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem_bytes);
-    metropolis_kernel<false><<<n_jobs, 32, smem_bytes, stream>>>(d_jobs);
+    if (use_D) launch_one<NJ, false, true>(d_jobs, n_jobs, smem_bytes, stream);
+    else launch_one<NJ, false, false>(d_jobs, n_jobs, smem_bytes, stream);
+  }
+}
+
+int lane_entries_for(int max_z) {
+  const int nj = (max_z + 15) / 16;
+  return nj <= 2 ? 2 : nj <= 4 ? 4 : nj <= 6 ? 6 : nj <= 8 ? 8 : 11;
+}
+
+void launch_metropolis(const ChainJob* d_jobs, int n_jobs, bool lattice_in_smem, bool use_D,
+                       uint32_t smem_bytes, int max_z, cudaStream_t stream) {
+  if (n_jobs <= 0) return;
+  switch (lane_entries_for(max_z)) {
+    case 2: launch_nj<2>(d_jobs, n_jobs, lattice_in_smem, use_D, smem_bytes, stream); break;
+    case 4: launch_nj<4>(d_jobs, n_jobs, lattice_in_smem, use_D, smem_bytes, stream); break;
+    case 6: launch_nj<6>(d_jobs, n_jobs, lattice_in_smem, use_D, smem_bytes, stream); break;
+    case 8: launch_nj<8>(d_jobs, n_jobs, lattice_in_smem, use_D, smem_bytes, stream); break;
+    default: launch_nj<11>(d_jobs, n_jobs, lattice_in_smem, use_D, smem_bytes, stream); break;
   }
 }
 

@@ -1,0 +1,213 @@
+// metropolis_halo.cu -- Metropolis-Kawasaki swap trials for fcc/bcc chains
+// staged with a periodic halo (see halo_engine.cuh): the batched path's
+// kernel for every lattice that fits.  One warp (CTA) per chain; trials in
+// the reference's order (monte_carlo_step_lattice / _nbr,
+// src/metropolis.F90:751-891) on the chain's own mt19937ar stream.
+#include "halo_engine.cuh"
+#include "kernels.cuh"
+
+namespace brawl {
+
+// Species of canonical compact site i through the halo layout.
+struct HaloLat {
+  int sz, sy, origin, SZ, SY, off;
+  __device__ __forceinline__ int operator()(int i) const {
+    extern __shared__ int8_t s_i8[];
+    const int Z = i / sz, r = i - Z * sz, Y = r / sy, X = r - Y * sy;
+    return s_i8[off + origin + Z * SZ + Y * SY + X];
+  }
+};
+
+// Fixed-point delta for any pair (neighbouring sites included), from the
+// canonical neighbour indices.  Out of line: only pairs within the
+// interaction range come here.
+__device__ __noinline__ int halo_delta_general(const ChainJob* __restrict__ Jg, int ents_off,
+                                               int I_off, int F_off, HaloLat lat, int ax, int ay,
+                                               int az, int ai, int bx, int by, int bz, int bi,
+                                               int sa, int sb, int lane) {
+  extern __shared__ int32_t s_i32[];
+  extern __shared__ uint32_t s_u32[];
+  const Geom g = Jg->g;
+  const bool h = lane >= 16;
+  const int cx = h ? bx : ax, cy = h ? by : ay, cz = h ? bz : az;
+  const int own = h ? bi : ai, other = h ? ai : bi;
+  const int so = h ? sb : sa, sn = h ? sa : sb;
+  const int nsp = g.ns + 1;
+  const int rowN = I_off + F_off + sn * g.nsh * nsp;
+  const int rowO = I_off + F_off + so * g.nsh * nsp;
+  int acc = 0;
+  for (int k = lane & 15; k < g.z; k += 16) {
+    int dx, dy, dz, sh;
+    unpack_entry(s_u32[ents_off / 4 + k], dx, dy, dz, sh);
+    const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
+    const int s_before = lat(ni);
+    const int s_after = ni == other ? so : (ni == own ? sn : s_before);
+    acc += s_i32[rowN + sh * nsp + s_after] - s_i32[rowO + sh * nsp + s_before];
+  }
+  return __reduce_add_sync(kFull, acc);
+}
+
+// The reference-order FP64 decision (see metropolis.cu); returns bit 0
+// accept, bit 1 uniform drawn, bit 2 FP64 libm tier, bit 3 double-double.
+__device__ __noinline__ int halo_exact_decision(const ChainJob* __restrict__ Jg, HaloLat lat,
+                                                const double* V, const uint32_t* ents,
+                                                const int16_t* sstart, int ax, int ay, int az,
+                                                int ai, int bx, int by, int bz, int bi, int sa,
+                                                int sb, int lane, uint32_t wu) {
+  const Geom g = Jg->g;
+  SitePair p;
+  p.ax = ax; p.ay = ay; p.az = az; p.ai = ai;
+  p.bx = bx; p.by = by; p.bz = bz; p.bi = bi;
+  p.sa = sa; p.sb = sb;
+  double e_un, e_sw;
+  exact_pair_energies(g, lat, V, ents, sstart, p, lane, e_un, e_sw);
+  const double delta_e = __dsub_rn(e_sw, e_un);
+  if (delta_e < 0.0) return 1;
+  DecideStats st = {0u, 0u};
+  const int acc = u_lt_exp(wu, __dmul_rn(-Jg->beta, delta_e), st);
+  return acc | 2 | (st.fp64 ? 4 : 0) | (st.cr ? 8 : 0);
+}
+
+template <int NJ>
+__global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __restrict__ jobs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ uint32_t s_u32[];
+  extern __shared__ int8_t s_i8[];
+  const ChainJob* Jg = jobs + blockIdx.x;
+  const Geom g = Jg->g;
+  const HaloGeom H = Jg->hg;
+  const int lane = threadIdx.x;
+  const HaloLayout L = halo_layout(g, H);
+  uint32_t* mt = reinterpret_cast<uint32_t*>(smem + L.mt);
+  uint32_t* tbuf = reinterpret_cast<uint32_t*>(smem + L.tbuf);
+  double* V = reinterpret_cast<double*>(smem + L.V);
+  uint32_t* ents = reinterpret_cast<uint32_t*>(smem + L.ents);
+  int16_t* sstart = reinterpret_cast<int16_t*>(smem + L.sstart);
+  int32_t* I = reinterpret_cast<int32_t*>(smem + L.I);
+  int8_t* lat = reinterpret_cast<int8_t*>(smem + L.lat);
+
+  // ---- stage state ------------------------------------------------------
+  const int nsp = g.ns + 1;
+  const int nI = nsp * nsp * g.nsh * (1 + nsp), nV = g.ns * g.ns * g.nsh;
+  const uint32_t* rng = Jg->rng;
+  for (int i = lane; i < kMTN; i += 32) mt[i] = rng[i];
+  for (int i = lane; i < nI; i += 32) I[i] = Jg->F[i];
+  for (int i = lane; i < nV; i += 32) V[i] = Jg->V[i];
+  for (int i = lane; i < g.z; i += 32) ents[i] = Jg->entries[i];
+  for (int i = lane; i <= g.nsh; i += 32) sstart[i] = Jg->shell_start[i];
+  __syncwarp();
+  halo_fill(g, H, Jg->lat, lat, lane);
+  Ring R;
+  ring_init(mt, tbuf, (int)rng[kMTN], lane, R);
+  HaloPlan<NJ> P;
+  make_halo_plan<NJ>(g, H, ents, lane, P);
+  __syncwarp();
+
+  const int lat_off = (int)L.lat;
+  const int tb = (int)(L.tbuf / 4);
+  const int I_off = (int)(L.I / 4);
+  const int D_abs = I_off + L.D_off;
+  const HaloLat hl = {g.sz, g.sy, H.origin, H.SZ, H.SY, lat_off};
+  const bool bcc = g.lattice == kBcc;
+  const int ys = g.ys;
+  const int nbr_swap = Jg->nbr_swap;
+  const int band = Jg->band;
+  const float bql2 = Jg->beta_q_l2, bband = Jg->beta_band;
+  const int64_t n_trials = Jg->n_trials;
+  const int n_peek = nbr_swap ? 5 : 7;
+  const int n_base = nbr_swap ? 4 : 6;
+  unsigned long long c_eval = 0, c_draws = 0, c_acc = 0, c_exp = 0, c_exact = 0;
+  unsigned int c_fp64 = 0, c_cr = 0, c_near = 0;
+
+  for (int64_t t = 0; t < n_trials; ++t) {
+    ring_ensure(mt, tbuf, R, n_peek, lane);
+    const int wb = tb + R.idx;
+    SitePair p;
+    draw_site(g, s_u32[wb], s_u32[wb + 1], s_u32[wb + 2], p.ax, p.ay, p.az);
+    if (nbr_swap) draw_nbr(g, s_u32[wb + 3], p.ax, p.ay, p.az, p.bx, p.by, p.bz);
+    else draw_site(g, s_u32[wb + 3], s_u32[wb + 4], s_u32[wb + 5], p.bx, p.by, p.bz);
+    const int Ya = p.ay >> ys, Xa = p.ax >> 1, Yb = p.by >> ys, Xb = p.bx >> 1;
+    const int pa = H.origin + p.az * H.SZ + Ya * H.SY + Xa;
+    const int pb = H.origin + p.bz * H.SZ + Yb * H.SY + Xb;
+    p.sa = s_i8[lat_off + pa];
+    p.sb = s_i8[lat_off + pb];
+    int consumed = n_base;
+    int accept = 1;  // same species: accepted without an energy evaluation or a draw
+    if (p.sa != p.sb) {
+      ++c_eval;
+      const bool near = pair_near(g, H, p.ax, p.ay, p.az, p.bx, p.by, p.bz);
+      p.ai = p.az * g.sz + Ya * g.sy + Xa;
+      p.bi = p.bz * g.sz + Yb * g.sy + Xb;
+      int dE;
+      if (!near) {
+        const bool par_a = bcc ? (p.az & 1) : (p.ax & 1);
+        const bool par_b = bcc ? (p.bz & 1) : (p.bx & 1);
+        dE = halo_delta<NJ>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
+      } else {
+        ++c_near;
+        dE = halo_delta_general(Jg, (int)L.ents, I_off, L.F_off, hl, p.ax, p.ay, p.az, p.ai,
+                                p.bx, p.by, p.bz, p.bi, p.sa, p.sb, lane);
+      }
+      const uint32_t wu = s_u32[wb + n_base];
+      accept = -1;
+      if (dE < -band) {
+        accept = 1;
+      } else if (dE > band) {
+        consumed = n_base + 1;
+        accept = fast_exp2_decision(bql2, bband, dE, wu);
+      }
+      if (accept < 0) {
+        ++c_exact;
+        const int r = halo_exact_decision(Jg, hl, V, ents, sstart, p.ax, p.ay, p.az, p.ai, p.bx,
+                                          p.by, p.bz, p.bi, p.sa, p.sb, lane, wu);
+        accept = r & 1;
+        consumed = (r & 2) ? n_base + 1 : n_base;
+        c_fp64 += (r >> 2) & 1;
+        c_cr += (r >> 3) & 1;
+      }
+      if (consumed > n_base) ++c_exp;
+      if (accept) halo_write_pair(H, lat, lane, p.az, Ya, Xa, p.sb, p.bz, Yb, Xb, p.sa);
+    }
+    c_acc += accept;
+    c_draws += consumed;
+    ring_consume(R, consumed);
+  }
+
+  // ---- write back ---------------------------------------------------------
+  __syncwarp();
+  halo_store(g, H, lat, Jg->lat, lane);
+  ring_writeback(mt, tbuf, R, Jg->rng, lane);
+  if (lane == 0) {
+    unsigned long long* c = Jg->counters;
+    c[kCntTrials] += (unsigned long long)n_trials;
+    c[kCntEvaluated] += c_eval;
+    c[kCntDraws] += c_draws;
+    c[kCntAccepted] += c_acc;
+    c[kCntExpTests] += c_exp;
+    c[kCntExactPath] += c_exact;
+    c[kCntExpFp64] += c_fp64;
+    c[kCntExpCr] += c_cr;
+  }
+}
+
+template <int NJ>
+static void launch_halo_nj(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes,
+                           cudaStream_t stream) {
+  cudaFuncSetAttribute(metropolis_halo_kernel<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_bytes);
+  metropolis_halo_kernel<NJ><<<n_jobs, 32, smem_bytes, stream>>>(d_jobs);
+}
+
+void launch_metropolis_halo(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z,
+                            cudaStream_t stream) {
+  if (n_jobs <= 0) return;
+  switch (lane_entries_for(max_z)) {
+    case 2: launch_halo_nj<2>(d_jobs, n_jobs, smem_bytes, stream); break;
+    case 4: launch_halo_nj<4>(d_jobs, n_jobs, smem_bytes, stream); break;
+    case 6: launch_halo_nj<6>(d_jobs, n_jobs, smem_bytes, stream); break;
+    case 8: launch_halo_nj<8>(d_jobs, n_jobs, smem_bytes, stream); break;
+    default: launch_halo_nj<11>(d_jobs, n_jobs, smem_bytes, stream); break;
+  }
+}
+
+}  // namespace brawl

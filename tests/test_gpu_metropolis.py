@@ -8,7 +8,7 @@ import pytest
 
 import brawl_gb300 as B
 from brawl_gb300 import inputs as I
-from brawl_gb300 import metropolis as MET
+from brawl_gb300 import metropolis as anneal
 from brawl_gb300 import output as OUT
 from oracle import oracle as O
 from tests import golden_io as G
@@ -53,7 +53,7 @@ def test_golden_anneal_on_gpu(test, rank):
     seed = ch.f90_init_genrand(0, rank)
     assert seed == 110179 + 11 * rank
     ch.initial_setup(p.species_concentrations, p.numbers_or_none())
-    out = MET.simulated_annealing(ch, m, p.wc_range)
+    out = anneal.simulated_annealing(ch, m, p.wc_range)
     tag = "proc_%04d" % rank
     assert np.array_equal(out["initial_configs"][0],
                           G.config_zyx(test, tag + "_initial_config_at_0300.0.npz"))
@@ -90,6 +90,8 @@ SYSTEMS = [
     ("simple_cubic", (3, 3, 3), 2, 2, 400.0, 20000, False),
     ("simple_cubic", (2, 3, 4), 3, 1, 50.0, 20000, True),
     ("fcc", (4, 4, 4), 4, 3, 5.0, 30000, False),     # nearly every uphill move rejected
+    ("bcc", (3, 3, 4), 9, 8, 700.0, 20000, False),   # many species: no difference table
+    ("fcc", (3, 3, 3), 15, 2, 2000.0, 20000, False),
 ]
 
 
