@@ -81,6 +81,7 @@ def load(rebuild: bool = False):
         "brawl_lattice_shells": ([vp, i, vp], i),
         "brawl_radial_densities": ([vp, i, vp, vp], i),
         "brawl_counters": ([vp, vp], i),
+        "brawl_total_energy_noalloc": ([vp, vp, vp, vp, vp], i),
         "brawl_batch_create": ([vp, i, vp], i),
         "brawl_batch_destroy": ([vp], i),
         "brawl_batch_size": ([vp, vp], i),

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/brawl_gpu.h"
+#include "api_internal.h"
 #include "asro.cuh"
 #include "kernels.cuh"
 
@@ -1070,3 +1071,8 @@ int brawl_counters(brawl_ctx* ctx, int64_t* counters) {
 }
 
 }  // extern "C"
+
+namespace brawl {
+int api_fail(int code, const std::string& msg) { return fail(code, msg); }
+int api_make_geom(const brawl_setup& s, Geom& g) { return make_geom(s, g); }
+}  // namespace brawl

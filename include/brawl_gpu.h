@@ -124,6 +124,23 @@ int brawl_radial_densities(brawl_ctx *ctx, int wc_range, const double *shells, d
 /* Cumulative counters of this chain (BRAWL_NUM_COUNTERS values). */
 int brawl_counters(brawl_ctx *ctx, int64_t *counters);
 
+/* No counterpart in the reference.  The total energy of brawl_total_energy,
+ * bit-identical, for callers that cannot allocate device memory -- a host
+ * that gives all device memory to its own pool at start-up, or one that
+ * records its GPU work into a CUDA graph and must finish allocating before
+ * recording.  d_V_ex, d_config (reference layout) and d_energy (one double)
+ * are device memory the caller owns; nothing is allocated or freed.  The
+ * per-site scratch is one fixed array of 524288 doubles (4 MiB) inside the
+ * library, held by every device that loads it until the process exits;
+ * lattices with more sites are rejected with BRAWL_EINVAL.  The work is
+ * queued on `stream` (a cudaStream_t, NULL for the default stream) and the
+ * call returns without waiting.  The first call on each device (with that
+ * device current) does a one-time set-up, so make it before any stream
+ * capture.  Calls share the scratch array: calls that overlap on the GPU
+ * race.  The config must hold species 1..n_species on every lattice site. */
+int brawl_total_energy_noalloc(const brawl_setup *setup, const double *d_V_ex,
+                               const int8_t *d_config, double *d_energy, void *stream);
+
 /* ====================================================================== */
 /* Batches: many independent chains (replicas, temperatures, walkers) of  */
 /* uneven lattice, species and shell counts, run together -- the          */
