@@ -16,7 +16,8 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["load", "Setup", "Chain", "Batch", "BrawlError", "LATTICES", "K_B_IN_RY", "RY_TO_EV"]
+__all__ = ["load", "Setup", "Chain", "Batch", "NestedSampling", "BrawlError", "LATTICES",
+           "K_B_IN_RY", "RY_TO_EV"]
 
 # src/constants.f90:41-49 (as written there)
 K_B_IN_EV = 8.167333262e-5
@@ -38,6 +39,12 @@ class BrawlError(RuntimeError):
 class _Setup(C.Structure):
     _fields_ = [("lattice", C.c_int), ("n_1", C.c_int), ("n_2", C.c_int), ("n_3", C.c_int),
                 ("n_species", C.c_int), ("interaction_range", C.c_int)]
+
+
+class _NsDesc(C.Structure):
+    _fields_ = [("setup", _Setup), ("V_ex", C.c_void_p), ("seed", C.c_uint32),
+                ("n_walkers", C.c_int), ("n_steps", C.c_int),
+                ("species_concentrations", C.c_void_p), ("species_numbers", C.c_void_p)]
 
 
 class _ChainDesc(C.Structure):
@@ -82,6 +89,12 @@ def load(rebuild: bool = False):
         "brawl_radial_densities": ([vp, i, vp, vp], i),
         "brawl_counters": ([vp, vp], i),
         "brawl_total_energy_noalloc": ([vp, vp, vp, vp, vp], i),
+        "brawl_ns_create": ([vp, i, vp], i),
+        "brawl_ns_destroy": ([vp], i),
+        "brawl_ns_iterate": ([vp, i, vp], i),
+        "brawl_ns_energies": ([vp, i, vp], i),
+        "brawl_ns_walker_config": ([vp, i, i, vp], i),
+        "brawl_ns_counters": ([vp, i, vp], i),
         "brawl_batch_create": ([vp, i, vp], i),
         "brawl_batch_destroy": ([vp], i),
         "brawl_batch_size": ([vp, vp], i),
@@ -399,3 +412,69 @@ class Batch:
         out = np.zeros((wc, ns, ns), dtype=np.float64)
         _check(load().brawl_batch_radial_densities(self._h, c, wc, _ptr(shells), _ptr(out)))
         return out
+
+
+class NestedSampling:
+    """Independent nested-sampling runs resident on the GPU (brawl_ns):
+    nested_sampling_main (src/nested_sampling.f90:45-206)."""
+
+    def __init__(self, runs: list[dict]):
+        """Each run: dict(setup=Setup, V=array, seed=int, n_walkers=int,
+        n_steps=int, species_concentrations=array, species_numbers=array|None)."""
+        n = len(runs)
+        descs = (_NsDesc * n)()
+        keep = []
+        self.runs = runs
+        for k, r in enumerate(runs):
+            s = r["setup"]
+            V = _v_array(s, r["V"])
+            conc = np.ascontiguousarray(r["species_concentrations"], dtype=np.float64)
+            keep += [V, conc]
+            d = descs[k]
+            d.setup = s.c()
+            d.V_ex = V.ctypes.data
+            d.seed = int(r.get("seed", 5489)) & 0xFFFFFFFF
+            d.n_walkers = int(r["n_walkers"])
+            d.n_steps = int(r["n_steps"])
+            d.species_concentrations = conc.ctypes.data
+            nums = r.get("species_numbers")
+            if nums is not None:
+                nums = np.ascontiguousarray(nums, dtype=np.int64)
+                keep.append(nums)
+                d.species_numbers = nums.ctypes.data
+        h = C.c_void_p()
+        _check(load().brawl_ns_create(descs, n, C.byref(h)))
+        self._h = h
+        self.n = n
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().brawl_ns_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def iterate(self, n_iter: int) -> np.ndarray:
+        """Ceilings of the next n_iter iterations, shaped (runs, n_iter)."""
+        out = np.zeros((self.n, n_iter), dtype=np.float64)
+        _check(load().brawl_ns_iterate(self._h, int(n_iter), _ptr(out)))
+        return out
+
+    def energies(self, run: int) -> np.ndarray:
+        out = np.zeros(int(self.runs[run]["n_walkers"]), dtype=np.float64)
+        _check(load().brawl_ns_energies(self._h, run, _ptr(out)))
+        return out
+
+    def walker_config(self, run: int, walker: int) -> np.ndarray:
+        out = np.zeros(self.runs[run]["setup"].grid_shape, dtype=np.int8)
+        _check(load().brawl_ns_walker_config(self._h, run, walker, _ptr(out)))
+        return out
+
+    def counters(self, run: int) -> dict:
+        c = np.zeros(NUM_COUNTERS, dtype=np.int64)
+        _check(load().brawl_ns_counters(self._h, run, _ptr(c)))
+        return dict(zip(COUNTER_NAMES, (int(v) for v in c)))

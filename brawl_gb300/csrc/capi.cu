@@ -1076,3 +1076,228 @@ namespace brawl {
 int api_fail(int code, const std::string& msg) { return fail(code, msg); }
 int api_make_geom(const brawl_setup& s, Geom& g) { return make_geom(s, g); }
 }  // namespace brawl
+
+// ---------------------------------------------------------------------------
+// nested sampling
+// ---------------------------------------------------------------------------
+#include "ns_kernels.cuh"
+
+struct brawl_ns {
+  std::vector<Model> models;
+  std::vector<NsRun> runs;               // host images
+  std::vector<void*> allocs;
+  NsRun* d_runs = nullptr;
+  double* d_limits = nullptr;
+  size_t limits_cap = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t smem = 0;
+};
+
+extern "C" int brawl_ns_destroy(brawl_ns* ns) {
+  if (!ns) return BRAWL_OK;
+  if (ns->stream) cudaStreamSynchronize(ns->stream);
+  for (void* p : ns->allocs) cudaFree(p);
+  if (ns->d_limits) cudaFree(ns->d_limits);
+  if (ns->stream) cudaStreamDestroy(ns->stream);
+  delete ns;
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns** out) {
+  if (!descs || !out || n_runs < 1) return fail(BRAWL_EINVAL, "no runs");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(BRAWL_ECUDA, "no CUDA device");
+  brawl_ns* ns = new brawl_ns();
+  auto cleanup = [&](int rc) {
+    brawl_ns_destroy(ns);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&ns->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(fail(BRAWL_ECUDA, "stream create failed"));
+  int max_optin = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  ns->models.resize(n_runs);
+  ns->runs.resize(n_runs);
+  int64_t total_sites = 0;
+  int max_K = 0;
+  for (int r = 0; r < n_runs; ++r) {
+    const brawl_ns_desc& d = descs[r];
+    Model& m = ns->models[r];
+    int rc = make_model(d.setup, d.V_ex, m);
+    if (rc != BRAWL_OK) return cleanup(fail(rc, "run " + std::to_string(r) + ": " + g_err));
+    if (d.n_walkers < 1 || d.n_steps < 0 || !d.species_concentrations)
+      return cleanup(fail(BRAWL_EINVAL, "run " + std::to_string(r) + ": bad n_walkers/n_steps/concentrations"));
+    ns->smem = std::max(ns->smem, ns_smem_bytes(m.g));
+    NsRun& R = ns->runs[r];
+    std::memset(&R, 0, sizeof(R));
+    std::vector<double> conc(d.species_concentrations, d.species_concentrations + m.g.ns + 1);
+    rc = make_init_job(m, conc.data(), d.species_numbers, R.init);
+    if (rc != BRAWL_OK) return cleanup(fail(rc, "run " + std::to_string(r) + ": " + g_err));
+    R.K = d.n_walkers;
+    R.n_steps = d.n_steps;
+    R.n_at = d.setup.n_1 * d.setup.n_2 * d.setup.n_3 * 1 * d.setup.n_species;
+    R.half = (int)((float)d.n_walkers / 2.0f);
+    R.S = m.S;
+    total_sites += (int64_t)R.K * m.g.n_sites;
+    max_K = std::max(max_K, R.K);
+  }
+  if (ns->smem > (uint32_t)max_optin)
+    return cleanup(fail(BRAWL_EINVAL, "a run's lattice and tables exceed shared memory"));
+  auto dalloc = [&](size_t bytes, void** p) -> int {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(BRAWL_ENOMEM, cudaGetErrorString(e));
+    ns->allocs.push_back(*p);
+    return BRAWL_OK;
+  };
+  for (int r = 0; r < n_runs; ++r) {
+    const Model& m = ns->models[r];
+    NsRun& R = ns->runs[r];
+    ChainJob& j = R.job;
+    j.g = m.g;
+    j.band = m.band;
+    void *pV, *pF, *pE, *pS, *pRng, *pCnt, *pSt, *pW, *pEn, *pRn;
+    int rc = BRAWL_OK;
+    rc |= dalloc(m.V.size() * 8, &pV);
+    rc |= dalloc(m.F.size() * 4, &pF);
+    rc |= dalloc(m.entries.size() * 4, &pE);
+    rc |= dalloc(m.sstart.size() * 2, &pS);
+    rc |= dalloc((kMTN + 1) * 4, &pRng);
+    rc |= dalloc(kNumCounters * 8, &pCnt);
+    rc |= dalloc(4, &pSt);
+    rc |= dalloc((size_t)R.K * m.g.n_sites, &pW);
+    rc |= dalloc((size_t)R.K * 8, &pEn);
+    rc |= dalloc((size_t)R.K * 4, &pRn);
+    if (rc != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
+    uint32_t st[kMTN + 1];
+    mt_seed_host(descs[r].seed, st);
+    cudaMemcpy(pV, m.V.data(), m.V.size() * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(pF, m.F.data(), m.F.size() * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(pE, m.entries.data(), m.entries.size() * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(pS, m.sstart.data(), m.sstart.size() * 2, cudaMemcpyHostToDevice);
+    cudaMemcpy(pRng, st, sizeof(st), cudaMemcpyHostToDevice);
+    cudaMemset(pCnt, 0, kNumCounters * 8);
+    cudaMemset(pSt, 0, 4);
+    j.V = (const double*)pV;
+    j.F = (const int32_t*)pF;
+    j.entries = (const uint32_t*)pE;
+    j.shell_start = (const int16_t*)pS;
+    j.rng = (uint32_t*)pRng;
+    j.counters = (unsigned long long*)pCnt;
+    j.status = (int32_t*)pSt;
+    R.init.n_sites = m.g.n_sites;
+    R.init.ns = m.g.ns;
+    R.init.counters = j.counters;
+    R.init.status = j.status;
+    R.walkers = (int8_t*)pW;
+    R.energies = (double*)pEn;
+    R.rnde = (uint32_t*)pRn;
+  }
+  void* pRuns;
+  if (dalloc(n_runs * sizeof(NsRun), &pRuns) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
+  ns->d_runs = (NsRun*)pRuns;
+  CUDA_TRY(cudaMemcpy(ns->d_runs, ns->runs.data(), n_runs * sizeof(NsRun), cudaMemcpyHostToDevice));
+  launch_ns_init(ns->d_runs, n_runs, ns->stream);
+  // walker energies: total_energy of every walker, then the jitter
+  void *pSite, *pEj;
+  if (dalloc((size_t)total_sites * 8, &pSite) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
+  std::vector<EnergyJob> ej;
+  int64_t off = 0;
+  for (int r = 0; r < n_runs; ++r) {
+    const NsRun& R = ns->runs[r];
+    for (int w = 0; w < R.K; ++w) {
+      EnergyJob e;
+      std::memset(&e, 0, sizeof(e));
+      e.g = R.job.g;
+      e.lat = R.walkers + (size_t)w * R.job.g.n_sites;
+      e.V = R.job.V;
+      e.entries = R.job.entries;
+      e.shell_start = R.job.shell_start;
+      e.site_energy = (double*)pSite + off;
+      e.out = R.energies + w;
+      e.site_offset = off;
+      off += R.job.g.n_sites;
+      ej.push_back(e);
+    }
+  }
+  if (dalloc(ej.size() * sizeof(EnergyJob), &pEj) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
+  CUDA_TRY(cudaMemcpyAsync(pEj, ej.data(), ej.size() * sizeof(EnergyJob), cudaMemcpyHostToDevice, ns->stream));
+  launch_total_energy((EnergyJob*)pEj, (int)ej.size(), total_sites, ns->stream);
+  launch_ns_jitter(ns->d_runs, n_runs, max_K, ns->stream);
+  cudaError_t e = cudaStreamSynchronize(ns->stream);
+  if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
+  // the per-site scratch is only needed at set-up
+  cudaFree(pSite);
+  cudaFree(pEj);
+  ns->allocs.erase(std::remove(ns->allocs.begin(), ns->allocs.end(), pSite), ns->allocs.end());
+  ns->allocs.erase(std::remove(ns->allocs.begin(), ns->allocs.end(), pEj), ns->allocs.end());
+  for (int r = 0; r < n_runs; ++r) {
+    int32_t st = 0;
+    cudaMemcpy(&st, ns->runs[r].job.status, 4, cudaMemcpyDeviceToHost);
+    if (st) return cleanup(fail(BRAWL_ESTATE, "walker initialisation failed on run " + std::to_string(r)));
+  }
+  *out = ns;
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_ns_iterate(brawl_ns* ns, int n_iter, double* limits) {
+  if (!ns || n_iter < 0) return fail(BRAWL_EINVAL, "bad argument");
+  if (n_iter == 0) return BRAWL_OK;
+  const int n_runs = (int)ns->runs.size();
+  const size_t need = (size_t)n_runs * n_iter * 8;
+  if (need > ns->limits_cap) {
+    if (ns->d_limits) cudaFree(ns->d_limits);
+    ns->d_limits = nullptr;
+    ns->limits_cap = 0;
+    CUDA_TRY(cudaMalloc(&ns->d_limits, need));
+    ns->limits_cap = need;
+  }
+  // the device-side run state (iteration counters) is authoritative: read it back
+  std::vector<NsRun> cur(n_runs);
+  CUDA_TRY(cudaMemcpy(cur.data(), ns->d_runs, n_runs * sizeof(NsRun), cudaMemcpyDeviceToHost));
+  for (int r = 0; r < n_runs; ++r) {
+    cur[r].limits = ns->d_limits + (size_t)r * n_iter;
+    cur[r].n_iter = n_iter;
+  }
+  CUDA_TRY(cudaMemcpyAsync(ns->d_runs, cur.data(), n_runs * sizeof(NsRun), cudaMemcpyHostToDevice, ns->stream));
+  launch_ns_iterate(ns->d_runs, n_runs, ns->smem, ns->stream);
+  CUDA_TRY(cudaGetLastError());
+  if (limits)
+    CUDA_TRY(cudaMemcpyAsync(limits, ns->d_limits, need, cudaMemcpyDeviceToHost, ns->stream));
+  CUDA_TRY(cudaStreamSynchronize(ns->stream));
+  for (int r = 0; r < n_runs; ++r) {
+    int32_t st = 0;
+    CUDA_TRY(cudaMemcpy(&st, ns->runs[r].job.status, 4, cudaMemcpyDeviceToHost));
+    if (st) return fail(BRAWL_ESTATE, "nested sampling check failed on run " + std::to_string(r));
+  }
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_ns_energies(brawl_ns* ns, int run, double* energies) {
+  if (!ns || !energies || run < 0 || run >= (int)ns->runs.size()) return fail(BRAWL_EINVAL, "bad argument");
+  CUDA_TRY(cudaMemcpy(energies, ns->runs[run].energies, ns->runs[run].K * 8, cudaMemcpyDeviceToHost));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_ns_walker_config(brawl_ns* ns, int run, int walker, int8_t* config) {
+  if (!ns || !config || run < 0 || run >= (int)ns->runs.size()) return fail(BRAWL_EINVAL, "bad argument");
+  const NsRun& R = ns->runs[run];
+  if (walker < 0 || walker >= R.K) return fail(BRAWL_EINVAL, "bad walker");
+  const Geom& g = R.job.g;
+  const size_t grid = (size_t)8 * g.n1 * g.n2 * g.n3;
+  int8_t* d_grid = nullptr;
+  CUDA_TRY(cudaMalloc(&d_grid, grid));
+  launch_unpack(g, R.walkers + (size_t)walker * g.n_sites, d_grid, ns->stream);
+  cudaError_t e = cudaMemcpyAsync(config, d_grid, grid, cudaMemcpyDeviceToHost, ns->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ns->stream);
+  cudaFree(d_grid);
+  if (e != cudaSuccess) return fail(BRAWL_ECUDA, cudaGetErrorString(e));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_ns_counters(brawl_ns* ns, int run, int64_t* counters) {
+  if (!ns || !counters || run < 0 || run >= (int)ns->runs.size()) return fail(BRAWL_EINVAL, "bad argument");
+  CUDA_TRY(cudaMemcpy(counters, ns->runs[run].job.counters, kNumCounters * 8, cudaMemcpyDeviceToHost));
+  return BRAWL_OK;
+}

@@ -56,7 +56,7 @@ struct Ring {
 };
 
 // Twists mt in place and tempers the new block into the ring half next_half.
-__device__ __noinline__ void ring_generate(uint32_t* mt, uint32_t* tbuf, int next_half,
+static __device__ __noinline__ void ring_generate(uint32_t* mt, uint32_t* tbuf, int next_half,
                                            int lane) {
   mt_twist_warp(mt, lane);
   uint32_t* dst = tbuf + next_half * kMTN;

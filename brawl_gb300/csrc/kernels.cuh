@@ -98,6 +98,41 @@ struct InitJob {
 };
 void launch_initial_setup(const InitJob* d_jobs, int n_jobs, cudaStream_t stream);
 
+// The site-by-site draw loop of initial_setup for one configuration, on the
+// warp's stream (mt in shared memory at position pos); check is shared
+// scratch of kMaxSpecies counters.  Returns false when a quota can never be
+// met (guards against a corrupted job; the host validates counts).
+__device__ inline bool initial_setup_warp(const InitJob& J, int8_t* lat, uint32_t* mt, int& pos,
+                                          int64_t* check, unsigned long long& draws, int lane) {
+  if (lane < kMaxSpecies) check[lane] = 0;
+  __syncwarp();
+  const int ns = J.ns;
+  const unsigned long long limit = draws + (unsigned long long)J.n_sites * 4096ull + 1000000ull;
+  for (int site = 0; site < J.n_sites; ++site) {
+    int s = 0;
+    while (s == 0) {
+      const uint32_t w = __shfl_sync(kFull, mt_peek(mt, pos, 1, lane), 0);
+      pos += 1;
+      ++draws;
+      const int64_t wl = (int64_t)w;
+      for (int l = 0; l < ns; ++l) {
+        if (wl >= J.lo_w[l] && wl <= J.hi_w[l]) {
+          if (check[l] < J.counts[l]) {
+            s = l + 1;
+            __syncwarp();
+            if (lane == 0) check[l] += 1;
+            __syncwarp();
+          }
+        }
+      }
+      if (draws > limit) return false;
+    }
+    if (lane == 0) lat[site] = (int8_t)s;
+  }
+  __syncwarp();
+  return true;
+}
+
 // total_energy (src/bw_hamiltonian.f90:58-81): per-site FP64 energies in the
 // reference's order, then the sequential sum over sites in z, y, x order.
 struct EnergyJob {

@@ -21,36 +21,12 @@ __global__ void __launch_bounds__(32) initial_setup_kernel(const InitJob* __rest
   const InitJob& J = jobs[blockIdx.x];
   const int lane = threadIdx.x;
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
-  if (lane < kMaxSpecies) check[lane] = 0;
   int pos = (int)J.rng[kMTN];
   __syncwarp();
   unsigned long long draws = 0;
-  const int ns = J.ns;
-  for (int site = 0; site < J.n_sites; ++site) {
-    int s = 0;
-    while (s == 0) {
-      const uint32_t w = __shfl_sync(kFull, mt_peek(mt, pos, 1, lane), 0);
-      pos += 1;
-      ++draws;
-      const int64_t wl = (int64_t)w;
-      for (int l = 0; l < ns; ++l) {
-        if (wl >= J.lo_w[l] && wl <= J.hi_w[l]) {
-          if (check[l] < J.counts[l]) {
-            s = l + 1;
-            __syncwarp();
-            if (lane == 0) check[l] += 1;
-            __syncwarp();
-          }
-        }
-      }
-      if (draws > (unsigned long long)J.n_sites * 4096ull + 1000000ull) {
-        // a quota that can never be met (the host validates the counts, so
-        // this only guards against a corrupted job)
-        if (lane == 0) *J.status = kStatusBadSpecies;
-        return;
-      }
-    }
-    if (lane == 0) J.lat[site] = (int8_t)s;
+  if (!initial_setup_warp(J, J.lat, mt, pos, check, draws, lane)) {
+    if (lane == 0) *J.status = kStatusBadSpecies;
+    return;
   }
   __syncwarp();
   for (int i = lane; i < kMTN; i += 32) J.rng[i] = mt[i];

@@ -1,0 +1,269 @@
+// nested_sampling.cu -- nested sampling on the device
+// (src/nested_sampling.f90:45-206): K walkers drawn by initial_setup from
+// one stream, then per iteration the highest energy becomes the ceiling, a
+// random walker is cloned over it and walks n_steps (+ adaptive extra steps)
+// random swaps, each accepted iff E + dE stays below the ceiling.
+//
+// One warp per independent run.  The walkers live in HBM (compact, one byte
+// per site); the active walker is staged in shared memory for its walk.  A
+// walk step's dE is needed exactly whenever the move may be accepted (the
+// walker's energy is carried in FP64), so the fixed-point tier only rejects
+// moves that certainly climb over the ceiling; the others take the
+// reference-order FP64 sums.
+#include "halo_engine.cuh"
+#include "kernels.cuh"
+#include "ns_kernels.cuh"
+
+namespace brawl {
+
+// Walker initialisation: for each walker in order, initial_setup then one
+// draw for the 1e-8 energy jitter (nested_sampling.f90:86-96).
+__global__ void __launch_bounds__(32) ns_init_kernel(NsRun* __restrict__ runs) {
+  __shared__ uint32_t mt[kMTN];
+  __shared__ int64_t check[kMaxSpecies];
+  NsRun& R = runs[blockIdx.x];
+  const int lane = threadIdx.x;
+  uint32_t* rng = R.job.rng;
+  for (int i = lane; i < kMTN; i += 32) mt[i] = rng[i];
+  int pos = (int)rng[kMTN];
+  __syncwarp();
+  unsigned long long draws = 0;
+  const int n = R.job.g.n_sites;
+  for (int w = 0; w < R.K; ++w) {
+    if (!initial_setup_warp(R.init, R.walkers + (size_t)w * n, mt, pos, check, draws, lane)) {
+      if (lane == 0) *R.job.status = kStatusBadSpecies;
+      return;
+    }
+    const uint32_t u = __shfl_sync(kFull, mt_peek(mt, pos, 1, lane), 0);
+    pos += 1;
+    ++draws;
+    if (lane == 0) R.rnde[w] = u;
+  }
+  __syncwarp();
+  for (int i = lane; i < kMTN; i += 32) rng[i] = mt[i];
+  if (lane == 0) {
+    rng[kMTN] = (uint32_t)pos;
+    R.job.counters[kCntDraws] += draws;
+  }
+}
+
+// energies(w) = full_energy(walker w) + rnde * 1e-8 (the literal is single
+// precision in the reference).
+__global__ void ns_jitter_kernel(NsRun* __restrict__ runs, int n_runs) {
+  const int r = blockIdx.y;
+  if (r >= n_runs) return;
+  NsRun& R = runs[r];
+  const double c = (double)1.0e-8f;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < R.K; w += gridDim.x * blockDim.x) {
+    const double u = __dmul_rn((double)R.rnde[w], 2.3283064365386963e-10);
+    R.energies[w] = __dadd_rn(R.energies[w], __dmul_rn(u, c));
+  }
+}
+
+// Order-preserving integer key of a double (larger double, larger key).
+__device__ __forceinline__ unsigned long long dkey(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// Fixed-point lower bound of the ceiling gap: Gup >= (limit - E) * 2^S.
+__device__ __forceinline__ long long gap_up(double limit, double E, int S) {
+  const double gd = __dsub_rn(limit, E);
+  const double m = __dadd_rn(gd, __dmul_rn(fabs(gd), 8.881784197001252e-16));  // + |gd| 2^-50
+  const double s = ldexp(m, S);
+  if (!(s < 9.0e18)) return 0x7fffffffffffffffll;
+  if (s < -9.0e18) return -0x7fffffffffffffffll;
+  return (long long)ceil(s);
+}
+
+// Fixed-point swap delta for any pair, from canonical neighbour indices
+// (lanes 0-15 site 1, 16-31 site 2).
+__device__ __forceinline__ int ns_fixed_delta(const Geom& g, const int8_t* lat, const int32_t* F,
+                                              const uint32_t* ents, const SitePair& p, int lane) {
+  const bool h = lane >= 16;
+  const int cx = h ? p.bx : p.ax, cy = h ? p.by : p.ay, cz = h ? p.bz : p.az;
+  const int own = h ? p.bi : p.ai, other = h ? p.ai : p.bi;
+  const int so = h ? p.sb : p.sa, sn = h ? p.sa : p.sb;
+  const int nsp = g.ns + 1;
+  const int rowN = sn * g.nsh * nsp, rowO = so * g.nsh * nsp;
+  int acc = 0;
+  for (int k = lane & 15; k < g.z; k += 16) {
+    int dx, dy, dz, sh;
+    unpack_entry(ents[k], dx, dy, dz, sh);
+    const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
+    const int sb = lat[ni];
+    const int sa = ni == other ? so : (ni == own ? sn : sb);
+    acc += F[rowN + sh * nsp + sa] - F[rowO + sh * nsp + sb];
+  }
+  return __reduce_add_sync(kFull, acc);
+}
+
+__global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  NsRun& R = runs[blockIdx.x];
+  const ChainJob& J = R.job;
+  const Geom g = J.g;
+  const int lane = threadIdx.x;
+  const int n = g.n_sites;
+  const int nsp = g.ns + 1;
+  const int nF = nsp * g.nsh * nsp, nV = g.ns * g.ns * g.nsh;
+  // layout: mt | tbuf | V | F | ents | sstart | lattice
+  uint32_t* mt = reinterpret_cast<uint32_t*>(smem);
+  uint32_t* tbuf = mt + kMTN;
+  double* V = reinterpret_cast<double*>(smem + align_up((kMTN + kTbufWords) * 4, 16));
+  int32_t* F = reinterpret_cast<int32_t*>(V + nV);
+  uint32_t* ents = reinterpret_cast<uint32_t*>(F + nF);
+  int16_t* sstart = reinterpret_cast<int16_t*>(ents + g.z);
+  int8_t* lat = reinterpret_cast<int8_t*>(
+      smem + align_up((uint32_t)((reinterpret_cast<unsigned char*>(sstart + g.nsh + 1)) - smem), 16));
+  for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
+  for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
+  for (int i = lane; i < nF; i += 32) F[i] = J.F[i];
+  for (int i = lane; i < g.z; i += 32) ents[i] = J.entries[i];
+  for (int i = lane; i <= g.nsh; i += 32) sstart[i] = J.shell_start[i];
+  __syncwarp();
+  Ring ring;
+  ring_init(mt, tbuf, (int)J.rng[kMTN], lane, ring);
+
+  const int K = R.K;
+  const int half = R.half;
+  const int S = R.S;
+  const int band = J.band;
+  int extra_steps = R.extra_steps;
+  long long n_acc = R.n_acc;
+  long long it = R.iter;
+  unsigned long long c_steps = 0, c_draws = 0, c_acc = 0, c_exact = 0;
+  int status = kStatusOk;
+
+  for (int li = 0; li < R.n_iter; ++li) {
+    ++it;
+    // maxloc: first index of the largest energy
+    unsigned long long best = 0;
+    int bidx = 0x7fffffff;
+    for (int w = lane; w < K; w += 32) {
+      const unsigned long long k = dkey(R.energies[w]);
+      if (k > best || (k == best && w < bidx)) {
+        best = k;
+        bidx = w;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ok = __shfl_xor_sync(kFull, best, o);
+      const int oi = __shfl_xor_sync(kFull, bidx, o);
+      if (ok > best || (ok == best && oi < bidx)) {
+        best = ok;
+        bidx = oi;
+      }
+    }
+    const int imax = bidx;
+    const double limit = R.energies[imax];
+    if (lane == 0) R.limits[li] = limit;
+    // adaptive extra steps (nested_sampling.f90:129-144)
+    if (half > 0 && (it % half) == 0) {
+      if (((float)n_acc < (float)R.n_at * 0.05f) && (extra_steps < R.n_steps * 100))
+        extra_steps += R.n_steps;
+    }
+    // clone: irnd = ceiling(rnd * K), 0 only when rnd == 0 (clamped to 1)
+    ring_ensure(mt, tbuf, ring, 1, lane);
+    const uint32_t wr = tbuf[ring.idx];
+    ring_consume(ring, 1);
+    ++c_draws;
+    int irnd = (int)(((unsigned long long)wr * (unsigned long long)K + 0xffffffffull) >> 32);
+    if (irnd < 1) irnd = 1;
+    const int8_t* src = R.walkers + (size_t)(irnd - 1) * n;
+    for (int i = lane; i < n; i += 32) lat[i] = src[i];
+    double E = R.energies[irnd - 1];
+    __syncwarp();
+    long long gup = gap_up(limit, E, S);
+    n_acc = 0;
+    const long long steps = (long long)R.n_steps + extra_steps;
+    for (long long st = 0; st < steps; ++st) {
+      ring_ensure(mt, tbuf, ring, 3, lane);
+      SitePair p;
+      draw_site(g, tbuf[ring.idx], tbuf[ring.idx + 1], tbuf[ring.idx + 2], p.ax, p.ay, p.az);
+      ring_consume(ring, 3);
+      p.ai = compact_index(g, p.ax, p.ay, p.az);
+      p.sa = lat[p.ai];
+      int tries = 0;
+      do {
+        ring_ensure(mt, tbuf, ring, 3, lane);
+        draw_site(g, tbuf[ring.idx], tbuf[ring.idx + 1], tbuf[ring.idx + 2], p.bx, p.by, p.bz);
+        ring_consume(ring, 3);
+        p.bi = compact_index(g, p.bx, p.by, p.bz);
+        p.sb = lat[p.bi];
+        c_draws += 3;
+        if (++tries > (1 << 24)) {
+          status = kStatusBadSpecies;  // a single species: the reference loops forever
+          break;
+        }
+      } while (p.sb == p.sa);
+      if (status != kStatusOk) break;
+      c_draws += 3;
+      ++c_steps;
+      const int dE = ns_fixed_delta(g, lat, F, ents, p, lane);
+      // certainly E + dE >= ceiling: rejected without the FP64 sums
+      if ((long long)dE - band >= gup) continue;
+      ++c_exact;
+      double e_un, e_sw;
+      exact_pair_energies(g, CompactLat{lat}, V, ents, sstart, p, lane, e_un, e_sw);
+      const double delta_e = __dsub_rn(e_sw, e_un);
+      const double e_new = __dadd_rn(E, delta_e);
+      if (e_new < limit) {
+        E = e_new;
+        ++n_acc;
+        ++c_acc;
+        if (lane == 0) {
+          lat[p.ai] = (int8_t)p.sb;
+          lat[p.bi] = (int8_t)p.sa;
+        }
+        __syncwarp();
+        gup = gap_up(limit, E, S);
+      }
+    }
+    if (status != kStatusOk) break;
+    int8_t* dst = R.walkers + (size_t)imax * n;
+    for (int i = lane; i < n; i += 32) dst[i] = lat[i];
+    if (lane == 0) R.energies[imax] = E;
+    __syncwarp();
+  }
+  ring_writeback(mt, tbuf, ring, J.rng, lane);
+  if (lane == 0) {
+    R.extra_steps = extra_steps;
+    R.n_acc = n_acc;
+    R.iter = it;
+    unsigned long long* c = J.counters;
+    c[kCntTrials] += c_steps;
+    c[kCntEvaluated] += c_steps;
+    c[kCntDraws] += c_draws;
+    c[kCntAccepted] += c_acc;
+    c[kCntExactPath] += c_exact;
+    if (status != kStatusOk) *J.status = status;
+  }
+}
+
+uint32_t ns_smem_bytes(const Geom& g) {
+  const uint32_t nsp = (uint32_t)g.ns + 1;
+  uint32_t b = align_up((kMTN + kTbufWords) * 4, 16);
+  b += (uint32_t)(g.ns * g.ns * g.nsh) * 8 + nsp * (uint32_t)g.nsh * nsp * 4 + (uint32_t)g.z * 4 +
+       (uint32_t)(g.nsh + 1) * 2;
+  b = align_up(b, 16) + (uint32_t)g.n_sites;
+  return align_up(b, 16);
+}
+
+void launch_ns_init(NsRun* d_runs, int n_runs, cudaStream_t stream) {
+  ns_init_kernel<<<n_runs, 32, 0, stream>>>(d_runs);
+}
+
+void launch_ns_jitter(NsRun* d_runs, int n_runs, int max_K, cudaStream_t stream) {
+  dim3 grid((max_K + 255) / 256, n_runs);
+  ns_jitter_kernel<<<grid, 256, 0, stream>>>(d_runs, n_runs);
+}
+
+void launch_ns_iterate(NsRun* d_runs, int n_runs, uint32_t smem_bytes, cudaStream_t stream) {
+  cudaFuncSetAttribute(ns_iterate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_bytes);
+  ns_iterate_kernel<<<n_runs, 32, smem_bytes, stream>>>(d_runs);
+}
+
+}  // namespace brawl

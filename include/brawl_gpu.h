@@ -188,6 +188,38 @@ int brawl_batch_counters(brawl_batch *batch, int64_t *counters /* n_chains * 8 *
 int brawl_batch_radial_densities(brawl_batch *batch, int chain, int wc_range,
                                  const double *shells, double *rho);
 
+/* ====================================================================== */
+/* Nested sampling (src/nested_sampling.f90:45-206): independent runs,   */
+/* each with its own stream, walkers resident on the device.             */
+/* ====================================================================== */
+typedef struct brawl_ns brawl_ns;
+
+typedef struct brawl_ns_desc {
+    brawl_setup setup;
+    const double *V_ex;
+    uint32_t seed;                         /* init_genrand seed of the run */
+    int n_walkers;                         /* ns_params%n_walkers */
+    int n_steps;                           /* ns_params%n_steps */
+    const double *species_concentrations;  /* n_species+1 ([0] = 0) */
+    const int64_t *species_numbers;        /* n_species or NULL */
+} brawl_ns_desc;
+
+/* Seeds each run and draws its walkers as the reference does: for every
+ * walker initial_setup then one genrand() for the 1e-8 energy jitter; the
+ * walker energies are total_energy + jitter (nested_sampling.f90:78-98). */
+int brawl_ns_create(const brawl_ns_desc *runs, int n_runs, brawl_ns **out);
+int brawl_ns_destroy(brawl_ns *ns);
+/* n_iter iterations of every run (nested_sampling.f90:114-200); limits
+ * receives each iteration's ceiling, run-major (n_runs x n_iter). */
+int brawl_ns_iterate(brawl_ns *ns, int n_iter, double *limits);
+/* The walkers' energies of one run (n_walkers doubles). */
+int brawl_ns_energies(brawl_ns *ns, int run, double *energies);
+/* One walker's configuration, reference layout. */
+int brawl_ns_walker_config(brawl_ns *ns, int run, int walker, int8_t *config);
+/* Counters of one run (BRAWL_NUM_COUNTERS values: [0] walk steps,
+ * [2] words drawn, [3] accepted steps, [5] steps that needed the FP64 sums). */
+int brawl_ns_counters(brawl_ns *ns, int run, int64_t *counters);
+
 #ifdef __cplusplus
 }
 #endif
