@@ -16,7 +16,8 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["load", "Setup", "Chain", "Batch", "NestedSampling", "BrawlError", "LATTICES",
+__all__ = ["load", "Setup", "Chain", "Batch", "NestedSampling", "WangLandauWalkers", "BrawlError",
+           "LATTICES",
            "K_B_IN_RY", "RY_TO_EV"]
 
 # src/constants.f90:41-49 (as written there)
@@ -45,6 +46,12 @@ class _NsDesc(C.Structure):
     _fields_ = [("setup", _Setup), ("V_ex", C.c_void_p), ("seed", C.c_uint32),
                 ("n_walkers", C.c_int), ("n_steps", C.c_int),
                 ("species_concentrations", C.c_void_p), ("species_numbers", C.c_void_p)]
+
+
+class _WlDesc(C.Structure):
+    _fields_ = [("setup", _Setup), ("V_ex", C.c_void_p), ("seed", C.c_uint32),
+                ("config", C.c_void_p), ("start_idx", C.c_int), ("end_idx", C.c_int),
+                ("window", C.c_int)]
 
 
 class _ChainDesc(C.Structure):
@@ -95,6 +102,20 @@ def load(rebuild: bool = False):
         "brawl_ns_energies": ([vp, i, vp], i),
         "brawl_ns_walker_config": ([vp, i, i, vp], i),
         "brawl_ns_counters": ([vp, i, vp], i),
+        "brawl_wl_create": ([vp, i, i, vp, vp], i),
+        "brawl_wl_destroy": ([vp], i),
+        "brawl_wl_sweeps": ([vp, i64, d, i, vp], i),
+        "brawl_wl_average": ([vp], i),
+        "brawl_wl_get_lng": ([vp, i, vp], i),
+        "brawl_wl_set_lng": ([vp, i, vp], i),
+        "brawl_wl_get_hist": ([vp, i, vp], i),
+        "brawl_wl_set_hist": ([vp, i, vp], i),
+        "brawl_wl_energies": ([vp, vp], i),
+        "brawl_wl_get_config": ([vp, i, vp], i),
+        "brawl_wl_set_config": ([vp, i, vp], i),
+        "brawl_wl_swap_configs": ([vp, i, i], i),
+        "brawl_wl_genrand": ([vp, i, i64, vp], i),
+        "brawl_wl_counters": ([vp, i, vp], i),
         "brawl_batch_create": ([vp, i, vp], i),
         "brawl_batch_destroy": ([vp], i),
         "brawl_batch_size": ([vp, vp], i),
@@ -477,4 +498,101 @@ class NestedSampling:
     def counters(self, run: int) -> dict:
         c = np.zeros(NUM_COUNTERS, dtype=np.int64)
         _check(load().brawl_ns_counters(self._h, run, _ptr(c)))
+        return dict(zip(COUNTER_NAMES, (int(v) for v in c)))
+
+
+class WangLandauWalkers:
+    """Wang-Landau walkers resident on the GPU (brawl_wl): sweeps() of
+    every walker and the in-window averages (src/wang-landau.F90:539-632)."""
+
+    def __init__(self, walkers: list[dict], bin_edges):
+        """Each walker: dict(setup, V, seed, config, start_idx, end_idx,
+        window); bin_edges has bins+1 entries."""
+        n = len(walkers)
+        descs = (_WlDesc * n)()
+        keep = []
+        self.walkers = walkers
+        for k, w in enumerate(walkers):
+            s = w["setup"]
+            V = _v_array(s, w["V"])
+            cfg = np.ascontiguousarray(w["config"], dtype=np.int8)
+            keep += [V, cfg]
+            d = descs[k]
+            d.setup = s.c()
+            d.V_ex = V.ctypes.data
+            d.seed = int(w["seed"]) & 0xFFFFFFFF
+            d.config = cfg.ctypes.data
+            d.start_idx = int(w["start_idx"])
+            d.end_idx = int(w["end_idx"])
+            d.window = int(w["window"])
+        self.bin_edges = np.ascontiguousarray(bin_edges, dtype=np.float64)
+        self.bins = self.bin_edges.size - 1
+        h = C.c_void_p()
+        _check(load().brawl_wl_create(descs, n, self.bins, _ptr(self.bin_edges), C.byref(h)))
+        self._h = h
+        self.n = n
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().brawl_wl_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sweeps(self, n_trials: int, wl_f: float, hist_period: int) -> np.ndarray:
+        acc = np.zeros(self.n, dtype=np.int64)
+        _check(load().brawl_wl_sweeps(self._h, int(n_trials), float(wl_f), int(hist_period), _ptr(acc)))
+        return acc
+
+    def average(self) -> None:
+        _check(load().brawl_wl_average(self._h))
+
+    def lng(self, w: int) -> np.ndarray:
+        out = np.zeros(self.bins, dtype=np.float64)
+        _check(load().brawl_wl_get_lng(self._h, w, _ptr(out)))
+        return out
+
+    def set_lng(self, w: int, lng) -> None:
+        a = np.ascontiguousarray(lng, dtype=np.float64)
+        _check(load().brawl_wl_set_lng(self._h, w, _ptr(a)))
+
+    def hist(self, w: int) -> np.ndarray:
+        nb = int(self.walkers[w]["end_idx"]) - int(self.walkers[w]["start_idx"]) + 1
+        out = np.zeros(nb, dtype=np.float64)
+        _check(load().brawl_wl_get_hist(self._h, w, _ptr(out)))
+        return out
+
+    def set_hist(self, w: int, hist) -> None:
+        a = np.ascontiguousarray(hist, dtype=np.float64)
+        _check(load().brawl_wl_set_hist(self._h, w, _ptr(a)))
+
+    def energies(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.float64)
+        _check(load().brawl_wl_energies(self._h, _ptr(out)))
+        return out
+
+    def config(self, w: int) -> np.ndarray:
+        out = np.zeros(self.walkers[w]["setup"].grid_shape, dtype=np.int8)
+        _check(load().brawl_wl_get_config(self._h, w, _ptr(out)))
+        return out
+
+    def set_config(self, w: int, cfg) -> None:
+        a = np.ascontiguousarray(cfg, dtype=np.int8)
+        _check(load().brawl_wl_set_config(self._h, w, _ptr(a)))
+
+    def swap_configs(self, a: int, b: int) -> None:
+        _check(load().brawl_wl_swap_configs(self._h, a, b))
+
+    def genrand(self, w: int, n: int) -> np.ndarray:
+        out = np.zeros(n, dtype=np.float64)
+        _check(load().brawl_wl_genrand(self._h, w, int(n), _ptr(out)))
+        return out
+
+    def counters(self, w: int) -> dict:
+        c = np.zeros(NUM_COUNTERS, dtype=np.int64)
+        _check(load().brawl_wl_counters(self._h, w, _ptr(c)))
         return dict(zip(COUNTER_NAMES, (int(v) for v in c)))

@@ -1301,3 +1301,234 @@ extern "C" int brawl_ns_counters(brawl_ns* ns, int run, int64_t* counters) {
   CUDA_TRY(cudaMemcpy(counters, ns->runs[run].job.counters, kNumCounters * 8, cudaMemcpyDeviceToHost));
   return BRAWL_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Wang-Landau walkers: a batch (lattices, streams, tables, energies) plus
+// ln g and histogram buffers.
+// ---------------------------------------------------------------------------
+#include "wl_kernels.cuh"
+
+struct brawl_wl {
+  brawl_batch* b = nullptr;
+  int bins = 0;
+  double e1 = 0.0, range = 0.0;
+  std::vector<WlWalker> w;
+  std::vector<WlGroup> groups;
+  WlWalker* d_w = nullptr;
+  WlGroup* d_groups = nullptr;
+  double* d_lng = nullptr;
+  double* d_hist = nullptr;
+  uint32_t smem = 0;
+};
+
+namespace {
+int batch_genrand(brawl_batch* b, int c, int64_t n, double* out) {
+  uint32_t st[kMTN + 1];
+  TRY(brawl_batch_rng_get(b, c, st));
+  int pos = (int)st[kMTN];
+  for (int64_t i = 0; i < n; ++i) {
+    if (pos >= kMTN) {
+      for (int k = 0; k < kMTN; ++k) {
+        uint32_t y = (st[k] & 0x80000000u) | (st[(k + 1) % kMTN] & 0x7fffffffu);
+        st[k] = st[(k + kMTM) % kMTN] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      }
+      pos = 0;
+    }
+    uint32_t y = st[pos++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    out[i] = (double)y * (1.0 / 4294967296.0);
+  }
+  st[kMTN] = (uint32_t)pos;
+  CUDA_TRY(cudaMemcpyAsync(b->jobs[c].rng, st, sizeof(st), cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+}  // namespace
+
+extern "C" int brawl_wl_destroy(brawl_wl* wl) {
+  if (!wl) return BRAWL_OK;
+  if (wl->b) brawl_batch_destroy(wl->b);
+  if (wl->d_w) cudaFree(wl->d_w);
+  if (wl->d_groups) cudaFree(wl->d_groups);
+  if (wl->d_lng) cudaFree(wl->d_lng);
+  if (wl->d_hist) cudaFree(wl->d_hist);
+  delete wl;
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
+                               const double* bin_edges, brawl_wl** out) {
+  if (!walkers || !out || n < 1 || bins < 1 || !bin_edges) return fail(BRAWL_EINVAL, "bad argument");
+  *out = nullptr;
+  for (int c = 0; c < n; ++c) {
+    if (!walkers[c].config) return fail(BRAWL_EINVAL, "walker " + std::to_string(c) + ": config required");
+    if (walkers[c].start_idx < 1 || walkers[c].end_idx > bins || walkers[c].start_idx > walkers[c].end_idx)
+      return fail(BRAWL_EINVAL, "walker " + std::to_string(c) + ": window outside 1..bins");
+    for (int k = 0; k < c; ++k)
+      if (walkers[k].window == walkers[c].window && walkers[c - 1].window != walkers[c].window)
+        return fail(BRAWL_EINVAL, "walkers of a window must be consecutive");
+  }
+  std::vector<brawl_chain_desc> d(n);
+  for (int c = 0; c < n; ++c) {
+    std::memset(&d[c], 0, sizeof(d[c]));
+    d[c].setup = walkers[c].setup;
+    d[c].V_ex = walkers[c].V_ex;
+    d[c].seed = walkers[c].seed;
+    d[c].config = walkers[c].config;
+  }
+  brawl_wl* wl = new brawl_wl();
+  auto cleanup = [&](int rc) {
+    brawl_wl_destroy(wl);
+    return rc;
+  };
+  int rc = brawl_batch_create(d.data(), n, &wl->b);
+  if (rc != BRAWL_OK) return cleanup(rc);
+  wl->bins = bins;
+  wl->e1 = bin_edges[0];
+  wl->range = bin_edges[bins] - bin_edges[0];
+  size_t hist_total = 0;
+  for (int c = 0; c < n; ++c) hist_total += walkers[c].end_idx - walkers[c].start_idx + 1;
+  if (cudaMalloc(&wl->d_lng, (size_t)n * bins * 8) != cudaSuccess ||
+      cudaMalloc(&wl->d_hist, hist_total * 8) != cudaSuccess ||
+      cudaMalloc(&wl->d_w, n * sizeof(WlWalker)) != cudaSuccess)
+    return cleanup(fail(BRAWL_ENOMEM, "walker buffers"));
+  cudaMemset(wl->d_lng, 0, (size_t)n * bins * 8);
+  cudaMemset(wl->d_hist, 0, hist_total * 8);
+  wl->w.resize(n);
+  size_t hoff = 0;
+  int max_optin = 0;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, wl->b->device);
+  for (int c = 0; c < n; ++c) {
+    WlWalker& W = wl->w[c];
+    std::memset(&W, 0, sizeof(W));
+    W.job = wl->b->jobs[c];
+    W.lng = wl->d_lng + (size_t)c * bins;
+    W.hist = wl->d_hist + hoff;
+    W.start = walkers[c].start_idx;
+    W.end = walkers[c].end_idx;
+    W.bins = bins;
+    W.e1 = wl->e1;
+    W.range = wl->range;
+    hoff += W.end - W.start + 1;
+    wl->smem = std::max(wl->smem, wl_smem_bytes(W.job.g, W.end - W.start + 1));
+    if (c == 0 || walkers[c].window != walkers[c - 1].window) wl->groups.push_back({c, 0});
+    wl->groups.back().count += 1;
+  }
+  if (wl->smem > (uint32_t)max_optin) return cleanup(fail(BRAWL_EINVAL, "window or lattice too large for shared memory"));
+  if (cudaMalloc(&wl->d_groups, wl->groups.size() * sizeof(WlGroup)) != cudaSuccess)
+    return cleanup(fail(BRAWL_ENOMEM, "groups"));
+  cudaMemcpy(wl->d_groups, wl->groups.data(), wl->groups.size() * sizeof(WlGroup), cudaMemcpyHostToDevice);
+  *out = wl;
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_sweeps(brawl_wl* wl, int64_t n_trials, double wl_f, int hist_period,
+                               int64_t* accepted) {
+  if (!wl || n_trials < 0) return fail(BRAWL_EINVAL, "bad argument");
+  brawl_batch* b = wl->b;
+  const int n = (int)wl->w.size();
+  std::vector<double> e0(n);
+  TRY(brawl_batch_total_energy(b, e0.data()));
+  for (int c = 0; c < n; ++c) {
+    WlWalker& W = wl->w[c];
+    W.e0 = e0[c];
+    W.wl_f = wl_f;
+    W.n_trials = n_trials;
+    W.hist_period = hist_period;
+  }
+  CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), n * sizeof(WlWalker), cudaMemcpyHostToDevice, b->stream));
+  launch_wl_sweeps(wl->d_w, n, wl->smem, b->stream);
+  launch_wl_average(wl->d_groups, (int)wl->groups.size(), wl->d_w, wl->bins, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  std::vector<WlWalker> res(n);
+  CUDA_TRY(cudaMemcpyAsync(res.data(), wl->d_w, n * sizeof(WlWalker), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (accepted)
+    for (int c = 0; c < n; ++c) accepted[c] = res[c].accepted;
+  int r = check_status(b);
+  if (r != BRAWL_OK) return fail(BRAWL_ESTATE, "a walker's energy is outside its window");
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_average(brawl_wl* wl) {
+  if (!wl) return fail(BRAWL_EINVAL, "null argument");
+  CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), wl->w.size() * sizeof(WlWalker), cudaMemcpyHostToDevice, wl->b->stream));
+  launch_wl_average(wl->d_groups, (int)wl->groups.size(), wl->d_w, wl->bins, wl->b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_get_lng(brawl_wl* wl, int c, double* lng) {
+  if (!wl || !lng || c < 0 || c >= (int)wl->w.size()) return fail(BRAWL_EINVAL, "bad argument");
+  CUDA_TRY(cudaMemcpy(lng, wl->w[c].lng, (size_t)wl->bins * 8, cudaMemcpyDeviceToHost));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_set_lng(brawl_wl* wl, int c, const double* lng) {
+  if (!wl || !lng || c < 0 || c >= (int)wl->w.size()) return fail(BRAWL_EINVAL, "bad argument");
+  CUDA_TRY(cudaMemcpy(wl->w[c].lng, lng, (size_t)wl->bins * 8, cudaMemcpyHostToDevice));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_get_hist(brawl_wl* wl, int c, double* hist) {
+  if (!wl || !hist || c < 0 || c >= (int)wl->w.size()) return fail(BRAWL_EINVAL, "bad argument");
+  const WlWalker& W = wl->w[c];
+  CUDA_TRY(cudaMemcpy(hist, W.hist, (size_t)(W.end - W.start + 1) * 8, cudaMemcpyDeviceToHost));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_set_hist(brawl_wl* wl, int c, const double* hist) {
+  if (!wl || !hist || c < 0 || c >= (int)wl->w.size()) return fail(BRAWL_EINVAL, "bad argument");
+  const WlWalker& W = wl->w[c];
+  CUDA_TRY(cudaMemcpy(W.hist, hist, (size_t)(W.end - W.start + 1) * 8, cudaMemcpyHostToDevice));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_energies(brawl_wl* wl, double* energies) {
+  if (!wl || !energies) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_total_energy(wl->b, energies);
+}
+
+extern "C" int brawl_wl_get_config(brawl_wl* wl, int c, int8_t* config) {
+  if (!wl) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_get_config(wl->b, c, config);
+}
+
+extern "C" int brawl_wl_set_config(brawl_wl* wl, int c, const int8_t* config) {
+  if (!wl) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_set_config(wl->b, c, config);
+}
+
+extern "C" int brawl_wl_swap_configs(brawl_wl* wl, int a, int c) {
+  if (!wl || a < 0 || c < 0 || a >= (int)wl->w.size() || c >= (int)wl->w.size())
+    return fail(BRAWL_EINVAL, "bad argument");
+  if (a == c) return BRAWL_OK;
+  brawl_batch* b = wl->b;
+  const Geom& ga = b->models[a].g;
+  const Geom& gc = b->models[c].g;
+  if (ga.lattice != gc.lattice || ga.n1 != gc.n1 || ga.n2 != gc.n2 || ga.n3 != gc.n3)
+    return fail(BRAWL_EINVAL, "walkers have different lattices");
+  TRY(ensure_grid(b, (size_t)ga.n_sites));
+  CUDA_TRY(cudaMemcpyAsync(b->d_grid, b->jobs[a].lat, ga.n_sites, cudaMemcpyDeviceToDevice, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(b->jobs[a].lat, b->jobs[c].lat, ga.n_sites, cudaMemcpyDeviceToDevice, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(b->jobs[c].lat, b->d_grid, ga.n_sites, cudaMemcpyDeviceToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_genrand(brawl_wl* wl, int c, int64_t n, double* out) {
+  if (!wl || c < 0 || c >= (int)wl->w.size() || n < 0 || (n > 0 && !out)) return fail(BRAWL_EINVAL, "bad argument");
+  return batch_genrand(wl->b, c, n, out);
+}
+
+extern "C" int brawl_wl_counters(brawl_wl* wl, int c, int64_t* counters) {
+  if (!wl || !counters || c < 0 || c >= (int)wl->w.size()) return fail(BRAWL_EINVAL, "bad argument");
+  std::vector<int64_t> all(wl->w.size() * kNumCounters);
+  TRY(brawl_batch_counters(wl->b, all.data()));
+  std::copy(all.begin() + (size_t)c * kNumCounters, all.begin() + (size_t)(c + 1) * kNumCounters, counters);
+  return BRAWL_OK;
+}

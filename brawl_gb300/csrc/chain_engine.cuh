@@ -54,6 +54,7 @@ enum Status : int {
   kStatusOk = 0,
   kStatusRngInvariant = 1,   // stream position left its block (internal error)
   kStatusBadSpecies = 2,     // a species code outside 1..ns was met
+  kStatusWalkerOutsideWindow = 3,  // a Wang-Landau walker's energy left its window
 };
 
 struct Geom {

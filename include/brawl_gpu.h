@@ -220,6 +220,52 @@ int brawl_ns_walker_config(brawl_ns *ns, int run, int walker, int8_t *config);
  * [2] words drawn, [3] accepted steps, [5] steps that needed the FP64 sums). */
 int brawl_ns_counters(brawl_ns *ns, int run, int64_t *counters);
 
+/* ====================================================================== */
+/* Wang-Landau walkers (src/wang-landau.F90): sweeps of every walker and  */
+/* the in-window average that follows them, with ln g, the histograms,    */
+/* the configurations and the streams resident on the device.             */
+/* ====================================================================== */
+typedef struct brawl_wl brawl_wl;
+
+typedef struct brawl_wl_desc {
+    brawl_setup setup;
+    const double *V_ex;
+    uint32_t seed;                         /* the walker's (rank's) stream */
+    const int8_t *config;                  /* start config (reference layout) */
+    int start_idx, end_idx;                /* 1-based window bins (window_indices) */
+    int window;                            /* walkers of a window are averaged together */
+} brawl_wl_desc;
+
+/* Walkers of one Wang-Landau simulation; bin_edges has bins+1 entries
+ * (create_energy_bins, src/wang-landau.F90:969-992).  Walkers of the same
+ * window must be consecutive; ln g starts at zero. */
+int brawl_wl_create(const brawl_wl_desc *walkers, int n_walkers, int bins,
+                    const double *bin_edges, brawl_wl **out);
+int brawl_wl_destroy(brawl_wl *wl);
+/* sweeps() on every walker (src/wang-landau.F90:539-632): e_unswapped from
+ * full_energy, n_trials = mc_sweeps*n_atoms trials adding wl_f to ln g, a
+ * histogram tick every hist_period trials, then ln g and the histograms
+ * averaged over the walkers of each window.  accepted (may be NULL)
+ * receives each walker's accepted moves.  BRAWL_ESTATE if a walker's
+ * energy is outside its window (the reference would index outside its
+ * histogram). */
+int brawl_wl_sweeps(brawl_wl *wl, int64_t n_trials, double wl_f, int hist_period,
+                    int64_t *accepted);
+/* dos_average (src/wang-landau.F90:1127-1133): the window average alone. */
+int brawl_wl_average(brawl_wl *wl);
+int brawl_wl_get_lng(brawl_wl *wl, int walker, double *lng);        /* bins */
+int brawl_wl_set_lng(brawl_wl *wl, int walker, const double *lng);
+int brawl_wl_get_hist(brawl_wl *wl, int walker, double *hist);      /* window bins */
+int brawl_wl_set_hist(brawl_wl *wl, int walker, const double *hist);
+int brawl_wl_energies(brawl_wl *wl, double *energies);              /* full_energy per walker */
+int brawl_wl_get_config(brawl_wl *wl, int walker, int8_t *config);
+int brawl_wl_set_config(brawl_wl *wl, int walker, const int8_t *config);
+/* Exchange the configurations of two walkers (replica_exchange's swap). */
+int brawl_wl_swap_configs(brawl_wl *wl, int a, int b);
+/* n genrand() draws from a walker's stream (exchange shuffles and tests). */
+int brawl_wl_genrand(brawl_wl *wl, int walker, int64_t n, double *out);
+int brawl_wl_counters(brawl_wl *wl, int walker, int64_t *counters);
+
 #ifdef __cplusplus
 }
 #endif

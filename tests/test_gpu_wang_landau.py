@@ -1,0 +1,96 @@
+"""GPU Wang-Landau walker updates against the oracle: sweeps() of every
+walker followed by the in-window average (walker order), bit for bit --
+ln g, histograms, configurations, accepted moves and the streams."""
+import numpy as np
+import pytest
+
+import brawl_gb300 as B
+from oracle import oracle as O
+from tests.test_gpu_metropolis import conc_vector, random_V
+
+pytestmark = pytest.mark.gpu
+
+
+def _emulate(mods, cfgs, rngs, walkers, bin_edges, lngs, hists, n_trials, wl_f, period):
+    bins = bin_edges.size - 1
+    acc = []
+    for k, w in enumerate(walkers):
+        e = mods[k].total_energy(cfgs[k])
+        a, _, _ = mods[k].wl_sweep(cfgs[k], rngs[k], bin_edges, lngs[k], hists[k], e, bins,
+                                   w["start_idx"], w["end_idx"], n_trials, wl_f, period)
+        acc.append(a)
+    windows = sorted(set(w["window"] for w in walkers))
+    for win in windows:
+        idx = [k for k, w in enumerate(walkers) if w["window"] == win]
+        if len(idx) < 2:
+            continue
+        inv = float(np.float32(len(idx)))
+        for arrs in (lngs, hists):
+            s = arrs[idx[0]].copy()
+            for k in idx[1:]:
+                s = s + arrs[k]
+            s = s / inv
+            for k in idx:
+                arrs[k][:] = s
+    return acc
+
+
+@pytest.mark.parametrize("lattice,n,ns,nsh,windows", [
+    ("bcc", (4, 4, 4), 4, 6, [(1, 30), (19, 48)]),
+    ("fcc", (3, 3, 3), 3, 3, [(10, 30), (20, 40), (18, 44)]),
+])
+def test_wang_landau_sweeps_match_oracle(lattice, n, ns, nsh, windows):
+    rng = np.random.default_rng(21)
+    V = random_V(rng, ns, nsh)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    mod0 = O.OracleModel(lattice, *n, V)
+    walkers, mods, cfgs, rngs = [], [], [], []
+    r0 = O.OracleRng(4242)
+    for win, (lo, hi) in enumerate(windows):
+        for rep in range(2):
+            cfg, _ = mod0.initial_setup(r0, conc_vector(ns))
+            seed = 110179 + 11 * len(walkers)
+            walkers.append(dict(setup=setup, V=V, seed=seed, config=cfg.copy(), start_idx=lo,
+                                end_idx=hi, window=win))
+            mods.append(O.OracleModel(lattice, *n, V))
+            cfgs.append(cfg.copy())
+            rngs.append(O.OracleRng(seed))
+    E = np.array([mod0.total_energy(c) for c in cfgs])
+    bins = 48
+    # bins around the walkers' energies so each starts inside every window
+    half = max(float(np.ptp(E)), 0.02) * 4.0
+    mid = float(E.mean())
+    bin_edges = mid - half + (np.arange(bins + 1) * (2 * half / bins))
+    bidx = [O.wl_bin_index(e, bin_edges, bins) for e in E]
+    assert all(lo <= b <= hi for b, (lo, hi) in zip(bidx, [windows[w["window"]] for w in walkers]))
+    lngs = [np.zeros(bins) for _ in walkers]
+    hists = [np.zeros(w["end_idx"] - w["start_idx"] + 1) for w in walkers]
+    wl = B.WangLandauWalkers(walkers, bin_edges)
+    wl_f = float(np.float32(0.05))
+    period = int(0.02 * float(np.float32(setup.n_atoms)))
+    for call in range(3):
+        acc_o = _emulate(mods, cfgs, rngs, walkers, bin_edges, lngs, hists, 700, wl_f, period)
+        acc_g = wl.sweeps(700, wl_f, period)
+        assert list(acc_g) == acc_o
+        for k in range(len(walkers)):
+            assert np.array_equal(wl.lng(k), lngs[k])
+            assert np.array_equal(wl.hist(k), hists[k])
+            assert np.array_equal(wl.config(k), cfgs[k])
+    for k in range(len(walkers)):
+        assert np.array_equal(wl.genrand(k, 20), np.array([rngs[k].uniform() for _ in range(20)]))
+    assert np.array_equal(wl.energies(), np.array([mods[k].total_energy(cfgs[k]) for k in range(len(walkers))]))
+
+
+def test_wang_landau_walker_outside_window_is_reported():
+    rng = np.random.default_rng(3)
+    V = random_V(rng, 2, 2)
+    setup = B.Setup("bcc", 3, 3, 3, 2, 2)
+    mod = O.OracleModel("bcc", 3, 3, 3, V)
+    cfg, _ = mod.initial_setup(O.OracleRng(5), conc_vector(2))
+    e = mod.total_energy(cfg)
+    bin_edges = e + 1.0 + np.arange(11) * 0.1      # every bin above the walker
+    wl = B.WangLandauWalkers([dict(setup=setup, V=V, seed=1, config=cfg, start_idx=1,
+                                   end_idx=10, window=0)], bin_edges)
+    with pytest.raises(B.BrawlError) as ex:
+        wl.sweeps(10, 0.05, 1)
+    assert ex.value.code == 6
