@@ -203,13 +203,65 @@ def measured_peaks() -> dict:
 
 
 def committed_traffic() -> dict | None:
-    """Per-trial DRAM traffic of the Metropolis kernel from the committed ncu
-    summary (profiles/metropolis_batched_traffic.json), if present."""
+    """DRAM traffic per launch of the Metropolis kernel on the 1024-replica
+    workload, from the committed ncu summary
+    (profiles/metropolis_batched_traffic.json), if present."""
     p = os.path.join(ROOT, "profiles", "metropolis_batched_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
             return json.load(f)
     return None
+
+
+def serving_leg(args) -> dict:
+    """The mixed job stream through the serving loop (brawl_serve_*):
+    Poisson arrivals at args.serve_rate jobs/s, latency = finish - submit
+    per job, throughput = swap trials of all jobs / makespan."""
+    from brawl_gb300 import serving as SV
+    jobs = SV.stream_jobs(args.serve_jobs, master_seed=424242, L_range=(6, args.serve_L_max),
+                          sweeps_range=(100, args.serve_sweeps_max))
+    rng = np.random.default_rng(99)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, len(jobs)))
+    with SV.Server() as srv:
+        ids = []
+        t0 = time.perf_counter()
+        for job, t in zip(jobs, arrivals):
+            dt = t0 + t - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(job))
+        res = [srv.wait(i) for i in ids]
+        makespan = time.perf_counter() - t0
+        stats = srv.stats()
+    ok = [r for r in res if r["status"] == 0]
+    failed = {}
+    for job, r in zip(jobs, res):
+        if r["status"] != 0:
+            key = f'{job["kind"]}:{r["status"]}'
+            failed[key] = failed.get(key, 0) + 1
+    lat = np.array([r["t_finish"] - r["t_submit"] for r in ok])
+    queue = np.array([r["t_admit"] - r["t_submit"] for r in ok])
+    by_kind = {}
+    for job, r in zip(jobs, res):
+        if r["status"] == 0:
+            by_kind.setdefault(job["kind"], []).append(r["t_finish"] - r["t_submit"])
+    trials = sum(SV.job_trials(j) for j, r in zip(jobs, res) if r["status"] == 0 and j["kind"] != "ns")
+    ns_steps = sum(int(r["trials"]) for j, r in zip(jobs, res) if r["status"] == 0 and j["kind"] == "ns")
+    return {
+        "stream": f"{len(jobs)} jobs of the seeded mixed stream: fcc/bcc, L in [6,{args.serve_L_max}], "
+                  f"2-5 species (Dirichlet composition), 2-6 shells; anneal {100}-{args.serve_sweeps_max} "
+                  "sweeps over 4 temperatures, WL window (4 walkers x 20 one-sweep calls), "
+                  "NS run (64 walkers, 100 iterations of one-sweep walks)",
+        "arrivals": f"Poisson, {args.serve_rate} jobs/s",
+        "jobs_ok": len(ok), "jobs_failed": failed,
+        "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+        "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+        "p50_queue_s": float(np.percentile(queue, 50)) if len(queue) else None,
+        "p50_by_kind_s": {k: float(np.percentile(v, 50)) for k, v in by_kind.items()},
+        "makespan_s": makespan,
+        "trials_per_s": (trials + ns_steps) / makespan,
+        "rounds": stats["rounds"],
+    }
 
 
 def dist_setup():
@@ -262,6 +314,11 @@ def main() -> int:
     ap.add_argument("--sweeps-per-step", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-jobs", type=int, default=150)
+    ap.add_argument("--serve-rate", type=float, default=15.0)
+    ap.add_argument("--serve-L-max", type=int, default=16)
+    ap.add_argument("--serve-sweeps-max", type=int, default=500)
+    ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -344,8 +401,8 @@ def main() -> int:
     peaks = measured_peaks()
     traffic = None
     tr = committed_traffic()
-    if tr and tr.get("dram_bytes_per_trial"):
-        traffic = float(tr["dram_bytes_per_trial"]) * T_all / args.steps
+    if tr and tr.get("dram_bytes_per_launch") and args.replicas == 1024:
+        traffic = float(tr["dram_bytes_per_launch"])     # one launch per step
 
     # ---- end to end through the C ABI with host buffers -------------------
     grid_bytes = batch.grid_bytes
@@ -393,6 +450,10 @@ def main() -> int:
                "sample": f"{cores} replicas of the workload (spread over L), {each} trials each, "
                          f"one process per core, {w:.1f} s"}
 
+    serving = None
+    if rank == 0 and world == 1 and not args.no_serve and args.serve_jobs > 0:
+        serving = serving_leg(args)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "trials/s", "n_gpus": world,
@@ -417,6 +478,7 @@ def main() -> int:
             "plain_gpu": {"value": plain_value, "unit": "trials/s",
                           "sample": f"{len(sample)} replicas, 1 sweep each, one launch per replica"},
             "batched_over_plain": value / plain_value,
+            "serving": serving,
             "clocks": clk,
             "gpu_launches": args.steps,
             "counters": {"trials": T_all, "evaluated": T_eval, "draws": draws,

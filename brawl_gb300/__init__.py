@@ -116,6 +116,20 @@ def load(rebuild: bool = False):
         "brawl_wl_swap_configs": ([vp, i, i], i),
         "brawl_wl_genrand": ([vp, i, i64, vp], i),
         "brawl_wl_counters": ([vp, i, vp], i),
+        "brawl_wl_replica_exchange": ([vp, vp, vp, vp], i),
+        "brawl_wl_flatness": ([vp, vp], i),
+        "brawl_wl_dos_combine": ([vp, vp], i),
+        "brawl_wl_reset_hist": ([vp], i),
+        "brawl_serve_create": ([vp, vp], i),
+        "brawl_serve_destroy": ([vp], i),
+        "brawl_serve_submit": ([vp, vp, vp], i),
+        "brawl_serve_poll": ([vp, C.c_uint64, vp], i),
+        "brawl_serve_wait": ([vp, C.c_uint64, d, vp], i),
+        "brawl_serve_values": ([vp, C.c_uint64, vp], i),
+        "brawl_serve_config": ([vp, C.c_uint64, vp], i),
+        "brawl_serve_release": ([vp, C.c_uint64], i),
+        "brawl_serve_stats": ([vp, vp], i),
+        "brawl_serve_profile": ([vp, vp], i),
         "brawl_batch_create": ([vp, i, vp], i),
         "brawl_batch_destroy": ([vp], i),
         "brawl_batch_size": ([vp, vp], i),
@@ -549,7 +563,31 @@ class WangLandauWalkers:
         return acc
 
     def average(self) -> None:
+        """dos_average: ln g averaged over each window's walkers."""
         _check(load().brawl_wl_average(self._h))
+
+    def replica_exchange(self) -> tuple[int, np.ndarray, np.ndarray]:
+        """replica_exchange: (accepted pairs, partner per walker or -1,
+        exchanged flag per walker)."""
+        partner = np.zeros(self.n, dtype=np.int32)
+        exch = np.zeros(self.n, dtype=np.int32)
+        na = C.c_int()
+        _check(load().brawl_wl_replica_exchange(self._h, _ptr(partner), _ptr(exch), C.byref(na)))
+        return int(na.value), partner, exch
+
+    def flatness(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.float64)
+        _check(load().brawl_wl_flatness(self._h, _ptr(out)))
+        return out
+
+    def dos_combine(self) -> np.ndarray:
+        """dos_combine: the stitched ln g, also written to every walker."""
+        out = np.zeros(self.bins, dtype=np.float64)
+        _check(load().brawl_wl_dos_combine(self._h, _ptr(out)))
+        return out
+
+    def reset_hist(self) -> None:
+        _check(load().brawl_wl_reset_hist(self._h))
 
     def lng(self, w: int) -> np.ndarray:
         out = np.zeros(self.bins, dtype=np.float64)

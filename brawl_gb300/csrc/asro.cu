@@ -101,6 +101,7 @@ void launch_asro(const AsroJob* d_job, const Geom& g, int n_class, cudaStream_t 
   const int nsp = g.ns + 1;
   const size_t smem = (size_t)(nsp * nsp * n_class + nsp) * 4;
   cudaFuncSetAttribute(asro_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  BRAWL_CARVEOUT(asro_kernel);
   asro_kernel<<<blocks, 256, smem, stream>>>(d_job);
 }
 

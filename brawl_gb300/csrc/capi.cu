@@ -37,6 +37,18 @@ int fail(int code, const std::string& msg) {
     }                                                                                 \
   } while (0)
 
+// Device memory of the objects is stream-ordered (cudaMallocAsync /
+// cudaFreeAsync on the object's own stream): creating and destroying an
+// object never waits for kernels of other streams, so a serving loop keeps
+// other jobs' work in flight while objects come and go.
+template <typename T>
+cudaError_t dalloc(T** p, size_t bytes, cudaStream_t s) {
+  return cudaMallocAsync(reinterpret_cast<void**>(p), bytes, s);
+}
+inline void dfree(const void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(const_cast<void*>(p), s);
+}
+
 #define TRY(x)                 \
   do {                         \
     int r_ = (x);              \
@@ -351,7 +363,8 @@ int check_status(brawl_batch* b) {
   for (size_t i = 0; i < st.size(); ++i)
     if (st[i] != 0) {
       int32_t zero = 0;
-      cudaMemcpy(b->d_status + i, &zero, 4, cudaMemcpyHostToDevice);
+      cudaMemcpyAsync(b->d_status + i, &zero, 4, cudaMemcpyHostToDevice, b->stream);
+      cudaStreamSynchronize(b->stream);
       return fail(BRAWL_ESTATE, "device check failed on chain " + std::to_string(i) + " (code " +
                                     std::to_string(st[i]) + ")");
     }
@@ -360,10 +373,10 @@ int check_status(brawl_batch* b) {
 
 int ensure_grid(brawl_batch* b, size_t bytes) {
   if (bytes <= b->grid_cap) return BRAWL_OK;
-  if (b->d_grid) cudaFree(b->d_grid);
+  dfree(b->d_grid, b->stream);
   b->d_grid = nullptr;
   b->grid_cap = 0;
-  CUDA_TRY(cudaMalloc(&b->d_grid, bytes));
+  CUDA_TRY(dalloc(&b->d_grid, bytes, b->stream));
   b->grid_cap = bytes;
   return BRAWL_OK;
 }
@@ -548,7 +561,7 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
   total = al(total + (size_t)n_chains * 8);
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
     return cleanup(fail(BRAWL_ECUDA, "stream create failed"));
-  cudaError_t e = cudaMalloc(&b->arena, total);
+  cudaError_t e = dalloc(&b->arena, total, b->stream);
   if (e != cudaSuccess) {
     b->arena = nullptr;
     return cleanup(fail(BRAWL_ENOMEM, std::string("arena: ") + cudaGetErrorString(e)));
@@ -588,7 +601,8 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
   b->d_status = reinterpret_cast<int32_t*>(b->arena + off_status);
   b->d_energy = reinterpret_cast<double*>(b->arena + off_energy);
   std::memcpy(&h[off_jobs], b->jobs.data(), n_chains * sizeof(ChainJob));
-  e = cudaMemcpy(b->arena, h.data(), total, cudaMemcpyHostToDevice);
+  e = cudaMemcpyAsync(b->arena, h.data(), total, cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
   b->last_counters.assign((size_t)n_chains * kNumCounters, 0);
   // configurations: given ones are packed, the others drawn by initial_setup
@@ -615,13 +629,13 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
   }
   if (!init.empty()) {
     InitJob* d_init = nullptr;
-    e = cudaMalloc(&d_init, init.size() * sizeof(InitJob));
+    e = dalloc(&d_init, init.size() * sizeof(InitJob), b->stream);
     if (e != cudaSuccess) return cleanup(fail(BRAWL_ENOMEM, cudaGetErrorString(e)));
     cudaMemcpyAsync(d_init, init.data(), init.size() * sizeof(InitJob), cudaMemcpyHostToDevice,
                     b->stream);
     launch_initial_setup(d_init, (int)init.size(), b->stream);
+    dfree(d_init, b->stream);
     e = cudaStreamSynchronize(b->stream);
-    cudaFree(d_init);
     if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
     int r = check_status(b);
     if (r != BRAWL_OK) return cleanup(r);
@@ -638,14 +652,13 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
 
 int brawl_batch_destroy(brawl_batch* b) {
   if (!b) return BRAWL_OK;
-  if (b->stream) cudaStreamSynchronize(b->stream);
-  if (b->arena) cudaFree(b->arena);
-  if (b->d_site_e) cudaFree(b->d_site_e);
-  if (b->d_grid) cudaFree(b->d_grid);
-  if (b->d_grids) cudaFree(b->d_grids);
-  if (b->d_gjobs) cudaFree(b->d_gjobs);
-  if (b->d_scratch) cudaFree(b->d_scratch);
-  if (b->stream) cudaStreamDestroy(b->stream);
+  if (b->stream) {
+    for (const void* p : {(const void*)b->arena, (const void*)b->d_site_e, (const void*)b->d_grid,
+                          (const void*)b->d_grids, (const void*)b->d_gjobs, (const void*)b->d_scratch})
+      dfree(p, b->stream);
+    cudaStreamSynchronize(b->stream);
+    cudaStreamDestroy(b->stream);
+  }
   delete b;
   return BRAWL_OK;
 }
@@ -687,16 +700,16 @@ int brawl_batch_metropolis_run_serial(brawl_batch* b, const int64_t* n_trials, i
   return run_metropolis(b, n_trials, accepted, true, b->stream, true);
 }
 
-int brawl_batch_total_energy(brawl_batch* b, double* energies) {
-  if (!b || !energies) return fail(BRAWL_EINVAL, "null argument");
+// Queues full_energy of every chain into b->d_energy on the batch stream.
+static int queue_batch_energy(brawl_batch* b) {
   const int n = (int)b->jobs.size();
   int64_t total_sites = 0;
   for (int c = 0; c < n; ++c) total_sites += b->models[c].g.n_sites;
   if ((size_t)total_sites * 8 > b->site_e_cap) {
-    if (b->d_site_e) cudaFree(b->d_site_e);
+    dfree(b->d_site_e, b->stream);
     b->d_site_e = nullptr;
     b->site_e_cap = 0;
-    CUDA_TRY(cudaMalloc(&b->d_site_e, (size_t)total_sites * 8));
+    CUDA_TRY(dalloc(&b->d_site_e, (size_t)total_sites * 8, b->stream));
     b->site_e_cap = (size_t)total_sites * 8;
   }
   std::vector<EnergyJob> ej(n);
@@ -717,6 +730,13 @@ int brawl_batch_total_energy(brawl_batch* b, double* energies) {
                            b->stream));
   launch_total_energy(b->d_ejobs, n, total_sites, b->stream);
   CUDA_TRY(cudaGetLastError());
+  return BRAWL_OK;
+}
+
+int brawl_batch_total_energy(brawl_batch* b, double* energies) {
+  if (!b || !energies) return fail(BRAWL_EINVAL, "null argument");
+  TRY(queue_batch_energy(b));
+  const int n = (int)b->jobs.size();
   CUDA_TRY(cudaMemcpyAsync(energies, b->d_energy, n * 8, cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   return BRAWL_OK;
@@ -751,9 +771,10 @@ static int ensure_grids(brawl_batch* b) {
     gj[c].status = b->jobs[c].status;
     off += (int64_t)8 * gj[c].g.n1 * gj[c].g.n2 * gj[c].g.n3;
   }
-  CUDA_TRY(cudaMalloc(&b->d_grids, (size_t)off));
-  CUDA_TRY(cudaMalloc(&b->d_gjobs, n * sizeof(GridJob)));
-  CUDA_TRY(cudaMemcpy(b->d_gjobs, gj.data(), n * sizeof(GridJob), cudaMemcpyHostToDevice));
+  CUDA_TRY(dalloc(&b->d_grids, (size_t)off, b->stream));
+  CUDA_TRY(dalloc(&b->d_gjobs, n * sizeof(GridJob), b->stream));
+  CUDA_TRY(cudaMemcpyAsync(b->d_gjobs, gj.data(), n * sizeof(GridJob), cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->total_cells = off;
   return BRAWL_OK;
 }
@@ -808,10 +829,10 @@ int brawl_batch_radial_densities(brawl_batch* b, int c, int wc_range, const doub
   const size_t n_counts = (size_t)nsp * nsp * plan.n_class + nsp;
   const size_t bytes = plan.offsets.size() * 4 + 256 + n_counts * 8;
   if (bytes > b->scratch_cap) {
-    if (b->d_scratch) cudaFree(b->d_scratch);
+    dfree(b->d_scratch, b->stream);
     b->d_scratch = nullptr;
     b->scratch_cap = 0;
-    CUDA_TRY(cudaMalloc(&b->d_scratch, bytes));
+    CUDA_TRY(dalloc(&b->d_scratch, bytes, b->stream));
     b->scratch_cap = bytes;
   }
   unsigned char* s = reinterpret_cast<unsigned char*>(b->d_scratch);
@@ -987,11 +1008,11 @@ int brawl_initial_setup(brawl_ctx* ctx, double* conc, const int64_t* numbers) {
   ij.counters = b->jobs[0].counters;
   ij.status = b->jobs[0].status;
   InitJob* d = nullptr;
-  CUDA_TRY(cudaMalloc(&d, sizeof(InitJob)));
+  CUDA_TRY(dalloc(&d, sizeof(InitJob), b->stream));
   cudaMemcpyAsync(d, &ij, sizeof(ij), cudaMemcpyHostToDevice, b->stream);
   launch_initial_setup(d, 1, b->stream);
+  dfree(d, b->stream);
   cudaError_t e = cudaStreamSynchronize(b->stream);
-  cudaFree(d);
   if (e != cudaSuccess) return fail(BRAWL_ECUDA, cudaGetErrorString(e));
   TRY(check_status(b));
   std::copy(c.begin(), c.end(), conc);
@@ -1095,10 +1116,12 @@ struct brawl_ns {
 
 extern "C" int brawl_ns_destroy(brawl_ns* ns) {
   if (!ns) return BRAWL_OK;
-  if (ns->stream) cudaStreamSynchronize(ns->stream);
-  for (void* p : ns->allocs) cudaFree(p);
-  if (ns->d_limits) cudaFree(ns->d_limits);
-  if (ns->stream) cudaStreamDestroy(ns->stream);
+  if (ns->stream) {
+    for (void* p : ns->allocs) dfree(p, ns->stream);
+    dfree(ns->d_limits, ns->stream);
+    cudaStreamSynchronize(ns->stream);
+    cudaStreamDestroy(ns->stream);
+  }
   delete ns;
   return BRAWL_OK;
 }
@@ -1145,8 +1168,8 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
   }
   if (ns->smem > (uint32_t)max_optin)
     return cleanup(fail(BRAWL_EINVAL, "a run's lattice and tables exceed shared memory"));
-  auto dalloc = [&](size_t bytes, void** p) -> int {
-    cudaError_t e = cudaMalloc(p, bytes);
+  auto nsalloc = [&](size_t bytes, void** p) -> int {
+    cudaError_t e = dalloc(p, bytes, ns->stream);
     if (e != cudaSuccess) return fail(BRAWL_ENOMEM, cudaGetErrorString(e));
     ns->allocs.push_back(*p);
     return BRAWL_OK;
@@ -1159,26 +1182,27 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
     j.band = m.band;
     void *pV, *pF, *pE, *pS, *pRng, *pCnt, *pSt, *pW, *pEn, *pRn;
     int rc = BRAWL_OK;
-    rc |= dalloc(m.V.size() * 8, &pV);
-    rc |= dalloc(m.F.size() * 4, &pF);
-    rc |= dalloc(m.entries.size() * 4, &pE);
-    rc |= dalloc(m.sstart.size() * 2, &pS);
-    rc |= dalloc((kMTN + 1) * 4, &pRng);
-    rc |= dalloc(kNumCounters * 8, &pCnt);
-    rc |= dalloc(4, &pSt);
-    rc |= dalloc((size_t)R.K * m.g.n_sites, &pW);
-    rc |= dalloc((size_t)R.K * 8, &pEn);
-    rc |= dalloc((size_t)R.K * 4, &pRn);
+    rc |= nsalloc(m.V.size() * 8, &pV);
+    rc |= nsalloc(m.F.size() * 4, &pF);
+    rc |= nsalloc(m.entries.size() * 4, &pE);
+    rc |= nsalloc(m.sstart.size() * 2, &pS);
+    rc |= nsalloc((kMTN + 1) * 4, &pRng);
+    rc |= nsalloc(kNumCounters * 8, &pCnt);
+    rc |= nsalloc(4, &pSt);
+    rc |= nsalloc((size_t)R.K * m.g.n_sites, &pW);
+    rc |= nsalloc((size_t)R.K * 8, &pEn);
+    rc |= nsalloc((size_t)R.K * 4, &pRn);
     if (rc != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
     uint32_t st[kMTN + 1];
     mt_seed_host(descs[r].seed, st);
-    cudaMemcpy(pV, m.V.data(), m.V.size() * 8, cudaMemcpyHostToDevice);
-    cudaMemcpy(pF, m.F.data(), m.F.size() * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(pE, m.entries.data(), m.entries.size() * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(pS, m.sstart.data(), m.sstart.size() * 2, cudaMemcpyHostToDevice);
-    cudaMemcpy(pRng, st, sizeof(st), cudaMemcpyHostToDevice);
-    cudaMemset(pCnt, 0, kNumCounters * 8);
-    cudaMemset(pSt, 0, 4);
+    cudaMemcpyAsync(pV, m.V.data(), m.V.size() * 8, cudaMemcpyHostToDevice, ns->stream);
+    cudaMemcpyAsync(pF, m.F.data(), m.F.size() * 4, cudaMemcpyHostToDevice, ns->stream);
+    cudaMemcpyAsync(pE, m.entries.data(), m.entries.size() * 4, cudaMemcpyHostToDevice, ns->stream);
+    cudaMemcpyAsync(pS, m.sstart.data(), m.sstart.size() * 2, cudaMemcpyHostToDevice, ns->stream);
+    cudaMemcpyAsync(pRng, st, sizeof(st), cudaMemcpyHostToDevice, ns->stream);
+    cudaMemsetAsync(pCnt, 0, kNumCounters * 8, ns->stream);
+    cudaMemsetAsync(pSt, 0, 4, ns->stream);
+    CUDA_TRY(cudaStreamSynchronize(ns->stream));
     j.V = (const double*)pV;
     j.F = (const int32_t*)pF;
     j.entries = (const uint32_t*)pE;
@@ -1195,13 +1219,13 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
     R.rnde = (uint32_t*)pRn;
   }
   void* pRuns;
-  if (dalloc(n_runs * sizeof(NsRun), &pRuns) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
+  if (nsalloc(n_runs * sizeof(NsRun), &pRuns) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
   ns->d_runs = (NsRun*)pRuns;
-  CUDA_TRY(cudaMemcpy(ns->d_runs, ns->runs.data(), n_runs * sizeof(NsRun), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpyAsync(ns->d_runs, ns->runs.data(), n_runs * sizeof(NsRun), cudaMemcpyHostToDevice, ns->stream));
   launch_ns_init(ns->d_runs, n_runs, ns->stream);
   // walker energies: total_energy of every walker, then the jitter
   void *pSite, *pEj;
-  if (dalloc((size_t)total_sites * 8, &pSite) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
+  if (nsalloc((size_t)total_sites * 8, &pSite) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
   std::vector<EnergyJob> ej;
   int64_t off = 0;
   for (int r = 0; r < n_runs; ++r) {
@@ -1221,20 +1245,21 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
       ej.push_back(e);
     }
   }
-  if (dalloc(ej.size() * sizeof(EnergyJob), &pEj) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
+  if (nsalloc(ej.size() * sizeof(EnergyJob), &pEj) != BRAWL_OK) return cleanup(BRAWL_ENOMEM);
   CUDA_TRY(cudaMemcpyAsync(pEj, ej.data(), ej.size() * sizeof(EnergyJob), cudaMemcpyHostToDevice, ns->stream));
   launch_total_energy((EnergyJob*)pEj, (int)ej.size(), total_sites, ns->stream);
   launch_ns_jitter(ns->d_runs, n_runs, max_K, ns->stream);
   cudaError_t e = cudaStreamSynchronize(ns->stream);
   if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
   // the per-site scratch is only needed at set-up
-  cudaFree(pSite);
-  cudaFree(pEj);
+  dfree(pSite, ns->stream);
+  dfree(pEj, ns->stream);
   ns->allocs.erase(std::remove(ns->allocs.begin(), ns->allocs.end(), pSite), ns->allocs.end());
   ns->allocs.erase(std::remove(ns->allocs.begin(), ns->allocs.end(), pEj), ns->allocs.end());
   for (int r = 0; r < n_runs; ++r) {
     int32_t st = 0;
-    cudaMemcpy(&st, ns->runs[r].job.status, 4, cudaMemcpyDeviceToHost);
+    cudaMemcpyAsync(&st, ns->runs[r].job.status, 4, cudaMemcpyDeviceToHost, ns->stream);
+    cudaStreamSynchronize(ns->stream);
     if (st) return cleanup(fail(BRAWL_ESTATE, "walker initialisation failed on run " + std::to_string(r)));
   }
   *out = ns;
@@ -1247,15 +1272,16 @@ extern "C" int brawl_ns_iterate(brawl_ns* ns, int n_iter, double* limits) {
   const int n_runs = (int)ns->runs.size();
   const size_t need = (size_t)n_runs * n_iter * 8;
   if (need > ns->limits_cap) {
-    if (ns->d_limits) cudaFree(ns->d_limits);
+    dfree(ns->d_limits, ns->stream);
     ns->d_limits = nullptr;
     ns->limits_cap = 0;
-    CUDA_TRY(cudaMalloc(&ns->d_limits, need));
+    CUDA_TRY(dalloc(&ns->d_limits, need, ns->stream));
     ns->limits_cap = need;
   }
   // the device-side run state (iteration counters) is authoritative: read it back
   std::vector<NsRun> cur(n_runs);
-  CUDA_TRY(cudaMemcpy(cur.data(), ns->d_runs, n_runs * sizeof(NsRun), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpyAsync(cur.data(), ns->d_runs, n_runs * sizeof(NsRun), cudaMemcpyDeviceToHost, ns->stream));
+  CUDA_TRY(cudaStreamSynchronize(ns->stream));
   for (int r = 0; r < n_runs; ++r) {
     cur[r].limits = ns->d_limits + (size_t)r * n_iter;
     cur[r].n_iter = n_iter;
@@ -1287,11 +1313,11 @@ extern "C" int brawl_ns_walker_config(brawl_ns* ns, int run, int walker, int8_t*
   const Geom& g = R.job.g;
   const size_t grid = (size_t)8 * g.n1 * g.n2 * g.n3;
   int8_t* d_grid = nullptr;
-  CUDA_TRY(cudaMalloc(&d_grid, grid));
+  CUDA_TRY(dalloc(&d_grid, grid, ns->stream));
   launch_unpack(g, R.walkers + (size_t)walker * g.n_sites, d_grid, ns->stream);
   cudaError_t e = cudaMemcpyAsync(config, d_grid, grid, cudaMemcpyDeviceToHost, ns->stream);
+  dfree(d_grid, ns->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ns->stream);
-  cudaFree(d_grid);
   if (e != cudaSuccess) return fail(BRAWL_ECUDA, cudaGetErrorString(e));
   return BRAWL_OK;
 }
@@ -1319,6 +1345,15 @@ struct brawl_wl {
   double* d_lng = nullptr;
   double* d_hist = nullptr;
   uint32_t smem = 0;
+  // exchange / flatness / combine scratch
+  int per_window = 0;                    // walkers per window when all windows have as many
+  int* d_ibin = nullptr;
+  int2* d_ov = nullptr;
+  int* d_partner = nullptr;
+  int* d_exchanged = nullptr;
+  int* d_nacc = nullptr;
+  double* d_flat = nullptr;
+  double* d_combined = nullptr;
 };
 
 namespace {
@@ -1350,11 +1385,15 @@ int batch_genrand(brawl_batch* b, int c, int64_t n, double* out) {
 
 extern "C" int brawl_wl_destroy(brawl_wl* wl) {
   if (!wl) return BRAWL_OK;
-  if (wl->b) brawl_batch_destroy(wl->b);
-  if (wl->d_w) cudaFree(wl->d_w);
-  if (wl->d_groups) cudaFree(wl->d_groups);
-  if (wl->d_lng) cudaFree(wl->d_lng);
-  if (wl->d_hist) cudaFree(wl->d_hist);
+  if (wl->b) {
+    // freed on the batch's stream, which the batch's destruction then drains
+    for (const void* p : {(const void*)wl->d_w, (const void*)wl->d_groups, (const void*)wl->d_lng,
+                          (const void*)wl->d_hist, (const void*)wl->d_ibin, (const void*)wl->d_ov,
+                          (const void*)wl->d_partner, (const void*)wl->d_exchanged, (const void*)wl->d_nacc,
+                          (const void*)wl->d_flat, (const void*)wl->d_combined})
+      dfree(p, wl->b->stream);
+    brawl_batch_destroy(wl->b);
+  }
   delete wl;
   return BRAWL_OK;
 }
@@ -1391,12 +1430,13 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
   wl->range = bin_edges[bins] - bin_edges[0];
   size_t hist_total = 0;
   for (int c = 0; c < n; ++c) hist_total += walkers[c].end_idx - walkers[c].start_idx + 1;
-  if (cudaMalloc(&wl->d_lng, (size_t)n * bins * 8) != cudaSuccess ||
-      cudaMalloc(&wl->d_hist, hist_total * 8) != cudaSuccess ||
-      cudaMalloc(&wl->d_w, n * sizeof(WlWalker)) != cudaSuccess)
+  cudaStream_t ws = wl->b->stream;
+  if (dalloc(&wl->d_lng, (size_t)n * bins * 8, ws) != cudaSuccess ||
+      dalloc(&wl->d_hist, hist_total * 8, ws) != cudaSuccess ||
+      dalloc(&wl->d_w, n * sizeof(WlWalker), ws) != cudaSuccess)
     return cleanup(fail(BRAWL_ENOMEM, "walker buffers"));
-  cudaMemset(wl->d_lng, 0, (size_t)n * bins * 8);
-  cudaMemset(wl->d_hist, 0, hist_total * 8);
+  cudaMemsetAsync(wl->d_lng, 0, (size_t)n * bins * 8, ws);
+  cudaMemsetAsync(wl->d_hist, 0, hist_total * 8, ws);
   wl->w.resize(n);
   size_t hoff = 0;
   int max_optin = 0;
@@ -1418,9 +1458,21 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
     wl->groups.back().count += 1;
   }
   if (wl->smem > (uint32_t)max_optin) return cleanup(fail(BRAWL_EINVAL, "window or lattice too large for shared memory"));
-  if (cudaMalloc(&wl->d_groups, wl->groups.size() * sizeof(WlGroup)) != cudaSuccess)
+  if (dalloc(&wl->d_groups, wl->groups.size() * sizeof(WlGroup), ws) != cudaSuccess)
     return cleanup(fail(BRAWL_ENOMEM, "groups"));
-  cudaMemcpy(wl->d_groups, wl->groups.data(), wl->groups.size() * sizeof(WlGroup), cudaMemcpyHostToDevice);
+  wl->per_window = wl->groups[0].count;
+  for (const WlGroup& G : wl->groups)
+    if (G.count != wl->per_window) wl->per_window = 0;
+  if (dalloc(&wl->d_ibin, n * sizeof(int), ws) != cudaSuccess ||
+      dalloc(&wl->d_ov, n * sizeof(int2), ws) != cudaSuccess ||
+      dalloc(&wl->d_partner, n * sizeof(int), ws) != cudaSuccess ||
+      dalloc(&wl->d_exchanged, n * sizeof(int), ws) != cudaSuccess ||
+      dalloc(&wl->d_nacc, 2 * sizeof(int), ws) != cudaSuccess ||
+      dalloc(&wl->d_flat, n * sizeof(double), ws) != cudaSuccess ||
+      dalloc(&wl->d_combined, (size_t)bins * sizeof(double), ws) != cudaSuccess)
+    return cleanup(fail(BRAWL_ENOMEM, "exchange buffers"));
+  cudaMemcpyAsync(wl->d_groups, wl->groups.data(), wl->groups.size() * sizeof(WlGroup), cudaMemcpyHostToDevice, ws);
+  if (cudaStreamSynchronize(ws) != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, "walker set-up"));
   *out = wl;
   return BRAWL_OK;
 }
@@ -1430,18 +1482,17 @@ extern "C" int brawl_wl_sweeps(brawl_wl* wl, int64_t n_trials, double wl_f, int 
   if (!wl || n_trials < 0) return fail(BRAWL_EINVAL, "bad argument");
   brawl_batch* b = wl->b;
   const int n = (int)wl->w.size();
-  std::vector<double> e0(n);
-  TRY(brawl_batch_total_energy(b, e0.data()));
+  TRY(queue_batch_energy(b));
   for (int c = 0; c < n; ++c) {
     WlWalker& W = wl->w[c];
-    W.e0 = e0[c];
+    W.e0_src = b->d_energy + c;
     W.wl_f = wl_f;
     W.n_trials = n_trials;
     W.hist_period = hist_period;
   }
   CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), n * sizeof(WlWalker), cudaMemcpyHostToDevice, b->stream));
   launch_wl_sweeps(wl->d_w, n, wl->smem, b->stream);
-  launch_wl_average(wl->d_groups, (int)wl->groups.size(), wl->d_w, wl->bins, b->stream);
+  launch_wl_average(wl->d_groups, (int)wl->groups.size(), wl->d_w, wl->bins, 1, b->stream);
   CUDA_TRY(cudaGetLastError());
   std::vector<WlWalker> res(n);
   CUDA_TRY(cudaMemcpyAsync(res.data(), wl->d_w, n * sizeof(WlWalker), cudaMemcpyDeviceToHost, b->stream));
@@ -1456,8 +1507,75 @@ extern "C" int brawl_wl_sweeps(brawl_wl* wl, int64_t n_trials, double wl_f, int 
 extern "C" int brawl_wl_average(brawl_wl* wl) {
   if (!wl) return fail(BRAWL_EINVAL, "null argument");
   CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), wl->w.size() * sizeof(WlWalker), cudaMemcpyHostToDevice, wl->b->stream));
-  launch_wl_average(wl->d_groups, (int)wl->groups.size(), wl->d_w, wl->bins, wl->b->stream);
+  launch_wl_average(wl->d_groups, (int)wl->groups.size(), wl->d_w, wl->bins, 0, wl->b->stream);
   CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_replica_exchange(brawl_wl* wl, int* partner, int* exchanged,
+                                         int* n_accepted) {
+  if (!wl) return fail(BRAWL_EINVAL, "null argument");
+  if (wl->per_window <= 0)
+    return fail(BRAWL_EINVAL, "replica exchange needs the same number of walkers in every window");
+  brawl_batch* b = wl->b;
+  const int n = (int)wl->w.size();
+  const Geom& g0 = b->models[0].g;
+  for (int c = 1; c < n; ++c) {
+    const Geom& g = b->models[c].g;
+    if (g.lattice != g0.lattice || g.n1 != g0.n1 || g.n2 != g0.n2 || g.n3 != g0.n3)
+      return fail(BRAWL_EINVAL, "walkers have different lattices");
+  }
+  TRY(queue_batch_energy(b));
+  CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), n * sizeof(WlWalker), cudaMemcpyHostToDevice, b->stream));
+  launch_wl_exchange(wl->d_w, b->d_energy, wl->d_groups, (int)wl->groups.size(), wl->per_window,
+                     wl->d_ibin, wl->d_ov, wl->d_partner, wl->d_exchanged, wl->d_nacc, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  int nacc = 0;
+  CUDA_TRY(cudaMemcpyAsync(&nacc, wl->d_nacc, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  if (partner)
+    CUDA_TRY(cudaMemcpyAsync(partner, wl->d_partner, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  if (exchanged)
+    CUDA_TRY(cudaMemcpyAsync(exchanged, wl->d_exchanged, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (n_accepted) *n_accepted = nacc;
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_flatness(brawl_wl* wl, double* flatness) {
+  if (!wl || !flatness) return fail(BRAWL_EINVAL, "null argument");
+  brawl_batch* b = wl->b;
+  const int n = (int)wl->w.size();
+  CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), n * sizeof(WlWalker), cudaMemcpyHostToDevice, b->stream));
+  launch_wl_flatness(wl->d_w, n, wl->d_flat, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(flatness, wl->d_flat, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_dos_combine(brawl_wl* wl, double* lng) {
+  if (!wl) return fail(BRAWL_EINVAL, "null argument");
+  brawl_batch* b = wl->b;
+  const int n = (int)wl->w.size();
+  CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), n * sizeof(WlWalker), cudaMemcpyHostToDevice, b->stream));
+  launch_wl_combine(wl->d_w, n, wl->d_groups, (int)wl->groups.size(), wl->bins, wl->d_combined,
+                    wl->d_nacc + 1, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  int status = 0;
+  CUDA_TRY(cudaMemcpyAsync(&status, wl->d_nacc + 1, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  if (lng)
+    CUDA_TRY(cudaMemcpyAsync(lng, wl->d_combined, (size_t)wl->bins * 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (status != 0) return fail(BRAWL_ESTATE, "a window has no overlap with the previous one");
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_reset_hist(brawl_wl* wl) {
+  if (!wl) return fail(BRAWL_EINVAL, "null argument");
+  size_t total = 0;
+  for (const WlWalker& W : wl->w) total += W.end - W.start + 1;
+  CUDA_TRY(cudaMemsetAsync(wl->d_hist, 0, total * 8, wl->b->stream));
   CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
   return BRAWL_OK;
 }
@@ -1532,3 +1650,52 @@ extern "C" int brawl_wl_counters(brawl_wl* wl, int c, int64_t* counters) {
   std::copy(all.begin() + (size_t)c * kNumCounters, all.begin() + (size_t)(c + 1) * kNumCounters, counters);
   return BRAWL_OK;
 }
+
+// ---------------------------------------------------------------------------
+// accessors for the serving loop (server.cu), which batches chains, walkers
+// and runs of many objects into shared launches
+// ---------------------------------------------------------------------------
+namespace brawl {
+
+int api_batch_chain(brawl_batch* b, int c, ChainSlot& out) {
+  if (!b || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad chain");
+  const Model& m = b->models[c];
+  out.job = b->jobs[c];
+  out.halo = b->halo[c];
+  HaloGeom H;
+  bool ok;
+  make_halo(m.g, H, ok);
+  out.halo_smem = out.halo ? halo_layout(m.g, H).total : 0;
+  out.smem_lat_bytes = smem_layout(m.g, true).total;
+  out.smem_glob_bytes = smem_layout(m.g, false).total;
+  out.use_D = smem_layout(m.g, false).use_D;
+  out.energy.g = m.g;
+  out.energy.lat = b->jobs[c].lat;
+  out.energy.V = b->jobs[c].V;
+  out.energy.entries = b->jobs[c].entries;
+  out.energy.shell_start = b->jobs[c].shell_start;
+  out.energy.site_energy = nullptr;
+  out.energy.out = nullptr;
+  out.energy.site_offset = 0;
+  return BRAWL_OK;
+}
+
+void api_batch_beta(brawl_batch* b, int c, ChainJob& j, double beta) { set_beta(j, b->models[c], beta); }
+
+int api_batch_set_rng(brawl_batch* b, int c, const uint32_t state[625]) {
+  if (!b || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad chain");
+  CUDA_TRY(cudaMemcpy(b->jobs[c].rng, state, (kMTN + 1) * 4, cudaMemcpyHostToDevice));
+  return BRAWL_OK;
+}
+
+cudaStream_t api_batch_stream(brawl_batch* b) { return b->stream; }
+brawl_batch* api_wl_batch(brawl_wl* wl) { return wl->b; }
+std::vector<WlWalker>& api_wl_walkers(brawl_wl* wl) { return wl->w; }
+uint32_t api_wl_smem(brawl_wl* wl) { return wl->smem; }
+
+NsRun* api_ns_device_run(brawl_ns* ns, int r) { return ns->d_runs + r; }
+uint32_t api_ns_smem(brawl_ns* ns) { return ns->smem; }
+int api_last_error_set(int code, const std::string& msg) { return fail(code, msg); }
+std::string api_last_error() { return g_err; }
+
+}  // namespace brawl

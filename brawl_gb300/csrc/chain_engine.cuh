@@ -29,6 +29,19 @@
 #include "exact_fp.cuh"
 #include "lattice_tables.h"
 
+// Every kernel asks for the largest shared-memory carveout once, so kernels
+// of all sizes from concurrent streams can share an SM without it being
+// reconfigured between them.
+#define BRAWL_CARVEOUT(...)                                                              \
+  do {                                                                                   \
+    static bool carveout_set_ = false;                                                   \
+    if (!carveout_set_) {                                                                \
+      cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributePreferredSharedMemoryCarveout,  \
+                           (int)cudaSharedmemCarveoutMaxShared);                         \
+      carveout_set_ = true;                                                              \
+    }                                                                                    \
+  } while (0)
+
 namespace brawl {
 
 constexpr unsigned kFull = 0xffffffffu;
@@ -99,7 +112,16 @@ struct ChainJob {
   const int16_t* shell_start; // nsh + 1 entry offsets
   unsigned long long* counters;
   int32_t* status;
+  unsigned long long* t_ns;   // when set: the CTA's device time (ns) is written here
 };
+
+// Device clock in ns (%globaltimer), for the per-chain timings a scheduler
+// uses to size the next launch's work.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // ---------------------------------------------------------------------------
 // mt19937ar (src/mt19937ar.c:82-125), warp-cooperative

@@ -37,6 +37,7 @@ __global__ void __launch_bounds__(32) initial_setup_kernel(const InitJob* __rest
 }
 
 void launch_initial_setup(const InitJob* d_jobs, int n_jobs, cudaStream_t stream) {
+  BRAWL_CARVEOUT(initial_setup_kernel);
   if (n_jobs > 0) initial_setup_kernel<<<n_jobs, 32, 0, stream>>>(d_jobs);
 }
 
@@ -98,7 +99,9 @@ void launch_total_energy(const EnergyJob* d_jobs, int n_jobs, int64_t total_site
   if (n_jobs <= 0) return;
   int64_t blocks = (total_sites + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
+  BRAWL_CARVEOUT(site_energies_kernel);
   site_energies_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_sites);
+  BRAWL_CARVEOUT(sum_sites_kernel);
   sum_sites_kernel<<<(n_jobs + 31) / 32, 32, 0, stream>>>(d_jobs, n_jobs);
 }
 
@@ -109,6 +112,7 @@ __global__ void one_site_energy_kernel(const EnergyJob* __restrict__ job, int x,
 
 void launch_site_energy(const EnergyJob* d_job, int x, int y, int z, double* out,
                         cudaStream_t stream) {
+  BRAWL_CARVEOUT(one_site_energy_kernel);
   one_site_energy_kernel<<<1, 1, 0, stream>>>(d_job, x, y, z, out);
 }
 
@@ -153,6 +157,7 @@ void launch_pack(const Geom& g, const int8_t* d_grid, int8_t* d_lat, int32_t* d_
   const int64_t total = (int64_t)8 * g.n1 * g.n2 * g.n3;
   int blocks = (int)((total + 255) / 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
+  BRAWL_CARVEOUT(pack_kernel);
   pack_kernel<<<blocks, 256, 0, stream>>>(g, d_grid, d_lat, d_status);
 }
 
@@ -160,6 +165,7 @@ void launch_unpack(const Geom& g, const int8_t* d_lat, int8_t* d_grid, cudaStrea
   const int64_t total = (int64_t)8 * g.n1 * g.n2 * g.n3;
   int blocks = (int)((total + 255) / 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
+  BRAWL_CARVEOUT(unpack_kernel);
   unpack_kernel<<<blocks, 256, 0, stream>>>(g, d_lat, d_grid);
 }
 
@@ -207,6 +213,7 @@ void launch_pack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells,
                        const int8_t* d_grids, cudaStream_t stream) {
   int64_t blocks = (total_cells + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
+  BRAWL_CARVEOUT(pack_batch_kernel);
   if (n_jobs > 0) pack_batch_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_cells, d_grids);
 }
 
@@ -214,6 +221,7 @@ void launch_unpack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells,
                          cudaStream_t stream) {
   int64_t blocks = (total_cells + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
+  BRAWL_CARVEOUT(unpack_batch_kernel);
   if (n_jobs > 0) unpack_batch_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_cells, d_grids);
 }
 

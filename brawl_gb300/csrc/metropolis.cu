@@ -85,6 +85,12 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
   const ChainJob J = jobs[blockIdx.x];
   const Geom g = J.g;
   const int lane = threadIdx.x;
+  __shared__ unsigned long long s_t_start;  // kept out of registers
+  __shared__ unsigned long long* s_t_ns;
+  if (lane == 0) {
+    s_t_start = global_ns();
+    s_t_ns = jobs[blockIdx.x].t_ns;
+  }
   const SmemLayout L = smem_layout(g, kSmemLat);
   uint32_t* mt = reinterpret_cast<uint32_t*>(smem + L.mt);
   int32_t* I = reinterpret_cast<int32_t*>(smem + L.I);
@@ -209,6 +215,7 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
     c[kCntExpFp64] += c_fp64;
     c[kCntExpCr] += c_cr;
     if (status != kStatusOk) *J.status = status;
+    if (s_t_ns) *s_t_ns = global_ns() - s_t_start;
   }
 }
 
@@ -217,6 +224,7 @@ static void launch_one(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes,
                        cudaStream_t stream) {
   cudaFuncSetAttribute(metropolis_kernel<NJ, kSmemLat, kUseD>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  BRAWL_CARVEOUT(metropolis_kernel<NJ, kSmemLat, kUseD>);
   metropolis_kernel<NJ, kSmemLat, kUseD><<<n_jobs, 32, smem_bytes, stream>>>(d_jobs);
 }
 

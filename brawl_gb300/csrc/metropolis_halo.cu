@@ -77,6 +77,8 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   const Geom g = Jg->g;
   const HaloGeom H = Jg->hg;
   const int lane = threadIdx.x;
+  __shared__ unsigned long long s_t_start;  // kept out of registers
+  if (lane == 0) s_t_start = global_ns();
   const HaloLayout L = halo_layout(g, H);
   uint32_t* mt = reinterpret_cast<uint32_t*>(smem + L.mt);
   uint32_t* tbuf = reinterpret_cast<uint32_t*>(smem + L.tbuf);
@@ -187,6 +189,7 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
     c[kCntExactPath] += c_exact;
     c[kCntExpFp64] += c_fp64;
     c[kCntExpCr] += c_cr;
+    if (Jg->t_ns) *Jg->t_ns = global_ns() - s_t_start;
   }
 }
 
@@ -195,6 +198,7 @@ static void launch_halo_nj(const ChainJob* d_jobs, int n_jobs, uint32_t smem_byt
                            cudaStream_t stream) {
   cudaFuncSetAttribute(metropolis_halo_kernel<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes);
+  BRAWL_CARVEOUT(metropolis_halo_kernel<NJ>);
   metropolis_halo_kernel<NJ><<<n_jobs, 32, smem_bytes, stream>>>(d_jobs);
 }
 

@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
   const ChainJob& J = R.job;
   const Geom g = J.g;
   const int lane = threadIdx.x;
+  const unsigned long long t_start = global_ns();
   const int n = g.n_sites;
   const int nsp = g.ns + 1;
   const int nF = nsp * g.nsh * nsp, nV = g.ns * g.ns * g.nsh;
@@ -239,6 +240,7 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
     c[kCntAccepted] += c_acc;
     c[kCntExactPath] += c_exact;
     if (status != kStatusOk) *J.status = status;
+    if (J.t_ns) *J.t_ns = global_ns() - t_start;
   }
 }
 
@@ -252,17 +254,20 @@ uint32_t ns_smem_bytes(const Geom& g) {
 }
 
 void launch_ns_init(NsRun* d_runs, int n_runs, cudaStream_t stream) {
+  BRAWL_CARVEOUT(ns_init_kernel);
   ns_init_kernel<<<n_runs, 32, 0, stream>>>(d_runs);
 }
 
 void launch_ns_jitter(NsRun* d_runs, int n_runs, int max_K, cudaStream_t stream) {
   dim3 grid((max_K + 255) / 256, n_runs);
+  BRAWL_CARVEOUT(ns_jitter_kernel);
   ns_jitter_kernel<<<grid, 256, 0, stream>>>(d_runs, n_runs);
 }
 
 void launch_ns_iterate(NsRun* d_runs, int n_runs, uint32_t smem_bytes, cudaStream_t stream) {
   cudaFuncSetAttribute(ns_iterate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes);
+  BRAWL_CARVEOUT(ns_iterate_kernel);
   ns_iterate_kernel<<<n_runs, 32, smem_bytes, stream>>>(d_runs);
 }
 

@@ -31,6 +31,7 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   const ChainJob& J = W.job;
   const Geom g = J.g;
   const int lane = threadIdx.x;
+  const unsigned long long t_start = global_ns();
   const int nV = g.ns * g.ns * g.nsh;
   const int nb = W.end - W.start + 1;
   // layout: mt | tbuf | V | lng slice | hist slice | ents | sstart | lattice
@@ -59,14 +60,15 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   const double e1 = W.e1, range = W.range, f = W.wl_f;
   const int bins = W.bins, start = W.start, end = W.end;
   const int period = W.hist_period;
-  double e_un = W.e0;
+  double e_un = (W.i0 > 0 && W.e_state) ? *W.e_state : (W.e0_src ? *W.e0_src : W.e0);
   int ibin = wl_bin_index(e_un, e1, range, bins);
   int status = (ibin < start || ibin > end) ? kStatusWalkerOutsideWindow : kStatusOk;
   unsigned long long c_eval = 0, c_draws = 0, c_exp = 0;
   long long accepted = 0;
   DecideStats st = {0u, 0u};
 
-  for (long long i = 1; i <= W.n_trials && status == kStatusOk; ++i) {
+  const long long i_end = W.i0 + W.n_trials;
+  for (long long i = W.i0 + 1; i <= i_end && status == kStatusOk; ++i) {
     ring_ensure(mt, tbuf, ring, 7, lane);
     const int wb = ring.idx;
     SitePair p;
@@ -123,6 +125,7 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   ring_writeback(mt, tbuf, ring, J.rng, lane);
   if (lane == 0) {
     W.e_out = e_un;
+    if (W.e_state) *W.e_state = e_un;
     W.accepted = accepted;
     unsigned long long* c = J.counters;
     c[kCntTrials] += (unsigned long long)W.n_trials;
@@ -134,23 +137,28 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
     c[kCntExpFp64] += st.fp64;
     c[kCntExpCr] += st.cr;
     if (status != kStatusOk) *J.status = status;
+    if (J.t_ns) *J.t_ns = global_ns() - t_start;
   }
 }
 
 // The window average: for every bin, the walkers' values summed in walker
 // order and divided by their count (MPI_Allreduce SUM then /num_walkers,
-// src/wang-landau.F90:628-631).  groups[k] lists the walkers of window k.
+// src/wang-landau.F90:628-631; dos_average, :1127-1133, averages ln g
+// alone).  groups[k] lists the walkers of window k.
 __global__ void wl_average_kernel(const WlGroup* __restrict__ groups, WlWalker* walkers,
-                                  int bins) {
+                                  int bins, int with_hist) {
   const WlGroup G = groups[blockIdx.y];
   if (G.count <= 1) return;
   const double inv = (double)(float)G.count;
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bins; b += gridDim.x * blockDim.x) {
+  const int nbins = walkers[G.first].bins;  // the bins argument (the largest) sizes the grid
+  (void)bins;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += gridDim.x * blockDim.x) {
     double s = walkers[G.first].lng[b];
     for (int k = 1; k < G.count; ++k) s = __dadd_rn(s, walkers[G.first + k].lng[b]);
     const double a = __ddiv_rn(s, inv);
     for (int k = 0; k < G.count; ++k) walkers[G.first + k].lng[b] = a;
   }
+  if (!with_hist) return;
   const int nb = walkers[G.first].end - walkers[G.first].start + 1;
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
     double s = walkers[G.first].hist[b];
@@ -170,14 +178,323 @@ uint32_t wl_smem_bytes(const Geom& g, int nb) {
 
 void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, cudaStream_t stream) {
   cudaFuncSetAttribute(wl_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  BRAWL_CARVEOUT(wl_sweep_kernel);
   wl_sweep_kernel<<<n, 32, smem, stream>>>(d_walkers);
 }
 
 void launch_wl_average(const WlGroup* d_groups, int n_groups, WlWalker* d_walkers, int bins,
-                       cudaStream_t stream) {
+                       int with_hist, cudaStream_t stream) {
   if (n_groups <= 0) return;
   dim3 grid((bins + 255) / 256, n_groups);
-  wl_average_kernel<<<grid, 256, 0, stream>>>(d_groups, d_walkers, bins);
+  BRAWL_CARVEOUT(wl_average_kernel);
+  wl_average_kernel<<<grid, 256, 0, stream>>>(d_groups, d_walkers, bins, with_hist);
+}
+
+// ---------------------------------------------------------------------------
+// replica_exchange (src/wang-landau.F90:1392-1501) for walkers ordered by
+// window, per_window each (walker w plays MPI rank w).  One warp: the bins
+// and overlaps of every walker in parallel, then the reference's sequence --
+// per adjacent pair of windows both candidate lists shuffled on walker 0's
+// stream (shuffle_rows, :1513-1525), equal overlaps matched in list order,
+// and every matched lower walker drawing genrand() < exp(lng(i) - lng(j))
+// from its own stream, the pair's configurations swapped on acceptance.
+// A stream is staged in shared memory (624 words + position, the layout the
+// chains keep in global memory) while it is drawn from.
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ void stream_load(uint32_t* s, const uint32_t* g, int lane) {
+  for (int i = lane; i <= kMTN; i += 32) s[i] = g[i];
+  __syncwarp();
+}
+
+__device__ __forceinline__ void stream_store(uint32_t* g, const uint32_t* s, int lane) {
+  __syncwarp();
+  for (int i = lane; i <= kMTN; i += 32) g[i] = s[i];
+  __syncwarp();
+}
+
+// genrand_int32 on a staged stream; warp-collective, every lane gets the word.
+__device__ __forceinline__ uint32_t stream_draw(uint32_t* s, int lane) {
+  int pos = (int)s[kMTN];
+  if (pos >= kMTN) {
+    mt_twist_warp(s, lane);
+    pos = 0;
+  }
+  const uint32_t w = mt_temper(s[pos]);
+  __syncwarp();
+  if (lane == 0) s[kMTN] = (uint32_t)(pos + 1);
+  __syncwarp();
+  return w;
+}
+
+// shuffle_rows: rows r = n..2 swap with MIN(1+int(genrand()*r), n);
+// int(u*r) = floor(w*r / 2^32) exactly for r < 2^21.
+__device__ void shuffle_rows(int2* rows, int n, uint32_t* s, int lane) {
+  for (int r = n; r >= 2; --r) {
+    const uint32_t w = stream_draw(s, lane);
+    int k = 1 + (int)__umulhi(w, (uint32_t)r);
+    k = k > n ? n : k;
+    if (lane == 0) {
+      const int2 t = rows[r - 1];
+      rows[r - 1] = rows[k - 1];
+      rows[k - 1] = t;
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(32) wl_exchange_kernel(WlWalker* __restrict__ W,
+                                                         const double* __restrict__ energy,
+                                                         const WlGroup* __restrict__ groups,
+                                                         int n_windows, int per_window,
+                                                         int* __restrict__ ibin,
+                                                         int2* __restrict__ ov,
+                                                         int* __restrict__ partner,
+                                                         int* __restrict__ exchanged,
+                                                         int* __restrict__ n_accepted) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  uint32_t* st0 = sm;                        // walker 0's stream
+  uint32_t* st1 = sm + 640;                  // a matched walker's stream
+  int2* lo = reinterpret_cast<int2*>(sm + 1280);
+  int2* up = lo + per_window;
+  int2* pairs = up + per_window;
+  int* s_np = reinterpret_cast<int*>(pairs + per_window);
+  const int lane = threadIdx.x;
+  const int n = n_windows * per_window;
+  const double e1 = W[0].e1, range = W[0].range;
+  const int bins = W[0].bins;
+
+  for (int w = lane; w < n; w += 32) {
+    const int idx = w / per_window + 1;
+    const int ib = wl_bin_index(energy[w], e1, range, bins);
+    bool lower = false, upper = false;
+    if (idx > 1)
+      lower = ib < W[groups[idx - 2].first].end + 1 && ib > W[groups[idx - 1].first].start - 1;
+    if (idx < n_windows)
+      upper = ib > W[groups[idx].first].start - 1 && ib < W[groups[idx - 1].first].end + 1;
+    ibin[w] = ib;
+    ov[w] = make_int2(w, upper ? idx : (lower ? idx - 1 : 0));
+    partner[w] = -1;
+    exchanged[w] = 0;
+  }
+  __syncwarp();
+  stream_load(st0, W[0].job.rng, lane);
+  int n_acc = 0;
+  DecideStats st = {0u, 0u};
+  for (int i = 1; i <= n_windows - 1; ++i) {
+    for (int j = lane; j < per_window; j += 32) {
+      lo[j] = ov[(i - 1) * per_window + j];
+      up[j] = ov[i * per_window + j];
+    }
+    __syncwarp();
+    shuffle_rows(lo, per_window, st0, lane);
+    shuffle_rows(up, per_window, st0, lane);
+    if (lane == 0) {
+      int np = 0;
+      for (int j = 0; j < per_window; ++j) {
+        if (lo[j].y == 0) continue;
+        for (int k = 0; k < per_window; ++k) {
+          if (up[k].y == 0) continue;
+          if (lo[j].y == up[k].y) {
+            pairs[np++] = make_int2(lo[j].x, up[k].x);
+            lo[j] = make_int2(0, 0);
+            up[k] = make_int2(0, 0);
+          }
+        }
+      }
+      *s_np = np;
+    }
+    __syncwarp();
+    const int np = *s_np;
+    for (int p = 0; p < np; ++p) {
+      const int a = pairs[p].x, b = pairs[p].y;
+      const int jb = wl_bin_index(energy[b], e1, range, bins);
+      uint32_t* s = a == 0 ? st0 : st1;
+      if (a != 0) stream_load(st1, W[a].job.rng, lane);
+      const uint32_t wu = stream_draw(s, lane);
+      if (a != 0) stream_store(W[a].job.rng, st1, lane);
+      const int ia = ibin[a];
+      int acc = 0;
+      if (ia >= 1 && ia <= bins && jb >= 1 && jb <= bins) {
+        const double d = __dsub_rn(W[a].lng[ia - 1], W[a].lng[jb - 1]);
+        acc = u_lt_exp(wu, d, st);
+      }
+      if (lane == 0) {
+        partner[a] = b;
+        partner[b] = a;
+      }
+      if (acc) {
+        int8_t* la = W[a].job.lat;
+        int8_t* lb = W[b].job.lat;
+        for (int t = lane; t < W[a].job.g.n_sites; t += 32) {
+          const int8_t x = la[t];
+          la[t] = lb[t];
+          lb[t] = x;
+        }
+        if (lane == 0) {
+          exchanged[a] = 1;
+          exchanged[b] = 1;
+        }
+        ++n_acc;
+      }
+      __syncwarp();
+    }
+  }
+  stream_store(W[0].job.rng, st0, lane);
+  if (lane == 0) *n_accepted = n_acc;
+}
+
+uint32_t wl_exchange_smem_bytes(int per_window) {
+  return 1280u * 4u + 3u * (uint32_t)per_window * 8u + 16u;
+}
+
+void launch_wl_exchange(WlWalker* d_walkers, const double* d_energy, const WlGroup* d_groups,
+                        int n_windows, int per_window, int* d_ibin, int2* d_ov, int* d_partner,
+                        int* d_exchanged, int* d_n_accepted, cudaStream_t stream) {
+  const uint32_t smem = wl_exchange_smem_bytes(per_window);
+  cudaFuncSetAttribute(wl_exchange_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  BRAWL_CARVEOUT(wl_exchange_kernel);
+  wl_exchange_kernel<<<1, 32, smem, stream>>>(d_walkers, d_energy, d_groups, n_windows, per_window,
+                                              d_ibin, d_ov, d_partner, d_exchanged, d_n_accepted);
+}
+
+// flatness = minval(hist)/(sum(hist)/mpi_bins) (src/wang-landau.F90:222),
+// one thread per walker summing its histogram in bin order.
+__global__ void wl_flatness_kernel(const WlWalker* __restrict__ W, int n, double* __restrict__ out) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= n) return;
+  const int nb = W[w].end - W[w].start + 1;
+  const double* h = W[w].hist;
+  double mn = h[0], s = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    const double v = h[b];
+    mn = v < mn ? v : mn;
+    s = __dadd_rn(s, v);
+  }
+  out[w] = __ddiv_rn(mn, __ddiv_rn(s, (double)nb));
+}
+
+void launch_wl_flatness(const WlWalker* d_walkers, int n, double* d_out, cudaStream_t stream) {
+  BRAWL_CARVEOUT(wl_flatness_kernel);
+  wl_flatness_kernel<<<(n + 127) / 128, 128, 0, stream>>>(d_walkers, n, d_out);
+}
+
+// dos_combine (src/wang-landau.F90:1147-1194) in one CTA: window by window,
+// the first bin of the overlap where the slopes of the combined and the
+// window's ln g differ least (the lowest such bin: the reference keeps the
+// first strict improvement), then the window's ln g shifted onto the
+// combined one from that bin to the window's end, exactly as the
+// reference's sequential loop rounds it: the meeting bin becomes
+// c' = (buf(k) + c(k)) - buf(k) and every later bin (buf(j) + c') - buf(k).
+// Finally the minimum is subtracted.  status: 0, or 1 when no overlap bin
+// was ever found (the reference would index bin 0).
+constexpr int kCombineThreads = 256;
+#define kInfD __longlong_as_double(0x7ff0000000000000LL)
+
+__global__ void __launch_bounds__(kCombineThreads) wl_combine_kernel(
+    const WlWalker* __restrict__ W, const WlGroup* __restrict__ groups, int n_groups,
+    double* __restrict__ out, int* __restrict__ status) {
+  __shared__ double red_d[kCombineThreads];
+  __shared__ int red_j[kCombineThreads];
+  __shared__ int s_beta;
+  __shared__ double s_c;
+  const int tid = threadIdx.x;
+  const int bins = W[0].bins;
+  const double* first = W[groups[0].first].lng;
+  for (int b = tid; b < bins; b += kCombineThreads) out[b] = first[b];
+  if (tid == 0) s_beta = 0;
+  __syncthreads();
+  for (int i = 1; i < n_groups; ++i) {
+    const WlWalker& Wi = W[groups[i].first];
+    const double* buf = Wi.lng;
+    const int s = Wi.start, e = Wi.end;
+    const int L = W[groups[i - 1].first].end - s;     // j = 0 .. L-1
+    double best = kInfD;
+    int bj = 0x7fffffff;
+    for (int j = tid; j < L; j += kCombineThreads) {
+      const double bo = __dsub_rn(out[s + j], out[s + j - 1]);
+      const double bm = __dsub_rn(buf[s + j], buf[s + j - 1]);
+      const double d = fabs(__dsub_rn(bo, bm));
+      if (d < 1.7976931348623157e308 && (d < best || (d == best && j < bj))) {
+        best = d;
+        bj = j;
+      }
+    }
+    red_d[tid] = best;
+    red_j[tid] = bj;
+    __syncthreads();
+    for (int h = kCombineThreads / 2; h > 0; h >>= 1) {
+      if (tid < h) {
+        const double d2 = red_d[tid + h];
+        const int j2 = red_j[tid + h];
+        if (d2 < red_d[tid] || (d2 == red_d[tid] && j2 < red_j[tid])) {
+          red_d[tid] = d2;
+          red_j[tid] = j2;
+        }
+      }
+      __syncthreads();
+    }
+    if (tid == 0) {
+      if (red_j[0] != 0x7fffffff) s_beta = s + red_j[0] + 1;
+      if (s_beta >= 1) {
+        const int k = s_beta;
+        s_c = __dsub_rn(__dadd_rn(buf[k - 1], out[k - 1]), buf[k - 1]);
+      }
+    }
+    __syncthreads();
+    const int k = s_beta;
+    if (k < 1) {
+      if (tid == 0) *status = 1;
+      return;
+    }
+    const double c = s_c, bk = buf[k - 1];
+    for (int j = k + tid; j <= e; j += kCombineThreads)
+      out[j - 1] = j == k ? c : __dsub_rn(__dadd_rn(buf[j - 1], c), bk);
+    __syncthreads();
+  }
+  // minimum (NaN ignored), then subtract
+  double mn = kInfD;
+  bool have = false;
+  for (int b = tid; b < bins; b += kCombineThreads) {
+    const double v = out[b];
+    if (v == v && (!have || v < mn)) {
+      mn = v;
+      have = true;
+    }
+  }
+  red_d[tid] = have ? mn : kInfD;
+  red_j[tid] = have ? 1 : 0;
+  __syncthreads();
+  for (int h = kCombineThreads / 2; h > 0; h >>= 1) {
+    if (tid < h && red_j[tid + h]) {
+      if (!red_j[tid] || red_d[tid + h] < red_d[tid]) red_d[tid] = red_d[tid + h];
+      red_j[tid] = 1;
+    }
+    __syncthreads();
+  }
+  const double m = red_j[0] ? red_d[0] : 0.0;
+  for (int b = tid; b < bins; b += kCombineThreads) out[b] = __dsub_rn(out[b], m);
+  if (tid == 0) *status = 0;
+}
+
+// MPI_BCAST of the combined ln g: every walker's copy.
+__global__ void wl_broadcast_kernel(WlWalker* __restrict__ W, const double* __restrict__ src) {
+  const int bins = W[0].bins;
+  double* dst = W[blockIdx.y].lng;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bins; b += gridDim.x * blockDim.x)
+    dst[b] = src[b];
+}
+
+void launch_wl_combine(WlWalker* d_walkers, int n, const WlGroup* d_groups, int n_groups, int bins,
+                       double* d_out, int* d_status, cudaStream_t stream) {
+  BRAWL_CARVEOUT(wl_combine_kernel);
+  wl_combine_kernel<<<1, kCombineThreads, 0, stream>>>(d_walkers, d_groups, n_groups, d_out, d_status);
+  dim3 grid((bins + 255) / 256, n);
+  BRAWL_CARVEOUT(wl_broadcast_kernel);
+  wl_broadcast_kernel<<<grid, 256, 0, stream>>>(d_walkers, d_out);
 }
 
 }  // namespace brawl

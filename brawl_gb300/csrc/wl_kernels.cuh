@@ -12,12 +12,17 @@ struct WlWalker {
   int32_t start, end;    // 1-based window bins
   int32_t bins;
   int32_t hist_period;   // INT(0.02*REAL(n_atoms))
-  double e0;             // e_unswapped at entry: full_energy(config)
+  const double* e0_src;  // full_energy(config) at entry, on the device
+  double e0;             // e_unswapped at entry (when e0_src is null)
   double e_out;          // e_unswapped at exit
   double wl_f;
   double e1, range;      // bin_edges(1), bin_edges(bins+1) - bin_edges(1)
   int64_t n_trials;
   int64_t accepted;
+  // A sweeps() call may run as several launches: i0 trials of the call are
+  // done, and e_state (when set) carries e_unswapped between the launches.
+  int64_t i0;
+  double* e_state;
 };
 
 // Walkers first..first+count-1 share a window and are averaged together.
@@ -28,6 +33,13 @@ struct WlGroup {
 uint32_t wl_smem_bytes(const Geom& g, int nb);
 void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, cudaStream_t stream);
 void launch_wl_average(const WlGroup* d_groups, int n_groups, WlWalker* d_walkers, int bins,
-                       cudaStream_t stream);
+                       int with_hist, cudaStream_t stream);
+uint32_t wl_exchange_smem_bytes(int per_window);
+void launch_wl_exchange(WlWalker* d_walkers, const double* d_energy, const WlGroup* d_groups,
+                        int n_windows, int per_window, int* d_ibin, int2* d_ov, int* d_partner,
+                        int* d_exchanged, int* d_n_accepted, cudaStream_t stream);
+void launch_wl_flatness(const WlWalker* d_walkers, int n, double* d_out, cudaStream_t stream);
+void launch_wl_combine(WlWalker* d_walkers, int n, const WlGroup* d_groups, int n_groups, int bins,
+                       double* d_out, int* d_status, cudaStream_t stream);
 
 }  // namespace brawl

@@ -39,6 +39,7 @@ extern "C" {
 #define BRAWL_ETIMEDOUT 4     /* a serving request did not finish in time */
 #define BRAWL_ECANCELLED 5    /* a serving request was cancelled */
 #define BRAWL_ESTATE 6        /* a device-side consistency check failed */
+#define BRAWL_EAGAIN 7        /* a serving request has not finished yet */
 
 /* ---- lattice codes (setup%lattice, src/initialise.F90:157-243) ----------- */
 #define BRAWL_SIMPLE_CUBIC 0  /* interaction_range 1-2 */
@@ -251,8 +252,29 @@ int brawl_wl_destroy(brawl_wl *wl);
  * histogram). */
 int brawl_wl_sweeps(brawl_wl *wl, int64_t n_trials, double wl_f, int hist_period,
                     int64_t *accepted);
-/* dos_average (src/wang-landau.F90:1127-1133): the window average alone. */
+/* dos_average (src/wang-landau.F90:1127-1133): ln g averaged over the
+ * walkers of each window (histograms untouched). */
 int brawl_wl_average(brawl_wl *wl);
+/* replica_exchange (src/wang-landau.F90:1392-1501, shuffle_rows :1513-1525)
+ * with walker w in the role of MPI rank w: every window must hold the same
+ * number of walkers and windows must be in ascending energy order.  The
+ * candidate lists are shuffled on walker 0's stream; a matched lower walker
+ * draws genrand() < exp(lng(i) - lng(j)) from its own stream; accepted
+ * pairs swap configurations.  partner / exchanged (n_walkers each, may be
+ * NULL): the walker paired with each walker (-1 for none) and whether its
+ * configuration was swapped; n_accepted (may be NULL): accepted pairs. */
+int brawl_wl_replica_exchange(brawl_wl *wl, int *partner, int *exchanged, int *n_accepted);
+/* Per-walker flatness minval(hist)/(sum(hist)/window_bins)
+ * (src/wang-landau.F90:222). */
+int brawl_wl_flatness(brawl_wl *wl, double *flatness);
+/* dos_combine (src/wang-landau.F90:1147-1194): the windows' ln g (first
+ * walker of each window) stitched where the slopes agree best and shifted
+ * to a zero minimum; every walker's ln g becomes the result (the
+ * reference's MPI_BCAST).  lng (bins, may be NULL) receives it.
+ * BRAWL_ESTATE when a window has no overlap with the previous one. */
+int brawl_wl_dos_combine(brawl_wl *wl, double *lng);
+/* mpi_wl_hist = 0 for every walker. */
+int brawl_wl_reset_hist(brawl_wl *wl);
 int brawl_wl_get_lng(brawl_wl *wl, int walker, double *lng);        /* bins */
 int brawl_wl_set_lng(brawl_wl *wl, int walker, const double *lng);
 int brawl_wl_get_hist(brawl_wl *wl, int walker, double *hist);      /* window bins */
@@ -265,6 +287,97 @@ int brawl_wl_swap_configs(brawl_wl *wl, int a, int b);
 /* n genrand() draws from a walker's stream (exchange shuffles and tests). */
 int brawl_wl_genrand(brawl_wl *wl, int walker, int64_t n, double *out);
 int brawl_wl_counters(brawl_wl *wl, int walker, int64_t *counters);
+
+/* ====================================================================== */
+/* Serving: a request loop that admits anneal, Wang-Landau and nested-    */
+/* sampling jobs as they arrive and runs every resident job's next        */
+/* quantum of work in shared launches (continuous batching).  No          */
+/* counterpart in the reference, whose drivers run one simulation per     */
+/* process; each job's results equal those of the same job run alone.     */
+/* ====================================================================== */
+typedef struct brawl_server brawl_server;
+
+typedef struct brawl_server_opts {
+    size_t hbm_budget;          /* device bytes for resident jobs (0: 4 GiB) */
+    int max_active;             /* resident jobs at most (0: 608) */
+    double round_ms;            /* device time each job's quantum of work aims at,
+                                   from the job's measured cost (0: 20 ms) */
+    int64_t max_trials;         /* cap on a job's Metropolis / Wang-Landau trials
+                                   per round (0: none) */
+    int max_iterations;         /* cap on a nested-sampling job's iterations per
+                                   round (0: none) */
+} brawl_server_opts;
+
+#define BRAWL_JOB_ANNEAL 1
+#define BRAWL_JOB_WL 2
+#define BRAWL_JOB_NS 3
+
+typedef struct brawl_job_desc {
+    int kind;                              /* BRAWL_JOB_* */
+    brawl_setup setup;
+    const double *V_ex;                    /* copied at submission */
+    uint32_t seed;
+    const double *species_concentrations;  /* n_species+1 ([0] = 0), copied */
+    const int64_t *species_numbers;        /* n_species or NULL, copied */
+    /* anneal (metropolis_simulated_annealing, src/metropolis.F90:84-558):
+     * T_steps temperatures T_start + k*delta_T, sweeps_per_T*n_atoms trials
+     * each; the energy is sampled at the end of every temperature. */
+    double T_start, delta_T;
+    int T_steps;
+    int64_t sweeps_per_T;
+    /* Wang-Landau window: wl_walkers walkers on one window of wl_bins bins
+     * spanning Ec -/+ h (Ry; Ec = the mean of the walkers' initial energies in
+     * walker order, h = wl_half_width or 1.25 times the largest |E_k - Ec|
+     * when that is larger);
+     * wl_calls sweeps() calls of wl_trials trials, ln f starting at wl_f and
+     * halved whenever every walker's histogram is flatter than wl_flatness
+     * (the histograms then reset); stops early once ln f < wl_tolerance. */
+    int wl_walkers, wl_bins, wl_calls;
+    int64_t wl_trials;
+    double wl_half_width, wl_f, wl_flatness, wl_tolerance;
+    /* nested sampling (src/nested_sampling.f90:45-206) */
+    int ns_walkers, ns_steps, ns_iter;
+} brawl_job_desc;
+
+typedef struct brawl_job_result {
+    int status;                 /* BRAWL_OK or the error that ended the job */
+    int kind;
+    double t_submit, t_admit, t_finish;  /* seconds since the server started */
+    double t_ready;             /* device objects built (after admission) */
+    int64_t trials;             /* Metropolis trials / WL trials / NS walk steps */
+    int64_t accepted;
+    double energy;              /* anneal: final energy; WL: walker 0's; NS: last ceiling */
+    double wl_f;                /* WL: ln f at the end */
+    int wl_halvings;
+    int n_values;               /* length of the job's value array */
+} brawl_job_result;
+
+int brawl_serve_create(const brawl_server_opts *opts, brawl_server **out);
+/* Stops the loop; jobs still queued or running end with BRAWL_ECANCELLED. */
+int brawl_serve_destroy(brawl_server *server);
+/* Queues a job (its inputs are copied); *id names it in later calls. */
+int brawl_serve_submit(brawl_server *server, const brawl_job_desc *job, uint64_t *id);
+/* BRAWL_OK with *result filled once the job has ended, BRAWL_EAGAIN before. */
+int brawl_serve_poll(brawl_server *server, uint64_t id, brawl_job_result *result);
+/* Waits up to timeout_s seconds (< 0: no limit); BRAWL_ETIMEDOUT if the
+ * job has not ended by then. */
+int brawl_serve_wait(brawl_server *server, uint64_t id, double timeout_s,
+                     brawl_job_result *result);
+/* The job's values (n_values doubles): anneal -- energy at the end of every
+ * temperature then the acceptance ratio of every temperature; WL -- ln g
+ * of walker 0 (wl_bins) then the bin edges (wl_bins+1); NS -- the ceiling
+ * of every iteration. */
+int brawl_serve_values(brawl_server *server, uint64_t id, double *values);
+/* The final configuration (reference layout; WL: walker 0; NS: walker 1). */
+int brawl_serve_config(brawl_server *server, uint64_t id, int8_t *config);
+/* Forgets an ended job. */
+int brawl_serve_release(brawl_server *server, uint64_t id);
+/* Rounds run and jobs resident/queued/ended so far. */
+int brawl_serve_stats(brawl_server *server, int64_t stats[4]);
+/* Per pipeline (anneal, Wang-Landau, nested sampling), 5 values each:
+ * rounds, seconds from launch to completion seen, seconds spent launching,
+ * seconds spent settling, trials (NS: iterations) handed out. */
+int brawl_serve_profile(brawl_server *server, double profile[15]);
 
 #ifdef __cplusplus
 }

@@ -11,6 +11,7 @@
  */
 #include "brawl_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -812,4 +813,137 @@ int64_t bo_wl_sweep(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
     if (c) c->accepted += accepted;
     *energy = e_unswapped;
     return accepted;
+}
+
+/* shuffle_rows (src/wang-landau.F90:1513-1525): rows i = n..2, partner
+ * MIN(1+int(genrand()*i), n), on the stream it is given. */
+static void wl_shuffle_rows(int rows[][2], int n, bo_rng *r)
+{
+    for (int i = n; i >= 2; i--) {
+        int k = 1 + (int)(bo_rng_uniform(r) * (double)i);
+        if (k > n) k = n;
+        int t0 = rows[i - 1][0], t1 = rows[i - 1][1];
+        rows[i - 1][0] = rows[k - 1][0];
+        rows[i - 1][1] = rows[k - 1][1];
+        rows[k - 1][0] = t0;
+        rows[k - 1][1] = t1;
+    }
+}
+
+int bo_wl_replica_exchange(int n_windows, int per_window, const int *win_start,
+                           const int *win_end, const double *bin_edges, int bins,
+                           const double *energies, const double *lng, bo_rng *rngs,
+                           int8_t *cfgs, size_t cfg_bytes, int *partner, int *accepted)
+{
+    /* src/wang-landau.F90:1403-1435: every walker's bin and the overlap it
+     * lies in (the lower window's index, 0 for none); the walker index plays
+     * the MPI rank (rank r is walker r, window r/per_window + 1). */
+    const int n = n_windows * per_window;
+    int *ibin = (int *)malloc(sizeof(int) * (size_t)n);
+    int (*ov)[2] = malloc(sizeof(int[2]) * (size_t)n);
+    int (*lo)[2] = malloc(sizeof(int[2]) * (size_t)per_window);
+    int (*up)[2] = malloc(sizeof(int[2]) * (size_t)per_window);
+    int (*pairs)[2] = malloc(sizeof(int[2]) * (size_t)per_window);
+    int8_t *tmp = (int8_t *)malloc(cfg_bytes);
+    int n_acc = 0;
+    for (int w = 0; w < n; w++) {
+        int idx = w / per_window + 1;
+        int ib = bo_wl_bin_index(energies[w], bin_edges, bins);
+        int lower = 0, upper = 0;
+        if (idx > 1)
+            lower = ib < win_end[idx - 2] + 1 && ib > win_start[idx - 1] - 1;
+        if (idx < n_windows)
+            upper = ib > win_start[idx] - 1 && ib < win_end[idx - 1] + 1;
+        ibin[w] = ib;
+        ov[w][0] = w;
+        ov[w][1] = upper ? idx : (lower ? idx - 1 : 0);
+        partner[w] = -1;
+        accepted[w] = 0;
+    }
+    /* :1437-1494: per adjacent pair of windows, shuffle both lists on the
+     * first walker's stream, match equal overlaps, then every matched lower
+     * walker draws against its own ln g and the pair swap configurations */
+    for (int i = 1; i <= n_windows - 1; i++) {
+        memcpy(lo, ov + (size_t)(i - 1) * per_window, sizeof(int[2]) * (size_t)per_window);
+        memcpy(up, ov + (size_t)i * per_window, sizeof(int[2]) * (size_t)per_window);
+        wl_shuffle_rows(lo, per_window, &rngs[0]);
+        wl_shuffle_rows(up, per_window, &rngs[0]);
+        int np = 0;
+        for (int j = 0; j < per_window; j++) {
+            if (lo[j][1] == 0) continue;
+            for (int k = 0; k < per_window; k++) {
+                if (up[k][1] == 0) continue;
+                if (lo[j][1] == up[k][1]) {
+                    pairs[np][0] = lo[j][0];
+                    pairs[np][1] = up[k][0];
+                    np++;
+                    lo[j][0] = lo[j][1] = 0;
+                    up[k][0] = up[k][1] = 0;
+                }
+            }
+        }
+        for (int p = 0; p < np; p++) {
+            int a = pairs[p][0], b = pairs[p][1];
+            int jb = bo_wl_bin_index(energies[b], bin_edges, bins);
+            const double *la = lng + (size_t)a * bins;
+            partner[a] = b;
+            partner[b] = a;
+            if (bo_rng_uniform(&rngs[a]) < exp(la[ibin[a] - 1] - la[jb - 1])) {
+                int8_t *ca = cfgs + (size_t)a * cfg_bytes, *cb = cfgs + (size_t)b * cfg_bytes;
+                memcpy(tmp, ca, cfg_bytes);
+                memcpy(ca, cb, cfg_bytes);
+                memcpy(cb, tmp, cfg_bytes);
+                accepted[a] = accepted[b] = 1;
+                n_acc++;
+            }
+        }
+    }
+    free(ibin); free(ov); free(lo); free(up); free(pairs); free(tmp);
+    return n_acc;
+}
+
+int bo_wl_dos_combine(int n_windows, const int *win_start, const int *win_end, int bins,
+                      const double *lng_windows, double *out)
+{
+    /* src/wang-landau.F90:1147-1194: start from window 1's ln g; for every
+     * next window find, in the overlap, the bin where the two slopes differ
+     * least (first such bin), shift the window's ln g to meet the combined
+     * one there and overwrite from that bin to the window's end; then
+     * subtract the minimum.  beta_index carries over between windows as in
+     * the reference (it is initialised once). */
+    memcpy(out, lng_windows, sizeof(double) * (size_t)bins);
+    int beta_index = 0;
+    for (int i = 2; i <= n_windows; i++) {
+        const double *buf = lng_windows + (size_t)(i - 1) * bins;
+        const int s = win_start[i - 1], e = win_end[i - 1];
+        double beta_diff = DBL_MAX;
+        for (int j = 0; j <= win_end[i - 2] - win_start[i - 1] - 1; j++) {
+            double bo = out[s + j] - out[s + j - 1];
+            double bm = buf[s + j] - buf[s + j - 1];
+            if (fabs(bo - bm) < beta_diff) {
+                beta_diff = fabs(bo - bm);
+                beta_index = s + j + 1;
+            }
+        }
+        if (beta_index < 1) return -1;     /* no overlap: the reference indexes bin 0 */
+        for (int j = beta_index; j <= e; j++)
+            out[j - 1] = buf[j - 1] + out[beta_index - 1] - buf[beta_index - 1];
+    }
+    double mn = 0.0;
+    int have = 0;
+    for (int b = 0; b < bins; b++)
+        if (out[b] == out[b] && (!have || out[b] < mn)) { mn = out[b]; have = 1; }
+    for (int b = 0; b < bins; b++) out[b] = out[b] - mn;
+    return 0;
+}
+
+double bo_wl_flatness(const double *hist, int n)
+{
+    /* src/wang-landau.F90:222: minval(hist)/(sum(hist)/mpi_bins) */
+    double mn = hist[0], s = 0.0;
+    for (int b = 0; b < n; b++) {
+        if (hist[b] < mn) mn = hist[b];
+        s = s + hist[b];
+    }
+    return mn / (s / (double)n);
 }

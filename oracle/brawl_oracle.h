@@ -19,6 +19,7 @@
 #ifndef BRAWL_ORACLE_H
 #define BRAWL_ORACLE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -161,6 +162,28 @@ typedef struct {
 int64_t bo_wl_sweep(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
                     bo_rng *r, const double *bin_edges, double *lng,
                     double *hist, double *energy, bo_counters *c);
+
+/* ---- Wang-Landau exchange and stitching (src/wang-landau.F90) ------------ */
+/* replica_exchange (:1392-1501) with shuffle_rows (:1513-1525).  Walkers are
+ * ordered by window, per_window each (walker w plays MPI rank w, window
+ * w/per_window + 1); win_start/win_end: 1-based bins of every window;
+ * energies: full energies at the call; lng: n x bins; rngs: n streams (the
+ * shuffles draw from rngs[0], rank 0's); cfgs: n x cfg_bytes, swapped on
+ * acceptance.  partner[w]: walker paired with w or -1; accepted[w]: 1 when
+ * w's configuration was exchanged.  Returns the accepted exchanges. */
+int bo_wl_replica_exchange(int n_windows, int per_window, const int *win_start,
+                           const int *win_end, const double *bin_edges, int bins,
+                           const double *energies, const double *lng, bo_rng *rngs,
+                           int8_t *cfgs, size_t cfg_bytes, int *partner, int *accepted);
+
+/* dos_combine (:1147-1194): lng_windows holds each window's ln g (n_windows
+ * x bins, after the in-window average); out: the stitched, min-shifted ln g.
+ * Returns -1 when a window has no overlap with the previous one. */
+int bo_wl_dos_combine(int n_windows, const int *win_start, const int *win_end, int bins,
+                      const double *lng_windows, double *out);
+
+/* flatness (:222): minval(hist)/(sum(hist)/n). */
+double bo_wl_flatness(const double *hist, int n);
 
 #ifdef __cplusplus
 }

@@ -121,6 +121,11 @@ def lib():
         L.bo_wl_sweep.argtypes = [C.POINTER(Model), C.POINTER(WlParams), vp, C.POINTER(Rng), vp,
                                   vp, vp, vp, C.POINTER(Counters)]
         L.bo_wl_sweep.restype = i64
+        L.bo_wl_replica_exchange.argtypes = [C.c_int, C.c_int, vp, vp, vp, C.c_int, vp, vp,
+                                             C.POINTER(Rng), vp, C.c_size_t, vp, vp]
+        L.bo_wl_dos_combine.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
+        L.bo_wl_flatness.argtypes = [vp, C.c_int]
+        L.bo_wl_flatness.restype = dp
         _lib = L
     return _lib
 
@@ -299,6 +304,52 @@ class OracleModel:
 def wl_bin_index(energy, bin_edges, bins) -> int:
     be = np.ascontiguousarray(bin_edges, dtype=np.float64)
     return lib().bo_wl_bin_index(energy, _ptr(be), bins)
+
+
+def wl_replica_exchange(win_start, win_end, per_window, bin_edges, energies, lngs, rngs, cfgs):
+    """replica_exchange over walkers ordered by window.  lngs: list of ln g
+    arrays (read only); rngs: list of OracleRng (advanced in place); cfgs:
+    list of equal-shape configurations (swapped in place).  Returns
+    (n_accepted, partner, accepted)."""
+    n_windows = len(win_start)
+    n = n_windows * per_window
+    assert len(lngs) == n and len(rngs) == n and len(cfgs) == n
+    ws = np.ascontiguousarray(win_start, dtype=np.int32)
+    we = np.ascontiguousarray(win_end, dtype=np.int32)
+    be = np.ascontiguousarray(bin_edges, dtype=np.float64)
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    L = np.ascontiguousarray(np.stack(lngs), dtype=np.float64)
+    arr = (Rng * n)()
+    for k, r in enumerate(rngs):
+        C.memmove(C.byref(arr[k]), C.byref(r.s), C.sizeof(Rng))
+    cf = np.ascontiguousarray(np.stack(cfgs))
+    partner = np.zeros(n, dtype=np.int32)
+    acc = np.zeros(n, dtype=np.int32)
+    na = lib().bo_wl_replica_exchange(n_windows, per_window, _ptr(ws), _ptr(we), _ptr(be), be.size - 1,
+                                      _ptr(e), _ptr(L), arr, _ptr(cf), cf[0].nbytes, _ptr(partner),
+                                      _ptr(acc))
+    for k, r in enumerate(rngs):
+        C.memmove(C.byref(r.s), C.byref(arr[k]), C.sizeof(Rng))
+    for k in range(n):
+        cfgs[k][...] = cf[k]
+    return na, partner, acc
+
+
+def wl_dos_combine(win_start, win_end, lng_windows):
+    """dos_combine: lng_windows is one ln g per window (n_windows x bins)."""
+    ws = np.ascontiguousarray(win_start, dtype=np.int32)
+    we = np.ascontiguousarray(win_end, dtype=np.int32)
+    L = np.ascontiguousarray(lng_windows, dtype=np.float64)
+    out = np.zeros(L.shape[1], dtype=np.float64)
+    rc = lib().bo_wl_dos_combine(len(ws), _ptr(ws), _ptr(we), L.shape[1], _ptr(L), _ptr(out))
+    if rc != 0:
+        raise ValueError("a window has no overlap with the previous one")
+    return out
+
+
+def wl_flatness(hist) -> float:
+    h = np.ascontiguousarray(hist, dtype=np.float64)
+    return lib().bo_wl_flatness(_ptr(h), h.size)
 
 
 def shell_offsets(lattice, shell):

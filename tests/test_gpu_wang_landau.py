@@ -94,3 +94,110 @@ def test_wang_landau_walker_outside_window_is_reported():
     with pytest.raises(B.BrawlError) as ex:
         wl.sweeps(10, 0.05, 1)
     assert ex.value.code == 6
+
+
+def _exchange_system(lattice, n, ns, nsh, n_windows, per_window, bins, seed):
+    """Walkers spread over n_windows overlapping windows of `bins` bins, each
+    starting inside its window; bin edges spanning a pool of random
+    configurations' energies."""
+    rng = np.random.default_rng(seed)
+    V = random_V(rng, ns, nsh)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    mod0 = O.OracleModel(lattice, *n, V)
+    r0 = O.OracleRng(seed + 1)
+    pool = [mod0.initial_setup(r0, conc_vector(ns))[0] for _ in range(160)]
+    E = np.array([mod0.total_energy(c) for c in pool])
+    lo_e, hi_e = float(E.min()), float(E.max())
+    pad = 1e-3 * (hi_e - lo_e)
+    bin_edges = (lo_e - pad) + np.arange(bins + 1) * ((hi_e - lo_e + 2 * pad) / bins)
+    # windows of equal width, each overlapping the next by half its width
+    width = (2 * bins) // (n_windows + 1)
+    starts = [1 + k * (width // 2) for k in range(n_windows)]
+    ends = [s + width - 1 for s in starts]
+    ends[-1] = bins
+    bidx = np.array([O.wl_bin_index(e, bin_edges, bins) for e in E])
+    used, walkers = set(), []
+    for k in range(n_windows):
+        # prefer configurations in the overlaps so exchanges are attempted
+        cand = [i for i in range(len(pool)) if starts[k] <= bidx[i] <= ends[k] and i not in used]
+        cand.sort(key=lambda i: min(bidx[i] - starts[k], ends[k] - bidx[i]))
+        assert len(cand) >= per_window
+        for i in cand[:per_window]:
+            used.add(i)
+            walkers.append(dict(setup=setup, V=V, seed=110179 + 11 * len(walkers),
+                                config=pool[i].copy(), start_idx=starts[k], end_idx=ends[k],
+                                window=k))
+    return setup, V, walkers, bin_edges, starts, ends
+
+
+@pytest.mark.parametrize("lattice,n,ns,nsh,n_windows,per_window", [
+    ("bcc", (4, 4, 4), 4, 4, 4, 3),
+    ("fcc", (3, 3, 3), 3, 3, 3, 4),
+])
+def test_wang_landau_exchange_flatness_combine_match_oracle(lattice, n, ns, nsh, n_windows, per_window):
+    bins = 60
+    setup, V, walkers, bin_edges, starts, ends = _exchange_system(lattice, n, ns, nsh, n_windows,
+                                                                  per_window, bins, 77)
+    mods = [O.OracleModel(lattice, *n, V) for _ in walkers]
+    cfgs = [w["config"].copy() for w in walkers]
+    rngs = [O.OracleRng(w["seed"]) for w in walkers]
+    lngs = [np.zeros(bins) for _ in walkers]
+    hists = [np.zeros(w["end_idx"] - w["start_idx"] + 1) for w in walkers]
+    wl = B.WangLandauWalkers(walkers, bin_edges)
+    wl_f = 1.0
+    period = max(1, int(0.02 * float(np.float32(setup.n_atoms))))
+    total_acc = 0
+    for it in range(6):
+        acc_o = _emulate(mods, cfgs, rngs, walkers, bin_edges, lngs, hists, 400, wl_f, period)
+        assert list(wl.sweeps(400, wl_f, period)) == acc_o
+        E = [mods[k].total_energy(cfgs[k]) for k in range(len(walkers))]
+        na_o, partner_o, exch_o = O.wl_replica_exchange(starts, ends, per_window, bin_edges, E, lngs,
+                                                        rngs, cfgs)
+        na_g, partner_g, exch_g = wl.replica_exchange()
+        assert na_g == na_o
+        assert np.array_equal(partner_g, partner_o)
+        assert np.array_equal(exch_g, exch_o)
+        for k in range(len(walkers)):
+            assert np.array_equal(wl.config(k), cfgs[k])
+        total_acc += na_o
+        flat_o = np.array([O.wl_flatness(h) for h in hists])
+        assert np.array_equal(wl.flatness(), flat_o)
+    assert (partner_o >= 0).any()
+    for k in range(len(walkers)):
+        assert np.array_equal(wl.genrand(k, 8), np.array([rngs[k].uniform() for _ in range(8)]))
+    # dos_average then dos_combine, as at the end of a Wang-Landau iteration
+    wl.average()
+    for k0 in range(0, len(walkers), per_window):
+        idx = list(range(k0, k0 + per_window))
+        s = lngs[idx[0]].copy()
+        for k in idx[1:]:
+            s = s + lngs[k]
+        s = s / float(np.float32(per_window))
+        for k in idx:
+            lngs[k][:] = s
+    for k in range(len(walkers)):
+        assert np.array_equal(wl.lng(k), lngs[k])
+    comb_o = O.wl_dos_combine(starts, ends, np.stack([lngs[k] for k in range(0, len(walkers), per_window)]))
+    comb_g = wl.dos_combine()
+    assert np.array_equal(comb_g, comb_o)
+    for k in range(len(walkers)):
+        assert np.array_equal(wl.lng(k), comb_o)
+    wl.reset_hist()
+    assert not wl.hist(0).any()
+
+
+def test_wang_landau_exchange_needs_equal_windows():
+    rng = np.random.default_rng(5)
+    V = random_V(rng, 2, 2)
+    setup = B.Setup("bcc", 3, 3, 3, 2, 2)
+    mod = O.OracleModel("bcc", 3, 3, 3, V)
+    r = O.OracleRng(9)
+    cfgs = [mod.initial_setup(r, conc_vector(2))[0] for _ in range(3)]
+    e = [mod.total_energy(c) for c in cfgs]
+    bin_edges = min(e) - 1.0 + np.arange(21) * ((max(e) - min(e) + 2.0) / 20)
+    ws = [dict(setup=setup, V=V, seed=k + 1, config=cfgs[k], start_idx=1, end_idx=20,
+               window=0 if k < 2 else 1) for k in range(3)]
+    wl = B.WangLandauWalkers(ws, bin_edges)
+    with pytest.raises(B.BrawlError) as ex:
+        wl.replica_exchange()
+    assert ex.value.code == 1

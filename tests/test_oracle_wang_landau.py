@@ -1,0 +1,152 @@
+"""The oracle's Wang-Landau exchange, stitching and flatness
+(src/wang-landau.F90:222, 1147-1194, 1392-1525) against an independent
+pure-Python restatement of the same reference lines, plus hand-worked
+cases.  CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def _py_bin(e, edges, bins):
+    return int(((e - edges[0]) / (edges[bins] - edges[0])) * bins) + 1
+
+
+def _py_exchange(ws, we, pw, edges, E, lngs, rng_words, cfgs):
+    """replica_exchange + shuffle_rows written out directly from the
+    reference; rng_words[w] is a callable returning walker w's next
+    genrand()."""
+    nwin = len(ws)
+    bins = len(edges) - 1
+    n = nwin * pw
+    ib, ov = [], []
+    for w in range(n):
+        idx = w // pw + 1
+        b = _py_bin(E[w], edges, bins)
+        lower = idx > 1 and b < we[idx - 2] + 1 and b > ws[idx - 1] - 1
+        upper = idx < nwin and b > ws[idx] - 1 and b < we[idx - 1] + 1
+        ib.append(b)
+        ov.append([w, idx if upper else (idx - 1 if lower else 0)])
+    partner, acc = [-1] * n, [0] * n
+    for i in range(1, nwin):
+        lo = [list(r) for r in ov[(i - 1) * pw:i * pw]]
+        up = [list(r) for r in ov[i * pw:(i + 1) * pw]]
+        for arr in (lo, up):
+            for r in range(pw, 1, -1):
+                k = min(1 + int(rng_words[0]() * r), pw)
+                arr[r - 1], arr[k - 1] = arr[k - 1], arr[r - 1]
+        ex = []
+        for j in range(pw):
+            if lo[j][1] == 0:
+                continue
+            for k in range(pw):
+                if up[k][1] == 0:
+                    continue
+                if lo[j][1] == up[k][1]:
+                    ex.append((lo[j][0], up[k][0]))
+                    lo[j] = [0, 0]
+                    up[k] = [0, 0]
+        for a, b in ex:
+            jb = _py_bin(E[b], edges, bins)
+            partner[a], partner[b] = b, a
+            if rng_words[a]() < math.exp(lngs[a][ib[a] - 1] - lngs[a][jb - 1]):
+                cfgs[a], cfgs[b] = cfgs[b].copy(), cfgs[a].copy()
+                acc[a] = acc[b] = 1
+    return sum(acc) // 2, partner, acc
+
+
+@pytest.mark.parametrize("nwin,pw,seed", [(2, 2, 1), (4, 3, 2), (5, 4, 3), (3, 6, 4)])
+def test_exchange_matches_python_restatement(nwin, pw, seed):
+    rng = np.random.default_rng(seed)
+    bins = 40
+    width = (2 * bins) // (nwin + 1)
+    ws = [1 + k * (width // 2) for k in range(nwin)]
+    we = [s + width - 1 for s in ws]
+    we[-1] = bins
+    edges = np.linspace(-1.0, 1.0, bins + 1)
+    n = nwin * pw
+    E = []
+    for w in range(n):
+        k = w // pw
+        b = int(rng.integers(ws[k], we[k] + 1))
+        E.append(float(edges[b - 1] + 0.5 * (edges[b] - edges[b - 1])))
+    lngs = [rng.uniform(0, 3, bins) for _ in range(n)]
+    cfgs = [rng.integers(1, 4, 16).astype(np.int8) for _ in range(n)]
+    r_c = [O.OracleRng(1000 + w) for w in range(n)]
+    r_p = [O.OracleRng(1000 + w) for w in range(n)]
+    cfg_c = [c.copy() for c in cfgs]
+    cfg_p = [c.copy() for c in cfgs]
+    na, partner, acc = O.wl_replica_exchange(ws, we, pw, edges, E, lngs, r_c, cfg_c)
+    na_p, partner_p, acc_p = _py_exchange(ws, we, pw, edges, E, lngs, [r.uniform for r in r_p], cfg_p)
+    assert na == na_p
+    assert list(partner) == partner_p
+    assert list(acc) == acc_p
+    for a, b in zip(cfg_c, cfg_p):
+        assert np.array_equal(a, b)
+    for a, b in zip(r_c, r_p):
+        assert np.array_equal(a.state_words(), b.state_words())
+
+
+def test_exchange_shuffles_draw_from_walker_zero():
+    """Every adjacent pair of windows shuffles two lists of pw rows on rank
+    0's stream: 2 (pw - 1) draws each, whether or not anything matches."""
+    nwin, pw, bins = 4, 3, 40
+    ws, we = [1, 11, 21, 31], [10, 20, 30, 40]     # no overlaps: nothing matches
+    edges = np.linspace(0.0, 1.0, bins + 1)
+    E = [float(edges[ws[w // pw] + 2]) for w in range(nwin * pw)]
+    rngs = [O.OracleRng(7 + w) for w in range(nwin * pw)]
+    ref = O.OracleRng(7)
+    cfgs = [np.zeros(4, np.int8) for _ in range(nwin * pw)]
+    na, partner, acc = O.wl_replica_exchange(ws, we, pw, edges, E, [np.zeros(bins)] * (nwin * pw),
+                                             rngs, cfgs)
+    assert na == 0 and (partner == -1).all()
+    for _ in range(2 * (pw - 1) * (nwin - 1)):
+        ref.uniform()
+    assert np.array_equal(rngs[0].state_words(), ref.state_words())
+    assert np.array_equal(rngs[1].state_words(), O.OracleRng(8).state_words())
+
+
+def test_dos_combine_hand_case():
+    lw = np.array([[0, 1, 2, 3, 4, 5, 6, 0, 0, 0],
+                   [0, 0, 0, 10, 11, 12.5, 13, 14, 15, 16]], dtype=np.float64)
+    out = O.wl_dos_combine([1, 4], [6, 10], lw)
+    # overlap bins 4..6: slopes agree at bin 4->5, so bins 5..10 follow
+    # window 2 shifted by 4 - 11
+    assert np.array_equal(out, [0, 1, 2, 3, 4, 5.5, 6, 7, 8, 9])
+
+
+def test_dos_combine_rounds_like_the_reference_loop():
+    rng = np.random.default_rng(11)
+    bins = 30
+    ws, we = [1, 8, 16], [12, 20, 30]
+    lw = rng.uniform(-5, 5, (3, bins)).cumsum(axis=1)
+    out = O.wl_dos_combine(ws, we, lw)
+    comb = lw[0].copy()
+    beta_index = 0
+    for i in range(2, 4):
+        buf = lw[i - 1]
+        s, e = ws[i - 1], we[i - 1]
+        diff = np.finfo(np.float64).max
+        for j in range(0, we[i - 2] - ws[i - 1]):
+            bo = comb[s + j] - comb[s + j - 1]
+            bm = buf[s + j] - buf[s + j - 1]
+            if abs(bo - bm) < diff:
+                diff = abs(bo - bm)
+                beta_index = s + j + 1
+        for j in range(beta_index, e + 1):
+            comb[j - 1] = buf[j - 1] + comb[beta_index - 1] - buf[beta_index - 1]
+    comb = comb - comb.min()
+    assert np.array_equal(out, comb)
+
+
+def test_dos_combine_without_overlap_is_an_error():
+    with pytest.raises(ValueError):
+        O.wl_dos_combine([1, 6], [5, 10], np.zeros((2, 10)))
+
+
+def test_flatness():
+    assert O.wl_flatness([2.0, 4.0, 6.0]) == 2.0 / 4.0
+    h = np.array([0.25, 0.5, 0.75, 1.0])
+    assert O.wl_flatness(h) == 0.25 / (2.5 / 4)
