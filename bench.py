@@ -319,6 +319,8 @@ def main() -> int:
     ap.add_argument("--serve-L-max", type=int, default=16)
     ap.add_argument("--serve-sweeps-max", type=int, default=500)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--speculation", type=int, default=0,
+                    help="trials per speculative round of the Metropolis kernel (0: library default)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -347,6 +349,8 @@ def main() -> int:
                            beta=1.0 / (float(wl["T"][r]) * K_B_IN_RY),
                            species_concentrations=wl["conc"]))
     batch = B.Batch(chains)
+    if args.speculation:
+        batch.set_speculation(args.speculation)
     sites = np.array([n_sites(int(L)) for L in wl["L"]], dtype=np.int64)
     trials = sites * args.sweeps_per_step
     trials_per_step = int(trials.sum())

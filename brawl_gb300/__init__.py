@@ -134,6 +134,7 @@ def load(rebuild: bool = False):
         "brawl_batch_destroy": ([vp], i),
         "brawl_batch_size": ([vp, vp], i),
         "brawl_batch_set_beta": ([vp, vp], i),
+        "brawl_batch_set_speculation": ([vp, i], i),
         "brawl_batch_metropolis_run": ([vp, vp, vp], i),
         "brawl_batch_metropolis_run_async": ([vp, vp, vp], i),
         "brawl_batch_sync": ([vp], i),
@@ -376,6 +377,10 @@ class Batch:
     def set_beta(self, beta) -> None:
         b = np.ascontiguousarray(np.broadcast_to(np.asarray(beta, dtype=np.float64), (self.n,)))
         _check(load().brawl_batch_set_beta(self._h, _ptr(b)))
+
+    def set_speculation(self, trials_per_round: int) -> None:
+        """Trials per speculative round of the fcc/bcc kernel (1-4); speed only."""
+        _check(load().brawl_batch_set_speculation(self._h, int(trials_per_round)))
 
     def _trials(self, n_trials) -> np.ndarray:
         return np.ascontiguousarray(np.broadcast_to(np.asarray(n_trials, dtype=np.int64), (self.n,)))

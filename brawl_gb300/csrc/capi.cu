@@ -348,6 +348,8 @@ struct brawl_batch {
   int n_halo_launch = 0;
   std::vector<unsigned long long> last_counters;
   int device = 0;
+  int max_optin = 0;
+  int spec_nc = kDefaultSpeculation;  // trials per speculative round (1: none)
 };
 
 struct brawl_ctx {
@@ -443,7 +445,8 @@ int run_metropolis(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, b
   if (serial) {
     for (int k = 0; k < n; ++k) {
       if (k < nh)
-        launch_metropolis_halo(b->d_jobs + k, 1, b->halo_smem, b->halo_max_z, stream);
+        launch_halo_chains(b->d_jobs + k, 1, b->halo_smem, b->halo_max_z, b->spec_nc, b->max_optin,
+                           stream);
       else
         launch_metropolis(b->d_jobs + k, 1, b->smem_lat, b->use_D, b->smem_bytes, b->max_z,
                           stream);
@@ -451,7 +454,8 @@ int run_metropolis(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, b
       CUDA_TRY(cudaStreamSynchronize(stream));
     }
   } else {
-    if (nh > 0) launch_metropolis_halo(b->d_jobs, nh, b->halo_smem, b->halo_max_z, stream);
+    if (nh > 0)
+      launch_halo_chains(b->d_jobs, nh, b->halo_smem, b->halo_max_z, b->spec_nc, b->max_optin, stream);
     if (n - nh > 0)
       launch_metropolis(b->d_jobs + nh, n - nh, b->smem_lat, b->use_D, b->smem_bytes, b->max_z,
                         stream);
@@ -499,6 +503,7 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
   // shared memory: lattice staged when every chain fits
   int max_optin = 0;
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  b->max_optin = max_optin;
   uint32_t need_smem = 0, need_gmem = 0;
   for (size_t c = 0; c < b->models.size(); ++c) {
     HaloGeom H;
@@ -666,6 +671,12 @@ int brawl_batch_destroy(brawl_batch* b) {
 int brawl_batch_size(brawl_batch* b, int* n) {
   if (!b || !n) return fail(BRAWL_EINVAL, "null argument");
   *n = (int)b->jobs.size();
+  return BRAWL_OK;
+}
+
+int brawl_batch_set_speculation(brawl_batch* b, int trials_per_round) {
+  if (!b || trials_per_round < 1 || trials_per_round > 4) return fail(BRAWL_EINVAL, "trials per round must be 1-4");
+  b->spec_nc = trials_per_round;
   return BRAWL_OK;
 }
 

@@ -46,6 +46,9 @@ namespace brawl {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMTN = 624;
+// trials per speculative round of the halo Metropolis kernel (1: one trial
+// at a time); brawl_batch_set_speculation overrides it per batch
+constexpr int kDefaultSpeculation = 1;
 constexpr int kMTM = 397;
 constexpr int kMaxZ = 168;           // neighbour entries of bcc with 10 shells
 constexpr int kMaxLaneEntries = 11;  // ceil(2 * kMaxZ / 32)

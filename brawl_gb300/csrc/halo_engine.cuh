@@ -42,12 +42,13 @@ __device__ __forceinline__ uint32_t mt_untemper(uint32_t y) {
 }
 
 // Ring of two tempered blocks in tbuf[0, 1248), plus a mirror of the first
-// 8 words at tbuf[1248, 1256) so a trial's words never wrap.  `idx` is the
+// 32 words at tbuf[1248, 1280) so the words of a trial (or of a round of
+// speculated trials) never wrap.  `idx` is the
 // ring slot of the next word, `avail` the generated words not yet consumed
 // (0..1248), `next_half` the half the next generated block goes to; mt holds
 // the newest generated block, untempered.
 constexpr int kRing = 2 * kMTN;
-constexpr int kRingMirror = 8;
+constexpr int kRingMirror = 32;
 
 struct Ring {
   int idx;
@@ -76,7 +77,7 @@ __device__ __forceinline__ void ring_init(const uint32_t* mt, uint32_t* tbuf, in
   __syncwarp();
 }
 
-// Makes n <= 8 words available from R.idx.  A block is only generated when
+// Makes n <= 32 words available from R.idx.  A block is only generated when
 // fewer than n remain, so the half it overwrites has been consumed.
 __device__ __forceinline__ void ring_ensure(uint32_t* mt, uint32_t* tbuf, Ring& R, int n,
                                             int lane) {
@@ -117,10 +118,10 @@ __device__ __forceinline__ int halo_index(const HaloGeom& H, int Z, int Yp, int 
 // Fills the padded lattice from the compact one (every padded cell reads its
 // canonical cell).
 __device__ inline void halo_fill(const Geom& g, const HaloGeom& H, const int8_t* lat_c,
-                                 int8_t* lat_p, int lane) {
+                                 int8_t* lat_p, int lane, int stride = 32) {
   const int PX = H.NX + 2 * H.hx, PY = H.NY + 2 * H.hy, PZ = H.NZ + 2 * H.hz;
   const int total = PX * PY * PZ;
-  for (int t = lane; t < total; t += 32) {
+  for (int t = lane; t < total; t += stride) {
     const int px = t % PX, py = (t / PX) % PY, pz = t / (PX * PY);
     int X = px - H.hx, Y = py - H.hy, Z = pz - H.hz;
     X = X < 0 ? X + H.NX : (X >= H.NX ? X - H.NX : X);
@@ -132,8 +133,8 @@ __device__ inline void halo_fill(const Geom& g, const HaloGeom& H, const int8_t*
 
 // Copies the interior back to the compact lattice.
 __device__ inline void halo_store(const Geom& g, const HaloGeom& H, const int8_t* lat_p,
-                                  int8_t* lat_c, int lane) {
-  for (int t = lane; t < g.n_sites; t += 32) {
+                                  int8_t* lat_c, int lane, int stride = 32) {
+  for (int t = lane; t < g.n_sites; t += stride) {
     const int Z = t / g.sz, r = t - Z * g.sz, Y = r / g.sy, X = r - Y * g.sy;
     lat_c[t] = lat_p[halo_index(H, Z, Y, X)];
   }

@@ -52,7 +52,7 @@ struct HaloLayout {
   int32_t F_off, D_off;
 };
 
-constexpr int kTbufWords = 2 * kMTN + 8;
+constexpr int kTbufWords = 2 * kMTN + 32;  // the ring and its mirror
 
 __host__ __device__ inline HaloLayout halo_layout(const Geom& g, const HaloGeom& H) {
   HaloLayout L;
@@ -75,6 +75,16 @@ __host__ __device__ inline HaloLayout halo_layout(const Geom& g, const HaloGeom&
 int lane_entries_for(int max_z);
 
 // Metropolis swap trials for chains staged with a halo (fcc/bcc that fit).
+// Speculative rounds of nc (2-4) trials per chain, nc(nc+1)/2 warps per CTA
+// (metropolis_spec.cu); spec_static_smem is the static shared memory the
+// kernel adds to smem_bytes.
+void launch_metropolis_spec(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z, int nc,
+                            cudaStream_t stream);
+uint32_t spec_static_smem(int nc);
+// The halo chains: speculative rounds of nc trials when nc >= 2 and the
+// slots fit beside the dynamic shared memory, the one-trial kernel otherwise.
+void launch_halo_chains(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z, int nc,
+                        int max_optin, cudaStream_t stream);
 void launch_metropolis_halo(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z,
                             cudaStream_t stream);
 

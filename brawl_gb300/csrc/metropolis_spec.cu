@@ -1,0 +1,336 @@
+// metropolis_spec.cu -- speculative rounds of Metropolis-Kawasaki swap trials
+// for fcc/bcc chains staged with a periodic halo.
+//
+// A chain's trials are sequential, and a trial's result depends on the
+// previous ones in two ways only: where its six (or seven) mt19937ar words
+// start, and the lattice it reads.  A trial draws six words (the two sites,
+// monte_carlo_step_lattice, src/metropolis.F90:751-813) and a seventh only
+// when the species differ and dE >= 0.  So trial d of a round starts at
+// offset 6d + m, m being how many of the d earlier trials drew a seventh
+// word (4d + m with nbr_swap).  A round of NC trials evaluates every
+// candidate (d, m), 0 <= m <= d, at once, one warp each, all on the lattice
+// as it stood at the start of the round.  The trials are then resolved in
+// order: trial d takes candidate (d, m_d).  That candidate is valid unless an
+// accepted swap of an earlier trial in the round lies within interaction
+// range of one of its sites, i.e. the swap touched a site the candidate read.
+// At the first such conflict the round stops, and the trial is re-evaluated
+// in the next round on the updated lattice.  Resolved swaps touch disjoint
+// sites and are written in parallel.  The result is the sequential kernel's:
+// same words, same decisions, same lattice, same counters.
+#include "halo_engine.cuh"
+#include "kernels.cuh"
+
+namespace brawl {
+
+namespace {
+
+struct SpecSlot {
+  int32_t words;    // words the trial consumes
+  int32_t accept;   // the trial's return value (1 for equal species)
+  int32_t changed;  // accepted with different species: the lattice changes
+  int32_t ax, ay, az, bx, by, bz;
+  int32_t Ya, Xa, Yb, Xb;
+  int32_t sa, sb;
+  int32_t flags;    // 1 evaluated, 2 seventh word, 4 exact tier, 8 FP64 exp, 16 double-double exp
+};
+
+struct SpecLat {
+  int sz, sy, origin, SZ, SY, off;
+  __device__ __forceinline__ int operator()(int i) const {
+    extern __shared__ int8_t s_i8[];
+    const int Z = i / sz, r = i - Z * sz, Y = r / sy, X = r - Y * sy;
+    return s_i8[off + origin + Z * SZ + Y * SY + X];
+  }
+};
+
+__device__ __noinline__ int spec_delta_general(const ChainJob* __restrict__ Jg, int ents_off, int I_off,
+                                               int F_off, SpecLat lat, int ax, int ay, int az, int ai,
+                                               int bx, int by, int bz, int bi, int sa, int sb, int lane) {
+  extern __shared__ int32_t s_i32[];
+  extern __shared__ uint32_t s_u32[];
+  const Geom g = Jg->g;
+  const bool h = lane >= 16;
+  const int cx = h ? bx : ax, cy = h ? by : ay, cz = h ? bz : az;
+  const int own = h ? bi : ai, other = h ? ai : bi;
+  const int so = h ? sb : sa, sn = h ? sa : sb;
+  const int nsp = g.ns + 1;
+  const int rowN = I_off + F_off + sn * g.nsh * nsp;
+  const int rowO = I_off + F_off + so * g.nsh * nsp;
+  int acc = 0;
+  for (int k = lane & 15; k < g.z; k += 16) {
+    int dx, dy, dz, sh;
+    unpack_entry(s_u32[ents_off / 4 + k], dx, dy, dz, sh);
+    const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
+    const int s_before = lat(ni);
+    const int s_after = ni == other ? so : (ni == own ? sn : s_before);
+    acc += s_i32[rowN + sh * nsp + s_after] - s_i32[rowO + sh * nsp + s_before];
+  }
+  return __reduce_add_sync(kFull, acc);
+}
+
+__device__ __noinline__ int spec_exact_decision(const ChainJob* __restrict__ Jg, SpecLat lat, const double* V,
+                                                const uint32_t* ents, const int16_t* sstart, int ax, int ay,
+                                                int az, int ai, int bx, int by, int bz, int bi, int sa, int sb,
+                                                int lane, uint32_t wu) {
+  const Geom g = Jg->g;
+  SitePair p;
+  p.ax = ax; p.ay = ay; p.az = az; p.ai = ai;
+  p.bx = bx; p.by = by; p.bz = bz; p.bi = bi;
+  p.sa = sa; p.sb = sb;
+  double e_un, e_sw;
+  exact_pair_energies(g, lat, V, ents, sstart, p, lane, e_un, e_sw);
+  const double delta_e = __dsub_rn(e_sw, e_un);
+  if (delta_e < 0.0) return 1;
+  DecideStats st = {0u, 0u};
+  const int acc = u_lt_exp(wu, __dmul_rn(-Jg->beta, delta_e), st);
+  return acc | 2 | (st.fp64 ? 4 : 0) | (st.cr ? 8 : 0);
+}
+
+// candidate index of (trial d, extra words m)
+__host__ __device__ constexpr int spec_slot(int d, int m) { return d * (d + 1) / 2 + m; }
+
+}  // namespace
+
+template <int NJ, int NC>
+__global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
+    metropolis_spec_kernel(const ChainJob* __restrict__ jobs) {
+  constexpr int W = NC * (NC + 1) / 2;
+  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ uint32_t s_u32[];
+  extern __shared__ int8_t s_i8[];
+  __shared__ SpecSlot slots[W];
+  __shared__ unsigned long long s_t_start;
+  const ChainJob* Jg = jobs + blockIdx.x;
+  const Geom g = Jg->g;
+  const HaloGeom H = Jg->hg;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_t_start = global_ns();
+  const HaloLayout L = halo_layout(g, H);
+  uint32_t* mt = reinterpret_cast<uint32_t*>(smem + L.mt);
+  uint32_t* tbuf = reinterpret_cast<uint32_t*>(smem + L.tbuf);
+  double* V = reinterpret_cast<double*>(smem + L.V);
+  uint32_t* ents = reinterpret_cast<uint32_t*>(smem + L.ents);
+  int16_t* sstart = reinterpret_cast<int16_t*>(smem + L.sstart);
+  int32_t* I = reinterpret_cast<int32_t*>(smem + L.I);
+  int8_t* lat = reinterpret_cast<int8_t*>(smem + L.lat);
+
+  // ---- stage state ------------------------------------------------------
+  const int nsp = g.ns + 1;
+  const int nI = nsp * nsp * g.nsh * (1 + nsp), nV = g.ns * g.ns * g.nsh;
+  const uint32_t* rng = Jg->rng;
+  for (int i = tid; i < kMTN; i += 32 * W) mt[i] = rng[i];
+  for (int i = tid; i < nI; i += 32 * W) I[i] = Jg->F[i];
+  for (int i = tid; i < nV; i += 32 * W) V[i] = Jg->V[i];
+  for (int i = tid; i < g.z; i += 32 * W) ents[i] = Jg->entries[i];
+  for (int i = tid; i <= g.nsh; i += 32 * W) sstart[i] = Jg->shell_start[i];
+  halo_fill(g, H, Jg->lat, lat, tid, 32 * W);
+  __syncthreads();
+  Ring R;
+  if (warp == 0) {
+    ring_init(mt, tbuf, (int)rng[kMTN], lane, R);
+  } else {
+    R.idx = (int)rng[kMTN];
+    R.avail = kMTN - R.idx;
+    R.next_half = 1;
+  }
+  HaloPlan<NJ> P;
+  make_halo_plan<NJ>(g, H, ents, lane, P);
+  __syncthreads();
+
+  const int lat_off = (int)L.lat;
+  const int tb = (int)(L.tbuf / 4);
+  const int I_off = (int)(L.I / 4);
+  const int D_abs = I_off + L.D_off;
+  const SpecLat hl = {g.sz, g.sy, H.origin, H.SZ, H.SY, lat_off};
+  const bool bcc = g.lattice == kBcc;
+  const int ys = g.ys;
+  const int nbr_swap = Jg->nbr_swap;
+  const int band = Jg->band;
+  const float bql2 = Jg->beta_q_l2, bband = Jg->beta_band;
+  const int64_t n_trials = Jg->n_trials;
+  const int n_peek = nbr_swap ? 5 : 7;
+  const int n_base = nbr_swap ? 4 : 6;
+  // this warp's candidate (d, m)
+  int my_d = 0, my_m = 0;
+#pragma unroll
+  for (int d = 0; d < NC; ++d)
+#pragma unroll
+    for (int m = 0; m <= d; ++m)
+      if (spec_slot(d, m) == warp) {
+        my_d = d;
+        my_m = m;
+      }
+  unsigned long long c_eval = 0, c_draws = 0, c_acc = 0, c_exp = 0, c_exact = 0;
+  unsigned int c_fp64 = 0, c_cr = 0;
+
+  int64_t t = 0;
+  while (t < n_trials) {
+    const int nd = (int)min((int64_t)NC, n_trials - t);
+    const int need = n_base * (nd - 1) + (nd - 1) + n_peek;
+    if (R.avail < need) {
+      if (warp == 0) ring_generate(mt, tbuf, R.next_half, lane);
+      R.avail += kMTN;
+      R.next_half ^= 1;
+      __syncthreads();
+    }
+    // ---- evaluate this warp's candidate on the round's lattice -----------
+    if (my_d < nd) {
+      const int wb = tb + R.idx + n_base * my_d + my_m;
+      SitePair p;
+      draw_site(g, s_u32[wb], s_u32[wb + 1], s_u32[wb + 2], p.ax, p.ay, p.az);
+      if (nbr_swap) draw_nbr(g, s_u32[wb + 3], p.ax, p.ay, p.az, p.bx, p.by, p.bz);
+      else draw_site(g, s_u32[wb + 3], s_u32[wb + 4], s_u32[wb + 5], p.bx, p.by, p.bz);
+      const int Ya = p.ay >> ys, Xa = p.ax >> 1, Yb = p.by >> ys, Xb = p.bx >> 1;
+      const int pa = H.origin + p.az * H.SZ + Ya * H.SY + Xa;
+      const int pb = H.origin + p.bz * H.SZ + Yb * H.SY + Xb;
+      p.sa = s_i8[lat_off + pa];
+      p.sb = s_i8[lat_off + pb];
+      int words = n_base, accept = 1, flags = 0;
+      if (p.sa != p.sb) {
+        flags = 1;
+        const bool near = pair_near(g, H, p.ax, p.ay, p.az, p.bx, p.by, p.bz);
+        p.ai = p.az * g.sz + Ya * g.sy + Xa;
+        p.bi = p.bz * g.sz + Yb * g.sy + Xb;
+        int dE;
+        if (!near) {
+          const bool par_a = bcc ? (p.az & 1) : (p.ax & 1);
+          const bool par_b = bcc ? (p.bz & 1) : (p.bx & 1);
+          dE = halo_delta<NJ>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
+        } else {
+          dE = spec_delta_general(Jg, (int)L.ents, I_off, L.F_off, hl, p.ax, p.ay, p.az, p.ai, p.bx, p.by,
+                                  p.bz, p.bi, p.sa, p.sb, lane);
+        }
+        const uint32_t wu = s_u32[wb + n_base];
+        accept = -1;
+        if (dE < -band) {
+          accept = 1;
+        } else if (dE > band) {
+          words = n_base + 1;
+          accept = fast_exp2_decision(bql2, bband, dE, wu);
+        }
+        if (accept < 0) {
+          flags |= 4;
+          const int r = spec_exact_decision(Jg, hl, V, ents, sstart, p.ax, p.ay, p.az, p.ai, p.bx, p.by,
+                                            p.bz, p.bi, p.sa, p.sb, lane, wu);
+          accept = r & 1;
+          words = (r & 2) ? n_base + 1 : n_base;
+          flags |= (r & 4) ? 8 : 0;
+          flags |= (r & 8) ? 16 : 0;
+        }
+        if (words > n_base) flags |= 2;
+      }
+      if (lane == 0) {
+        SpecSlot& S = slots[warp];
+        S.words = words;
+        S.accept = accept;
+        S.changed = accept && p.sa != p.sb;
+        S.ax = p.ax; S.ay = p.ay; S.az = p.az;
+        S.bx = p.bx; S.by = p.by; S.bz = p.bz;
+        S.Ya = Ya; S.Xa = Xa; S.Yb = Yb; S.Xb = Xb;
+        S.sa = p.sa; S.sb = p.sb;
+        S.flags = flags;
+      }
+    }
+    __syncthreads();
+    // ---- resolve in order (every thread, same result) ----------------------
+    int done = 0, m = 0, words = 0;
+    int chosen[NC];
+#pragma unroll
+    for (int d = 0; d < NC; ++d) chosen[d] = -1;
+#pragma unroll
+    for (int d = 0; d < NC; ++d) {
+      if (d >= nd || done < d) break;
+      const int k = spec_slot(d, m);
+      const SpecSlot& S = slots[k];
+      bool conflict = false;
+#pragma unroll
+      for (int e = 0; e < d; ++e) {
+        const SpecSlot& Q = slots[chosen[e]];
+        if (Q.changed)
+          conflict = conflict || pair_near(g, H, Q.ax, Q.ay, Q.az, S.ax, S.ay, S.az) ||
+                     pair_near(g, H, Q.ax, Q.ay, Q.az, S.bx, S.by, S.bz) ||
+                     pair_near(g, H, Q.bx, Q.by, Q.bz, S.ax, S.ay, S.az) ||
+                     pair_near(g, H, Q.bx, Q.by, Q.bz, S.bx, S.by, S.bz);
+      }
+      if (conflict) break;
+      chosen[d] = k;
+      done = d + 1;
+      words += S.words;
+      m += S.words - n_base;
+      const int f = S.flags;
+      c_eval += f & 1;
+      c_exp += (f >> 1) & 1;
+      c_exact += (f >> 2) & 1;
+      c_fp64 += (f >> 3) & 1;
+      c_cr += (f >> 4) & 1;
+      c_acc += S.accept;
+      c_draws += S.words;
+    }
+    // ---- write the resolved swaps (disjoint sites), one warp each ----------
+    if (warp < done) {
+      const SpecSlot& S = slots[chosen[warp]];
+      if (S.changed) halo_write_pair(H, lat, lane, S.az, S.Ya, S.Xa, S.sb, S.bz, S.Yb, S.Xb, S.sa);
+    }
+    __syncthreads();
+    ring_consume(R, words);
+    t += done;
+  }
+
+  // ---- write back ---------------------------------------------------------
+  halo_store(g, H, lat, Jg->lat, tid, 32 * W);
+  if (warp == 0) ring_writeback(mt, tbuf, R, Jg->rng, lane);
+  if (tid == 0) {
+    unsigned long long* c = Jg->counters;
+    c[kCntTrials] += (unsigned long long)n_trials;
+    c[kCntEvaluated] += c_eval;
+    c[kCntDraws] += c_draws;
+    c[kCntAccepted] += c_acc;
+    c[kCntExpTests] += c_exp;
+    c[kCntExactPath] += c_exact;
+    c[kCntExpFp64] += c_fp64;
+    c[kCntExpCr] += c_cr;
+    if (Jg->t_ns) *Jg->t_ns = global_ns() - s_t_start;
+  }
+}
+
+uint32_t spec_static_smem(int nc) { return (uint32_t)(nc * (nc + 1) / 2) * sizeof(SpecSlot) + 64; }
+
+template <int NJ, int NC>
+static void launch_spec(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, cudaStream_t stream) {
+  cudaFuncSetAttribute(metropolis_spec_kernel<NJ, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_bytes);
+  BRAWL_CARVEOUT(metropolis_spec_kernel<NJ, NC>);
+  metropolis_spec_kernel<NJ, NC><<<n_jobs, 32 * (NC * (NC + 1) / 2), smem_bytes, stream>>>(d_jobs);
+}
+
+template <int NC>
+static void launch_spec_nc(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z,
+                           cudaStream_t stream) {
+  switch (lane_entries_for(max_z)) {
+    case 2: launch_spec<2, NC>(d_jobs, n_jobs, smem_bytes, stream); break;
+    case 4: launch_spec<4, NC>(d_jobs, n_jobs, smem_bytes, stream); break;
+    case 6: launch_spec<6, NC>(d_jobs, n_jobs, smem_bytes, stream); break;
+    case 8: launch_spec<8, NC>(d_jobs, n_jobs, smem_bytes, stream); break;
+    default: launch_spec<11, NC>(d_jobs, n_jobs, smem_bytes, stream); break;
+  }
+}
+
+void launch_halo_chains(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z, int nc,
+                        int max_optin, cudaStream_t stream) {
+  if (nc >= 2 && smem_bytes + spec_static_smem(nc) <= (uint32_t)max_optin)
+    launch_metropolis_spec(d_jobs, n_jobs, smem_bytes, max_z, nc, stream);
+  else
+    launch_metropolis_halo(d_jobs, n_jobs, smem_bytes, max_z, stream);
+}
+
+void launch_metropolis_spec(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z, int nc,
+                            cudaStream_t stream) {
+  if (n_jobs <= 0) return;
+  switch (nc) {
+    case 2: launch_spec_nc<2>(d_jobs, n_jobs, smem_bytes, max_z, stream); break;
+    case 3: launch_spec_nc<3>(d_jobs, n_jobs, smem_bytes, max_z, stream); break;
+    default: launch_spec_nc<4>(d_jobs, n_jobs, smem_bytes, max_z, stream); break;
+  }
+}
+
+}  // namespace brawl

@@ -615,7 +615,7 @@ int launch_anneal(brawl_server* S, Pipe& P) {
   const int n = (int)staged.size();
   SV_TRY(grow(P.d_chain, P.chain_cap, (size_t)n, P.s));
   SV_TRY(stage_copy(P, P.d_chain, staged.data(), n * sizeof(ChainJob)));
-  if (nh > 0) launch_metropolis_halo(P.d_chain, nh, halo_smem, halo_z, P.s);
+  if (nh > 0) launch_halo_chains(P.d_chain, nh, halo_smem, halo_z, kDefaultSpeculation, S->max_optin, P.s);
   if (n - nh > 0) {
     const bool smem_lat = lat_smem <= (uint32_t)S->max_optin;
     launch_metropolis(P.d_chain + nh, n - nh, smem_lat, use_D, smem_lat ? lat_smem : glob_smem, table_z, P.s);

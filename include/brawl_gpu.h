@@ -167,6 +167,9 @@ int brawl_batch_destroy(brawl_batch *batch);
 int brawl_batch_size(brawl_batch *batch, int *n_chains);
 /* New inverse temperatures, one per chain. */
 int brawl_batch_set_beta(brawl_batch *batch, const double *beta);
+/* Trials per speculative round of the fcc/bcc Metropolis kernel (1-4, 1 =
+ * one trial at a time, the default).  Speed only: the trajectory is the same. */
+int brawl_batch_set_speculation(brawl_batch *batch, int trials_per_round);
 /* n_trials[c] Metropolis trials on every chain c, all chains in one launch.
  * accepted (may be NULL) receives each chain's accept sum for this call. */
 int brawl_batch_metropolis_run(brawl_batch *batch, const int64_t *n_trials, int64_t *accepted);

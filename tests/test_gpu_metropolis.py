@@ -130,6 +130,47 @@ def test_metropolis_matches_oracle(system):
     assert ch.total_energy() == mod.total_energy(cfg)
 
 
+SPEC_SYSTEMS = [s for s in SYSTEMS if s[0] != "simple_cubic"]
+
+
+@pytest.mark.parametrize("nc", [1, 2, 3, 4])
+def test_speculative_rounds_match_oracle(nc):
+    """Every fcc/bcc system (tiny lattices where most candidates conflict,
+    nbr_swap, near-zero temperature, many species) in one batch, run with nc
+    trials per speculative round, in uneven chunks: the oracle's trajectory,
+    counters and streams, bit for bit."""
+    chains, expect = [], []
+    for system in SPEC_SYSTEMS:
+        lattice, n, ns, nsh, T, trials, nbr = system
+        rng = np.random.default_rng(zlib.crc32(repr(system).encode()))
+        V = random_V(rng, ns, nsh)
+        setup = B.Setup(lattice, *n, ns, nsh)
+        nums = equi_numbers(setup.n_atoms, ns)
+        seed = int(rng.integers(1, 2**31))
+        mod, cfg, r, acc, c, beta = _oracle_run(lattice, n, V, seed, T, trials, nbr, conc_vector(ns), nums)
+        chains.append(dict(setup=setup, V=V, seed=seed, beta=beta, nbr_swap=nbr,
+                           species_concentrations=conc_vector(ns), species_numbers=nums))
+        expect.append((trials, cfg, acc, c, r, mod))
+    b = B.Batch(chains)
+    b.set_speculation(nc)
+    trials = np.array([e[0] for e in expect])
+    acc = np.zeros(len(chains), dtype=np.int64)
+    for frac in (3, 7):
+        acc += b.metropolis(trials // frac)
+    acc += b.metropolis(trials - trials // 3 - trials // 7)
+    cnt = b.counters()
+    names = B.COUNTER_NAMES
+    for k, (t, cfg, a, c, r, mod) in enumerate(expect):
+        assert acc[k] == a, SPEC_SYSTEMS[k]
+        assert np.array_equal(b.config(k), cfg), SPEC_SYSTEMS[k]
+        row = dict(zip(names, cnt[k]))
+        assert row["evaluated"] == c.evaluated and row["exp_tests"] == c.exp_tests
+        # the streams continue identically
+        g = O.OracleRng(1)
+        g.set_state_words(b.rng_state(k))
+        assert [g.uniform() for _ in range(700)] == [r.uniform() for _ in range(700)]
+
+
 def test_all_moves_on_the_exact_tier():
     """With every V equal, every swap's dE is exactly zero: each evaluated
     trial needs the FP64 reference-order sums (dE == 0 draws, exp(-0) = 1)."""
