@@ -230,7 +230,13 @@ def serving_leg(args) -> dict:
             if dt > 0:
                 time.sleep(dt)
             ids.append(srv.submit(job))
-        res = [srv.wait(i) for i in ids]
+        res = []
+        for i in ids:
+            try:
+                res.append(srv.wait(i, timeout=900.0))
+            except Exception as e:   # a job that did not end in time counts as failed
+                res.append({"status": getattr(e, "code", -1), "t_submit": 0.0, "t_admit": 0.0,
+                            "t_finish": 0.0, "trials": 0})
         makespan = time.perf_counter() - t0
         stats = srv.stats()
     ok = [r for r in res if r["status"] == 0]

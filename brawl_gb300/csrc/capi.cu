@@ -424,11 +424,43 @@ int set_chain_config(brawl_batch* b, int c, const int8_t* config) {
   return BRAWL_OK;
 }
 
+int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, bool serial,
+                        cudaStream_t stream, bool wait);
+
+// Kernel launches run fewer than 2^31 trials per chain (their tallies are
+// 32-bit); longer runs are split into consecutive launches, which continue
+// every chain exactly where the previous one stopped.
+constexpr int64_t kMaxLaunchTrials = ((int64_t)1 << 31) - 1;
+
 int run_metropolis(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, bool serial,
                    cudaStream_t stream, bool wait) {
   const int n = (int)b->jobs.size();
+  int64_t most = 0;
   for (int c = 0; c < n; ++c) {
     if (n_trials[c] < 0) return fail(BRAWL_EINVAL, "n_trials < 0");
+    most = std::max(most, n_trials[c]);
+  }
+  if (most <= kMaxLaunchTrials) return run_metropolis_once(b, n_trials, accepted, serial, stream, wait);
+  std::vector<int64_t> left(n_trials, n_trials + n), part(n), acc(n, 0), acc_part(n);
+  while (true) {
+    bool any = false;
+    for (int c = 0; c < n; ++c) {
+      part[c] = std::min(left[c], kMaxLaunchTrials);
+      left[c] -= part[c];
+      any = any || part[c] > 0;
+    }
+    if (!any) break;
+    TRY(run_metropolis_once(b, part.data(), acc_part.data(), serial, stream, true));
+    for (int c = 0; c < n; ++c) acc[c] += acc_part[c];
+  }
+  if (accepted) std::copy(acc.begin(), acc.end(), accepted);
+  return BRAWL_OK;
+}
+
+int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, bool serial,
+                        cudaStream_t stream, bool wait) {
+  const int n = (int)b->jobs.size();
+  for (int c = 0; c < n; ++c) {
     b->jobs[c].n_trials = n_trials[c];
     b->jobs[c].nbr_swap = b->nbr_swap[c];
   }

@@ -118,10 +118,14 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   const int64_t n_trials = Jg->n_trials;
   const int n_peek = nbr_swap ? 5 : 7;
   const int n_base = nbr_swap ? 4 : 6;
-  unsigned long long c_eval = 0, c_draws = 0, c_acc = 0, c_exp = 0, c_exact = 0;
-  unsigned int c_fp64 = 0, c_cr = 0, c_near = 0;
+  // 32-bit tallies (a launch runs fewer than 2^31 trials per chain, see
+  // launch_metropolis_halo); the words drawn follow from them: n_base per
+  // trial plus the uniforms
+  unsigned int b_eval = 0, b_acc = 0, b_exp = 0, b_exact = 0;
+  unsigned int c_fp64 = 0, c_cr = 0;
+  const int nt = (int)n_trials;
 
-  for (int64_t t = 0; t < n_trials; ++t) {
+  for (int t = 0; t < nt; ++t) {
     ring_ensure(mt, tbuf, R, n_peek, lane);
     const int wb = tb + R.idx;
     SitePair p;
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
     int consumed = n_base;
     int accept = 1;  // same species: accepted without an energy evaluation or a draw
     if (p.sa != p.sb) {
-      ++c_eval;
+      ++b_eval;
       const bool near = pair_near(g, H, p.ax, p.ay, p.az, p.bx, p.by, p.bz);
       p.ai = p.az * g.sz + Ya * g.sy + Xa;
       p.bi = p.bz * g.sz + Yb * g.sy + Xb;
@@ -146,7 +150,6 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
         const bool par_b = bcc ? (p.bz & 1) : (p.bx & 1);
         dE = halo_delta<NJ>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
       } else {
-        ++c_near;
         dE = halo_delta_general(Jg, (int)L.ents, I_off, L.F_off, hl, p.ax, p.ay, p.az, p.ai,
                                 p.bx, p.by, p.bz, p.bi, p.sa, p.sb, lane);
       }
@@ -159,7 +162,7 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
         accept = fast_exp2_decision(bql2, bband, dE, wu);
       }
       if (accept < 0) {
-        ++c_exact;
+        ++b_exact;
         const int r = halo_exact_decision(Jg, hl, V, ents, sstart, p.ax, p.ay, p.az, p.ai, p.bx,
                                           p.by, p.bz, p.bi, p.sa, p.sb, lane, wu);
         accept = r & 1;
@@ -167,13 +170,14 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
         c_fp64 += (r >> 2) & 1;
         c_cr += (r >> 3) & 1;
       }
-      if (consumed > n_base) ++c_exp;
+      if (consumed > n_base) ++b_exp;
       if (accept) halo_write_pair(H, lat, lane, p.az, Ya, Xa, p.sb, p.bz, Yb, Xb, p.sa);
     }
-    c_acc += accept;
-    c_draws += consumed;
+    b_acc += accept;
     ring_consume(R, consumed);
   }
+  const unsigned long long c_eval = b_eval, c_acc = b_acc, c_exp = b_exp, c_exact = b_exact;
+  const unsigned long long c_draws = (unsigned long long)n_base * (unsigned long long)n_trials + c_exp;
 
   // ---- write back ---------------------------------------------------------
   __syncwarp();

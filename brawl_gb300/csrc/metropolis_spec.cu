@@ -24,14 +24,18 @@ namespace brawl {
 
 namespace {
 
-struct SpecSlot {
-  int32_t words;    // words the trial consumes
-  int32_t accept;   // the trial's return value (1 for equal species)
-  int32_t changed;  // accepted with different species: the lattice changes
-  int32_t ax, ay, az, bx, by, bz;
-  int32_t Ya, Xa, Yb, Xb;
-  int32_t sa, sb;
-  int32_t flags;    // 1 evaluated, 2 seventh word, 4 exact tier, 8 FP64 exp, 16 double-double exp
+// One candidate's outcome.  hdr: words consumed (bits 0-3), the trial's
+// return value (bit 4), the lattice changes (bit 5), counters (bits 8-12:
+// evaluated, seventh word, exact tier, FP64 exp, double-double exp).
+// mask: bit k set when earlier candidate k has a site within interaction
+// range of one of this candidate's sites.  wr: the halo writes of an
+// accepted swap, one per lane of the first half warp (padded index |
+// species << 24, or -1).
+struct __align__(16) SpecSlot {
+  int32_t hdr;
+  uint32_t mask;
+  int32_t pad[2];
+  int32_t wr[16];
 };
 
 struct SpecLat {
@@ -175,11 +179,39 @@ __global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
     }
     // ---- evaluate this warp's candidate on the round's lattice -----------
     if (my_d < nd) {
-      const int wb = tb + R.idx + n_base * my_d + my_m;
+      const int w0 = tb + R.idx;
+      const int wb = w0 + n_base * my_d + my_m;
       SitePair p;
       draw_site(g, s_u32[wb], s_u32[wb + 1], s_u32[wb + 2], p.ax, p.ay, p.az);
       if (nbr_swap) draw_nbr(g, s_u32[wb + 3], p.ax, p.ay, p.az, p.bx, p.by, p.bz);
       else draw_site(g, s_u32[wb + 3], s_u32[wb + 4], s_u32[wb + 5], p.bx, p.by, p.bz);
+      // which earlier candidates (their sites need only the words) lie
+      // within range: lane 4q + c tests site (c >> 1) of candidate q against
+      // this candidate's site (c & 1)
+      uint32_t mask = 0;
+      if (my_d > 0) {
+        const int nq = spec_slot(my_d, 0);
+        const int q = lane >> 2, c = lane & 3;
+        bool near_q = false;
+        if (q < nq) {
+          int e = 0;
+#pragma unroll
+          for (int d = 1; d < NC; ++d) e += (q >= spec_slot(d, 0)) ? 1 : 0;
+          const int qw = w0 + n_base * e + (q - spec_slot(e, 0));
+          int qx, qy, qz;
+          draw_site(g, s_u32[qw], s_u32[qw + 1], s_u32[qw + 2], qx, qy, qz);
+          if (c & 2) {
+            if (nbr_swap) draw_nbr(g, s_u32[qw + 3], qx, qy, qz, qx, qy, qz);
+            else draw_site(g, s_u32[qw + 3], s_u32[qw + 4], s_u32[qw + 5], qx, qy, qz);
+          }
+          near_q = (c & 1) ? pair_near(g, H, qx, qy, qz, p.bx, p.by, p.bz)
+                           : pair_near(g, H, qx, qy, qz, p.ax, p.ay, p.az);
+        }
+        const uint32_t bal = __ballot_sync(kFull, near_q);
+#pragma unroll
+        for (int qq = 0; qq < NC * (NC - 1) / 2; ++qq)
+          if ((bal >> (4 * qq)) & 0xFu) mask |= 1u << qq;
+      }
       const int Ya = p.ay >> ys, Xa = p.ax >> 1, Yb = p.by >> ys, Xb = p.bx >> 1;
       const int pa = H.origin + p.az * H.SZ + Ya * H.SY + Xa;
       const int pb = H.origin + p.bz * H.SZ + Yb * H.SY + Xb;
@@ -219,57 +251,77 @@ __global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
         }
         if (words > n_base) flags |= 2;
       }
+      const bool changed = accept && p.sa != p.sb;
+      SpecSlot& S = slots[warp];
       if (lane == 0) {
-        SpecSlot& S = slots[warp];
-        S.words = words;
-        S.accept = accept;
-        S.changed = accept && p.sa != p.sb;
-        S.ax = p.ax; S.ay = p.ay; S.az = p.az;
-        S.bx = p.bx; S.by = p.by; S.bz = p.bz;
-        S.Ya = Ya; S.Xa = Xa; S.Yb = Yb; S.Xb = Xb;
-        S.sa = p.sa; S.sb = p.sb;
-        S.flags = flags;
+        S.hdr = words | (accept << 4) | ((changed ? 1 : 0) << 5) | (flags << 8);
+        S.mask = mask;
+      }
+      if (changed && lane < 16) {
+        // the halo writes of the swap: lanes 8k..8k+7 take site k through
+        // the 8 combinations of images per axis
+        const bool b = lane >= 8;
+        const int combo = lane & 7;
+        int Z = b ? p.bz : p.az, Y = b ? Yb : Ya, X = b ? Xb : Xa;
+        const int sp = b ? p.sa : p.sb;
+        bool ok = true;
+        if (combo & 1) {
+          if (X < H.hx) X += H.NX;
+          else if (X >= H.NX - H.hx) X -= H.NX;
+          else ok = false;
+        }
+        if (combo & 2) {
+          if (Y < H.hy) Y += H.NY;
+          else if (Y >= H.NY - H.hy) Y -= H.NY;
+          else ok = false;
+        }
+        if (combo & 4) {
+          if (Z < H.hz) Z += H.NZ;
+          else if (Z >= H.NZ - H.hz) Z -= H.NZ;
+          else ok = false;
+        }
+        S.wr[lane] = ok ? (halo_index(H, Z, Y, X) | (sp << 24)) : -1;
       }
     }
     __syncthreads();
     // ---- resolve in order (every thread, same result) ----------------------
     int done = 0, m = 0, words = 0;
-    int chosen[NC];
-#pragma unroll
-    for (int d = 0; d < NC; ++d) chosen[d] = -1;
+    uint32_t changed_bits = 0;
+    int k_sel[NC];
+    bool go = true;
 #pragma unroll
     for (int d = 0; d < NC; ++d) {
-      if (d >= nd || done < d) break;
-      const int k = spec_slot(d, m);
-      const SpecSlot& S = slots[k];
-      bool conflict = false;
-#pragma unroll
-      for (int e = 0; e < d; ++e) {
-        const SpecSlot& Q = slots[chosen[e]];
-        if (Q.changed)
-          conflict = conflict || pair_near(g, H, Q.ax, Q.ay, Q.az, S.ax, S.ay, S.az) ||
-                     pair_near(g, H, Q.ax, Q.ay, Q.az, S.bx, S.by, S.bz) ||
-                     pair_near(g, H, Q.bx, Q.by, Q.bz, S.ax, S.ay, S.az) ||
-                     pair_near(g, H, Q.bx, Q.by, Q.bz, S.bx, S.by, S.bz);
+      k_sel[d] = -1;
+      if (go && d < nd) {
+        const int k = spec_slot(d, m);
+        const int hdr = slots[k].hdr;
+        const uint32_t mask = slots[k].mask;
+        if (mask & changed_bits) {
+          go = false;
+        } else {
+          k_sel[d] = k;
+          done = d + 1;
+          const int w = hdr & 15;
+          words += w;
+          m += w - n_base;
+          if ((hdr >> 5) & 1) changed_bits |= 1u << k;
+          c_acc += (hdr >> 4) & 1;
+          c_eval += (hdr >> 8) & 1;
+          c_exp += (hdr >> 9) & 1;
+          c_exact += (hdr >> 10) & 1;
+          c_fp64 += (hdr >> 11) & 1;
+          c_cr += (hdr >> 12) & 1;
+          c_draws += w;
+        }
       }
-      if (conflict) break;
-      chosen[d] = k;
-      done = d + 1;
-      words += S.words;
-      m += S.words - n_base;
-      const int f = S.flags;
-      c_eval += f & 1;
-      c_exp += (f >> 1) & 1;
-      c_exact += (f >> 2) & 1;
-      c_fp64 += (f >> 3) & 1;
-      c_cr += (f >> 4) & 1;
-      c_acc += S.accept;
-      c_draws += S.words;
     }
     // ---- write the resolved swaps (disjoint sites), one warp each ----------
-    if (warp < done) {
-      const SpecSlot& S = slots[chosen[warp]];
-      if (S.changed) halo_write_pair(H, lat, lane, S.az, S.Ya, S.Xa, S.sb, S.bz, S.Yb, S.Xb, S.sa);
+    int kw = -1;
+#pragma unroll
+    for (int d = 0; d < NC; ++d) kw = warp == d ? k_sel[d] : kw;
+    if (kw >= 0 && lane < 16 && ((slots[kw].hdr >> 5) & 1)) {
+      const int v = slots[kw].wr[lane];
+      if (v >= 0) lat[v & 0xFFFFFF] = (int8_t)(v >> 24);
     }
     __syncthreads();
     ring_consume(R, words);

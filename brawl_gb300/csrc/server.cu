@@ -61,7 +61,7 @@ enum { kAnneal = 0, kWl = 1, kNs = 2, kKinds = 3 };
 // threads building admitted jobs' device objects and reading back ended
 // ones (a nested-sampling run's walker initialisation is one warp's
 // sequential work, so several run at once)
-constexpr int kWorkers = 8;
+constexpr int kWorkers = 16;
 // initial capacity of the pinned buffers: growing one (a pinned allocation)
 // waits for the whole device, so it should be rare
 constexpr size_t kPinnedEntries = 4096;
@@ -331,6 +331,7 @@ int64_t next_quantum(double t_round, const Job& j, int64_t left, int64_t first_q
     q = t > 4.0e18 ? (int64_t)4e18 : (int64_t)t;
   }
   q = std::max<int64_t>(q, 1);
+  q = std::min<int64_t>(q, (int64_t)1 << 30);  // a launch's per-chain tallies are 32-bit
   if (cap > 0) q = std::min(q, cap);
   return std::min(q, left);
 }
@@ -1034,8 +1035,14 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
   brawl_server* S = new brawl_server();
   std::memset(&S->o, 0, sizeof(S->o));
   if (opts) S->o = *opts;
-  if (S->o.hbm_budget == 0) S->o.hbm_budget = (size_t)4 << 30;
-  if (S->o.max_active <= 0) S->o.max_active = 608;
+  cudaGetDevice(&S->device);
+  if (S->o.hbm_budget == 0) {
+    // 60% of the device memory free now
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    S->o.hbm_budget = free_b / 10 * 6;
+  }
+  if (S->o.max_active <= 0) S->o.max_active = 4096;
   if (!(S->o.round_ms > 0.0)) S->o.round_ms = 20.0;
   if (S->o.max_trials < 0) S->o.max_trials = 0;
   if (S->o.max_iterations < 0) S->o.max_iterations = 0;

@@ -301,8 +301,9 @@ int brawl_wl_counters(brawl_wl *wl, int walker, int64_t *counters);
 typedef struct brawl_server brawl_server;
 
 typedef struct brawl_server_opts {
-    size_t hbm_budget;          /* device bytes for resident jobs (0: 4 GiB) */
-    int max_active;             /* resident jobs at most (0: 608) */
+    size_t hbm_budget;          /* device bytes for resident jobs (0: 60% of the
+                                   memory free at creation) */
+    int max_active;             /* resident jobs at most (0: 4096) */
     double round_ms;            /* device time each job's quantum of work aims at,
                                    from the job's measured cost (0: 20 ms) */
     int64_t max_trials;         /* cap on a job's Metropolis / Wang-Landau trials
