@@ -1488,6 +1488,7 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
     WlWalker& W = wl->w[c];
     std::memset(&W, 0, sizeof(W));
     W.job = wl->b->jobs[c];
+    W.S = wl->b->models[c].S;
     W.lng = wl->d_lng + (size_t)c * bins;
     W.hist = wl->d_hist + hoff;
     W.start = walkers[c].start_idx;
@@ -1522,7 +1523,7 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
 
 extern "C" int brawl_wl_sweeps(brawl_wl* wl, int64_t n_trials, double wl_f, int hist_period,
                                int64_t* accepted) {
-  if (!wl || n_trials < 0) return fail(BRAWL_EINVAL, "bad argument");
+  if (!wl || n_trials < 0 || n_trials > 0x7fffffff) return fail(BRAWL_EINVAL, "n_trials must be 0 .. 2^31-1");
   brawl_batch* b = wl->b;
   const int n = (int)wl->w.size();
   TRY(queue_batch_energy(b));

@@ -71,6 +71,7 @@ enum Status : int {
   kStatusRngInvariant = 1,   // stream position left its block (internal error)
   kStatusBadSpecies = 2,     // a species code outside 1..ns was met
   kStatusWalkerOutsideWindow = 3,  // a Wang-Landau walker's energy left its window
+  kStatusBandViolated = 4,   // an exact value fell outside its fixed-point bound (internal error)
 };
 
 struct Geom {
@@ -512,6 +513,100 @@ __device__ inline void exact_pair_energies(const Geom& g, const Lat& lat, const 
   }
   e_un = __dadd_rn(e[0], e[1]);
   e_sw = __dadd_rn(e[2], e[3]);
+}
+
+// The same sums with the terms staged first: every (evaluation, neighbour)
+// term V(species, neighbour species, shell) is looked up in parallel into
+// vbuf (4 * z doubles of shared memory), then each (evaluation, shell) chain
+// adds its terms in list order from 0.0, so the chain of dependent FP64 adds
+// is the only latency left.  Same values, same order: identical results.
+template <class Lat>
+__device__ inline void exact_pair_energies_staged(const Geom& g, const Lat& lat, const double* V,
+                                                  const uint32_t* ents, const int16_t* sstart,
+                                                  const SitePair& p, int lane, double& e_un,
+                                                  double& e_sw, double* vbuf) {
+  const int z = g.z, nsh = g.nsh, ns = g.ns;
+#pragma unroll 1
+  for (int ev = 0; ev < 4; ++ev) {
+    const bool on2 = ev & 1, after = ev >= 2;
+    const int cx = on2 ? p.bx : p.ax, cy = on2 ? p.by : p.ay, cz = on2 ? p.bz : p.az;
+    const int own = on2 ? p.bi : p.ai, other = on2 ? p.ai : p.bi;
+    const int s_own_before = on2 ? p.sb : p.sa;
+    const int s_own_after = on2 ? p.sa : p.sb;
+    const int cs = after ? s_own_after : s_own_before;
+    for (int k = lane; k < z; k += 32) {
+      int dx, dy, dz, sh;
+      unpack_entry(ents[k], dx, dy, dz, sh);
+      const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
+      int s = lat(ni);
+      if (after) {
+        if (ni == other) s = s_own_before;        // the partner now holds our old species
+        else if (ni == own) s = s_own_after;
+      }
+      vbuf[ev * z + k] = V[(cs - 1) + ns * ((s - 1) + ns * sh)];
+    }
+  }
+  __syncwarp();
+  const int nc = 4 * nsh;
+  double part[2] = {0.0, 0.0};
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int c = lane + 32 * r;
+    if (c < nc) {
+      const int ev = c / nsh, sh = c - ev * nsh;
+      const double* t = vbuf + ev * z + sstart[sh];
+      const int len = sstart[sh + 1] - sstart[sh];
+      double sum = 0.0;
+      // four terms loaded ahead of their adds, so the loads of the next
+      // group overlap the dependent adds of this one
+      int k = 0;
+      for (; k + 4 <= len; k += 4) {
+        const double v0 = t[k], v1 = t[k + 1], v2 = t[k + 2], v3 = t[k + 3];
+        sum = __dadd_rn(sum, v0);
+        sum = __dadd_rn(sum, v1);
+        sum = __dadd_rn(sum, v2);
+        sum = __dadd_rn(sum, v3);
+      }
+      for (; k < len; ++k) sum = __dadd_rn(sum, t[k]);
+      part[r] = sum;
+    }
+  }
+  double e[4];
+#pragma unroll
+  for (int ev = 0; ev < 4; ++ev) {
+    double acc = 0.0;
+    for (int sh = 0; sh < nsh; ++sh) {
+      const int c = ev * nsh + sh;
+      double v = c < 32 ? __shfl_sync(kFull, part[0], c) : __shfl_sync(kFull, part[1], c - 32);
+      acc = sh == 0 ? v : __dadd_rn(acc, v);
+    }
+    e[ev] = acc;
+  }
+  e_un = __dadd_rn(e[0], e[1]);
+  e_sw = __dadd_rn(e[2], e[3]);
+  __syncwarp();  // vbuf is reused by the next call
+}
+
+// Fixed-point swap delta for any pair, from canonical neighbour indices
+// (lanes 0-15 site 1, 16-31 site 2).
+__device__ __forceinline__ int compact_fixed_delta(const Geom& g, const int8_t* lat, const int32_t* F,
+                                              const uint32_t* ents, const SitePair& p, int lane) {
+  const bool h = lane >= 16;
+  const int cx = h ? p.bx : p.ax, cy = h ? p.by : p.ay, cz = h ? p.bz : p.az;
+  const int own = h ? p.bi : p.ai, other = h ? p.ai : p.bi;
+  const int so = h ? p.sb : p.sa, sn = h ? p.sa : p.sb;
+  const int nsp = g.ns + 1;
+  const int rowN = sn * g.nsh * nsp, rowO = so * g.nsh * nsp;
+  int acc = 0;
+  for (int k = lane & 15; k < g.z; k += 16) {
+    int dx, dy, dz, sh;
+    unpack_entry(ents[k], dx, dy, dz, sh);
+    const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
+    const int sb = lat[ni];
+    const int sa = ni == other ? so : (ni == own ? sn : sb);
+    acc += F[rowN + sh * nsp + sa] - F[rowO + sh * nsp + sb];
+  }
+  return __reduce_add_sync(kFull, acc);
 }
 
 // FP32 filter of u < exp(-beta*dE) for a fixed-point dE > band.

@@ -27,16 +27,24 @@ namespace {
 // One candidate's outcome.  hdr: words consumed (bits 0-3), the trial's
 // return value (bit 4), the lattice changes (bit 5), counters (bits 8-12:
 // evaluated, seventh word, exact tier, FP64 exp, double-double exp).
-// mask: bit k set when earlier candidate k has a site within interaction
-// range of one of this candidate's sites.  wr: the halo writes of an
-// accepted swap, one per lane of the first half warp (padded index |
-// species << 24, or -1).
+// xy / zz: the two sites' doubled coordinates, 16 bits each (ax | ay << 16,
+// bx | by << 16, az | bz << 16).  wr: the halo writes of an accepted swap,
+// one per lane of the first half warp (padded index | species << 24, or -1).
 struct __align__(16) SpecSlot {
   int32_t hdr;
-  uint32_t mask;
-  int32_t pad[2];
+  int32_t a_xy, b_xy, zz;
   int32_t wr[16];
 };
+
+// Whether an accepted swap at slot q touched a site that candidate s read:
+// lanes 0-3 test the four (site of q, site of s) pairs, the warp votes.
+__device__ __forceinline__ bool spec_conflict(const Geom& g, const HaloGeom& H, int4 q, int4 s, int lane) {
+  const int c = lane & 3;
+  const int qxy = (c & 2) ? q.z : q.y, sxy = (c & 1) ? s.z : s.y;
+  const int qz = (c & 2) ? (q.w >> 16) : (q.w & 0xffff), sz = (c & 1) ? (s.w >> 16) : (s.w & 0xffff);
+  const bool near = pair_near(g, H, qxy & 0xffff, qxy >> 16, qz, sxy & 0xffff, sxy >> 16, sz);
+  return __ballot_sync(kFull, near && lane < 4) != 0u;
+}
 
 struct SpecLat {
   int sz, sy, origin, SZ, SY, off;
@@ -164,12 +172,14 @@ __global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
         my_d = d;
         my_m = m;
       }
-  unsigned long long c_eval = 0, c_draws = 0, c_acc = 0, c_exp = 0, c_exact = 0;
+  // 32-bit tallies (fewer than 2^31 trials per launch)
+  unsigned int b_eval = 0, b_acc = 0, b_exp = 0, b_exact = 0;
   unsigned int c_fp64 = 0, c_cr = 0;
 
-  int64_t t = 0;
-  while (t < n_trials) {
-    const int nd = (int)min((int64_t)NC, n_trials - t);
+  int t = 0;
+  const int nt = (int)n_trials;
+  while (t < nt) {
+    const int nd = min(NC, nt - t);
     const int need = n_base * (nd - 1) + (nd - 1) + n_peek;
     if (R.avail < need) {
       if (warp == 0) ring_generate(mt, tbuf, R.next_half, lane);
@@ -179,39 +189,11 @@ __global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
     }
     // ---- evaluate this warp's candidate on the round's lattice -----------
     if (my_d < nd) {
-      const int w0 = tb + R.idx;
-      const int wb = w0 + n_base * my_d + my_m;
+      const int wb = tb + R.idx + n_base * my_d + my_m;
       SitePair p;
       draw_site(g, s_u32[wb], s_u32[wb + 1], s_u32[wb + 2], p.ax, p.ay, p.az);
       if (nbr_swap) draw_nbr(g, s_u32[wb + 3], p.ax, p.ay, p.az, p.bx, p.by, p.bz);
       else draw_site(g, s_u32[wb + 3], s_u32[wb + 4], s_u32[wb + 5], p.bx, p.by, p.bz);
-      // which earlier candidates (their sites need only the words) lie
-      // within range: lane 4q + c tests site (c >> 1) of candidate q against
-      // this candidate's site (c & 1)
-      uint32_t mask = 0;
-      if (my_d > 0) {
-        const int nq = spec_slot(my_d, 0);
-        const int q = lane >> 2, c = lane & 3;
-        bool near_q = false;
-        if (q < nq) {
-          int e = 0;
-#pragma unroll
-          for (int d = 1; d < NC; ++d) e += (q >= spec_slot(d, 0)) ? 1 : 0;
-          const int qw = w0 + n_base * e + (q - spec_slot(e, 0));
-          int qx, qy, qz;
-          draw_site(g, s_u32[qw], s_u32[qw + 1], s_u32[qw + 2], qx, qy, qz);
-          if (c & 2) {
-            if (nbr_swap) draw_nbr(g, s_u32[qw + 3], qx, qy, qz, qx, qy, qz);
-            else draw_site(g, s_u32[qw + 3], s_u32[qw + 4], s_u32[qw + 5], qx, qy, qz);
-          }
-          near_q = (c & 1) ? pair_near(g, H, qx, qy, qz, p.bx, p.by, p.bz)
-                           : pair_near(g, H, qx, qy, qz, p.ax, p.ay, p.az);
-        }
-        const uint32_t bal = __ballot_sync(kFull, near_q);
-#pragma unroll
-        for (int qq = 0; qq < NC * (NC - 1) / 2; ++qq)
-          if ((bal >> (4 * qq)) & 0xFu) mask |= 1u << qq;
-      }
       const int Ya = p.ay >> ys, Xa = p.ax >> 1, Yb = p.by >> ys, Xb = p.bx >> 1;
       const int pa = H.origin + p.az * H.SZ + Ya * H.SY + Xa;
       const int pb = H.origin + p.bz * H.SZ + Yb * H.SY + Xb;
@@ -253,10 +235,9 @@ __global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
       }
       const bool changed = accept && p.sa != p.sb;
       SpecSlot& S = slots[warp];
-      if (lane == 0) {
-        S.hdr = words | (accept << 4) | ((changed ? 1 : 0) << 5) | (flags << 8);
-        S.mask = mask;
-      }
+      if (lane == 0)
+        *reinterpret_cast<int4*>(&S) = make_int4(words | (accept << 4) | ((changed ? 1 : 0) << 5) | (flags << 8),
+                                                 p.ax | (p.ay << 16), p.bx | (p.by << 16), p.az | (p.bz << 16));
       if (changed && lane < 16) {
         // the halo writes of the swap: lanes 8k..8k+7 take site k through
         // the 8 combinations of images per axis
@@ -284,42 +265,51 @@ __global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
       }
     }
     __syncthreads();
-    // ---- resolve in order (every thread, same result) ----------------------
+    // ---- resolve in order (every warp, same result) -------------------------
+    // trial d takes candidate (d, m); it stands unless an accepted swap of an
+    // earlier trial of the round is within range of one of its sites
     int done = 0, m = 0, words = 0;
-    uint32_t changed_bits = 0;
     int k_sel[NC];
+    int4 h_sel[NC];
     bool go = true;
 #pragma unroll
     for (int d = 0; d < NC; ++d) {
       k_sel[d] = -1;
+      h_sel[d] = make_int4(0, 0, 0, 0);
       if (go && d < nd) {
         const int k = spec_slot(d, m);
-        const int hdr = slots[k].hdr;
-        const uint32_t mask = slots[k].mask;
-        if (mask & changed_bits) {
+        const int4 h = *reinterpret_cast<const int4*>(&slots[k]);
+        bool conflict = false;
+#pragma unroll
+        for (int e = 0; e < d; ++e)
+          if ((h_sel[e].x >> 5) & 1) conflict = conflict || spec_conflict(g, H, h_sel[e], h, lane);
+        if (conflict) {
           go = false;
         } else {
           k_sel[d] = k;
+          h_sel[d] = h;
           done = d + 1;
-          const int w = hdr & 15;
+          const int w = h.x & 15;
           words += w;
           m += w - n_base;
-          if ((hdr >> 5) & 1) changed_bits |= 1u << k;
-          c_acc += (hdr >> 4) & 1;
-          c_eval += (hdr >> 8) & 1;
-          c_exp += (hdr >> 9) & 1;
-          c_exact += (hdr >> 10) & 1;
-          c_fp64 += (hdr >> 11) & 1;
-          c_cr += (hdr >> 12) & 1;
-          c_draws += w;
+          const int f = h.x;
+          b_acc += (f >> 4) & 1;
+          b_eval += (f >> 8) & 1;
+          b_exp += (f >> 9) & 1;
+          b_exact += (f >> 10) & 1;
+          c_fp64 += (f >> 11) & 1;
+          c_cr += (f >> 12) & 1;
         }
       }
     }
     // ---- write the resolved swaps (disjoint sites), one warp each ----------
-    int kw = -1;
+    int kw = -1, hw = 0;
 #pragma unroll
-    for (int d = 0; d < NC; ++d) kw = warp == d ? k_sel[d] : kw;
-    if (kw >= 0 && lane < 16 && ((slots[kw].hdr >> 5) & 1)) {
+    for (int d = 0; d < NC; ++d) {
+      kw = warp == d ? k_sel[d] : kw;
+      hw = warp == d ? h_sel[d].x : hw;
+    }
+    if (kw >= 0 && ((hw >> 5) & 1) && lane < 16) {
       const int v = slots[kw].wr[lane];
       if (v >= 0) lat[v & 0xFFFFFF] = (int8_t)(v >> 24);
     }
@@ -327,6 +317,9 @@ __global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
     ring_consume(R, words);
     t += done;
   }
+
+  const unsigned long long c_eval = b_eval, c_acc = b_acc, c_exp = b_exp, c_exact = b_exact;
+  const unsigned long long c_draws = (unsigned long long)n_base * (unsigned long long)n_trials + c_exp;
 
   // ---- write back ---------------------------------------------------------
   halo_store(g, H, lat, Jg->lat, tid, 32 * W);

@@ -76,27 +76,6 @@ __device__ __forceinline__ long long gap_up(double limit, double E, int S) {
   return (long long)ceil(s);
 }
 
-// Fixed-point swap delta for any pair, from canonical neighbour indices
-// (lanes 0-15 site 1, 16-31 site 2).
-__device__ __forceinline__ int ns_fixed_delta(const Geom& g, const int8_t* lat, const int32_t* F,
-                                              const uint32_t* ents, const SitePair& p, int lane) {
-  const bool h = lane >= 16;
-  const int cx = h ? p.bx : p.ax, cy = h ? p.by : p.ay, cz = h ? p.bz : p.az;
-  const int own = h ? p.bi : p.ai, other = h ? p.ai : p.bi;
-  const int so = h ? p.sb : p.sa, sn = h ? p.sa : p.sb;
-  const int nsp = g.ns + 1;
-  const int rowN = sn * g.nsh * nsp, rowO = so * g.nsh * nsp;
-  int acc = 0;
-  for (int k = lane & 15; k < g.z; k += 16) {
-    int dx, dy, dz, sh;
-    unpack_entry(ents[k], dx, dy, dz, sh);
-    const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
-    const int sb = lat[ni];
-    const int sa = ni == other ? so : (ni == own ? sn : sb);
-    acc += F[rowN + sh * nsp + sa] - F[rowO + sh * nsp + sb];
-  }
-  return __reduce_add_sync(kFull, acc);
-}
 
 __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -108,7 +87,7 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
   const int n = g.n_sites;
   const int nsp = g.ns + 1;
   const int nF = nsp * g.nsh * nsp, nV = g.ns * g.ns * g.nsh;
-  // layout: mt | tbuf | V | F | ents | sstart | lattice
+  // layout: mt | tbuf | V | F | ents | sstart | lattice | vbuf
   uint32_t* mt = reinterpret_cast<uint32_t*>(smem);
   uint32_t* tbuf = mt + kMTN;
   double* V = reinterpret_cast<double*>(smem + align_up((kMTN + kTbufWords) * 4, 16));
@@ -117,6 +96,8 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
   int16_t* sstart = reinterpret_cast<int16_t*>(ents + g.z);
   int8_t* lat = reinterpret_cast<int8_t*>(
       smem + align_up((uint32_t)((reinterpret_cast<unsigned char*>(sstart + g.nsh + 1)) - smem), 16));
+  double* vbuf = reinterpret_cast<double*>(smem + align_up((uint32_t)(lat - reinterpret_cast<int8_t*>(smem)) +
+                                                                (uint32_t)g.n_sites, 16));
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
   for (int i = lane; i < nF; i += 32) F[i] = J.F[i];
@@ -202,12 +183,12 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
       if (status != kStatusOk) break;
       c_draws += 3;
       ++c_steps;
-      const int dE = ns_fixed_delta(g, lat, F, ents, p, lane);
+      const int dE = compact_fixed_delta(g, lat, F, ents, p, lane);
       // certainly E + dE >= ceiling: rejected without the FP64 sums
       if ((long long)dE - band >= gup) continue;
       ++c_exact;
       double e_un, e_sw;
-      exact_pair_energies(g, CompactLat{lat}, V, ents, sstart, p, lane, e_un, e_sw);
+      exact_pair_energies_staged(g, CompactLat{lat}, V, ents, sstart, p, lane, e_un, e_sw, vbuf);
       const double delta_e = __dsub_rn(e_sw, e_un);
       const double e_new = __dadd_rn(E, delta_e);
       if (e_new < limit) {
@@ -250,6 +231,7 @@ uint32_t ns_smem_bytes(const Geom& g) {
   b += (uint32_t)(g.ns * g.ns * g.nsh) * 8 + nsp * (uint32_t)g.nsh * nsp * 4 + (uint32_t)g.z * 4 +
        (uint32_t)(g.nsh + 1) * 2;
   b = align_up(b, 16) + (uint32_t)g.n_sites;
+  b = align_up(b, 16) + 4u * (uint32_t)g.z * 8;  // staged exact-sum terms
   return align_up(b, 16);
 }
 

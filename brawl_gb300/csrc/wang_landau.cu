@@ -25,6 +25,35 @@ __device__ __forceinline__ int wl_bin_index(double E, double e1, double range, i
   return (int)t + 1;
 }
 
+// The same bin, without the FP64 division when it cannot matter: with
+// rf = float(bins / range), tf = float(E - e1) * rf is within
+// |t| * 1.9e-7 of the reference's t (three single roundings and two
+// double ones), so when tf -/+ that margin truncate to the same integer,
+// so does t.  Otherwise (near a bin edge, far outside, NaN) the reference
+// expression decides.
+__device__ __forceinline__ int wl_bin_index_fast(double E, double e1, double range, int bins, float rf) {
+  const double d = __dsub_rn(E, e1);
+  const float tf = __fmul_rn(__double2float_rn(d), rf);
+  const float M = fabsf(tf) * 2.5e-7f + 1.0e-30f;
+  if (fabsf(tf) < 5.0e8f) {
+    // rounded outwards, so [lo, hi] contains the exact interval
+    const float lo = truncf(__fsub_rd(tf, M)), hi = truncf(__fadd_ru(tf, M));
+    if (lo == hi) return (int)lo + 1;
+  }
+  return wl_bin_index(E, e1, range, bins);
+}
+
+// e_swapped as the reference forms it: e_unswapped - pair_unswapped +
+// pair_swapped with the pair energies summed in its order.  Out of line: it
+// runs only for accepted moves and for the rare undecided bins.
+__device__ __noinline__ double wl_exact_e_sw(const Geom& g, const int8_t* lat, const double* V, const uint32_t* ents,
+                                             const int16_t* sstart, const SitePair& p, int lane, double e_un,
+                                             double* vbuf) {
+  double p_un, p_sw;
+  exact_pair_energies_staged(g, CompactLat{lat}, V, ents, sstart, p, lane, p_un, p_sw, vbuf);
+  return __dadd_rn(__dsub_rn(e_un, p_un), p_sw);
+}
+
 __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ walkers) {
   extern __shared__ __align__(16) unsigned char smem[];
   WlWalker& W = walkers[blockIdx.x];
@@ -33,19 +62,25 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   const int lane = threadIdx.x;
   const unsigned long long t_start = global_ns();
   const int nV = g.ns * g.ns * g.nsh;
+  const int nsp = g.ns + 1;
+  const int nF = nsp * g.nsh * nsp;
   const int nb = W.end - W.start + 1;
-  // layout: mt | tbuf | V | lng slice | hist slice | ents | sstart | lattice
+  // layout: mt | tbuf | V | F | lng slice | hist slice | ents | sstart | lattice | vbuf
   uint32_t* mt = reinterpret_cast<uint32_t*>(smem);
   uint32_t* tbuf = mt + kMTN;
   double* V = reinterpret_cast<double*>(smem + align_up((kMTN + kTbufWords) * 4, 16));
-  double* lng = V + nV;
+  int32_t* F = reinterpret_cast<int32_t*>(V + nV);
+  double* lng = reinterpret_cast<double*>(F + ((nF + 1) & ~1));
   double* hist = lng + nb;
   uint32_t* ents = reinterpret_cast<uint32_t*>(hist + nb);
   int16_t* sstart = reinterpret_cast<int16_t*>(ents + g.z);
   int8_t* lat = reinterpret_cast<int8_t*>(
       smem + align_up((uint32_t)((reinterpret_cast<unsigned char*>(sstart + g.nsh + 1)) - smem), 16));
+  double* vbuf = reinterpret_cast<double*>(smem + align_up((uint32_t)(lat - reinterpret_cast<int8_t*>(smem)) +
+                                                                (uint32_t)g.n_sites, 16));
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
+  for (int i = lane; i < nF; i += 32) F[i] = J.F[i];
   for (int i = lane; i < nb; i += 32) {
     lng[i] = W.lng[W.start - 1 + i];
     hist[i] = W.hist[i];
@@ -59,16 +94,21 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
 
   const double e1 = W.e1, range = W.range, f = W.wl_f;
   const int bins = W.bins, start = W.start, end = W.end;
+  const float rf = __double2float_rn(__ddiv_rn((double)bins, range));
   const int period = W.hist_period;
+  const int band = J.band;
+  const double q = ldexp(1.0, -W.S);               // one fixed-point quantum
+  const double pair_bound = ldexp(1.0, 30 - W.S);   // >= 4 z max|V|: bounds |pair energy|
   double e_un = (W.i0 > 0 && W.e_state) ? *W.e_state : (W.e0_src ? *W.e0_src : W.e0);
   int ibin = wl_bin_index(e_un, e1, range, bins);
   int status = (ibin < start || ibin > end) ? kStatusWalkerOutsideWindow : kStatusOk;
-  unsigned long long c_eval = 0, c_draws = 0, c_exp = 0;
-  long long accepted = 0;
+  unsigned int c_eval = 0, c_exp = 0, c_exact = 0, n_acc = 0;
   DecideStats st = {0u, 0u};
+  // histogram ticks at trials i with i % period == 0
+  long long until = period > 0 ? period - (W.i0 % period) : -1;
 
-  const long long i_end = W.i0 + W.n_trials;
-  for (long long i = W.i0 + 1; i <= i_end && status == kStatusOk; ++i) {
+  const int n_tr = (int)W.n_trials;
+  for (int it = 0; it < n_tr && status == kStatusOk; ++it) {
     ring_ensure(mt, tbuf, ring, 7, lane);
     const int wb = ring.idx;
     SitePair p;
@@ -78,15 +118,32 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
     p.bi = compact_index(g, p.bx, p.by, p.bz);
     p.sa = lat[p.ai];
     p.sb = lat[p.bi];
-    double e_sw = e_un;
-    int jbin = ibin;
     const bool differ = p.sa != p.sb;
+    int jbin = ibin;
+    bool exact_done = false;
+    double e_sw = e_un;
     if (differ) {
       ++c_eval;
-      double p_un, p_sw;
-      exact_pair_energies(g, CompactLat{lat}, V, ents, sstart, p, lane, p_un, p_sw);
-      e_sw = __dadd_rn(__dsub_rn(e_un, p_un), p_sw);
-      jbin = wl_bin_index(e_sw, e1, range, bins);
+      // The reference's e_swapped lies within band quanta of e_un + dE q
+      // (pair sums) plus the two roundings of e_un - p_un + p_sw; its bin is
+      // decided without the FP64 sums when that interval sits in one bin.
+      const int dE = compact_fixed_delta(g, lat, F, ents, p, lane);
+      const double lo_d = __dmul_rn((double)(dE - band), q), hi_d = __dmul_rn((double)(dE + band), q);
+      const double w = (2.0 * fabs(e_un) + fabs(lo_d) + fabs(hi_d) + pair_bound) * 2.3e-16;
+      const double elo = __dsub_rd(__dadd_rd(e_un, lo_d), w);
+      const double ehi = __dadd_ru(__dadd_ru(e_un, hi_d), w);
+      const float tlo = __fmul_rd(__double2float_rd(__dsub_rd(elo, e1)), rf);
+      const float thi = __fmul_ru(__double2float_ru(__dsub_ru(ehi, e1)), rf);
+      const float blo = truncf(__fsub_rd(tlo, fabsf(tlo) * 2.5e-7f + 1.0e-30f));
+      const float bhi = truncf(__fadd_ru(thi, fabsf(thi) * 2.5e-7f + 1.0e-30f));
+      if (blo == bhi && fabsf(tlo) < 5.0e8f && fabsf(thi) < 5.0e8f) {
+        jbin = (int)blo + 1;
+      } else {
+        ++c_exact;
+        exact_done = true;
+        e_sw = wl_exact_e_sw(g, lat, V, ents, sstart, p, lane, e_un, vbuf);
+        jbin = wl_bin_index_fast(e_sw, e1, range, bins, rf);
+      }
     }
     int consumed = 6;
     if (jbin >= start && jbin <= end) {
@@ -95,7 +152,13 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
       const uint32_t wu = tbuf[wb + 6];
       const double d = __dsub_rn(lng[ibin - start], lng[jbin - start]);
       if (log_u_lt(wu, d, st)) {
-        ++accepted;
+        ++n_acc;
+        if (differ && !exact_done) {
+          // accepted: the walker's energy takes the reference's exact value
+          ++c_exact;
+          e_sw = wl_exact_e_sw(g, lat, V, ents, sstart, p, lane, e_un, vbuf);
+          if (wl_bin_index_fast(e_sw, e1, range, bins, rf) != jbin) status = kStatusBandViolated;
+        }
         e_un = e_sw;
         if (differ && lane == 0) {
           lat[p.ai] = (int8_t)p.sb;
@@ -108,11 +171,12 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
     } else {
       jbin = ibin;
     }
-    if (period > 0 && (i % period) == 0 && lane == 0)
-      hist[jbin - start] = __dadd_rn(hist[jbin - start], 1.0);
+    if (--until == 0) {
+      if (lane == 0) hist[jbin - start] = __dadd_rn(hist[jbin - start], 1.0);
+      until = period;
+    }
     if (lane == 0) lng[jbin - start] = __dadd_rn(lng[jbin - start], f);
     __syncwarp();
-    c_draws += consumed;
     ring_consume(ring, consumed);
   }
 
@@ -126,14 +190,14 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   if (lane == 0) {
     W.e_out = e_un;
     if (W.e_state) *W.e_state = e_un;
-    W.accepted = accepted;
+    W.accepted = n_acc;
     unsigned long long* c = J.counters;
     c[kCntTrials] += (unsigned long long)W.n_trials;
     c[kCntEvaluated] += c_eval;
-    c[kCntDraws] += c_draws;
-    c[kCntAccepted] += (unsigned long long)accepted;
+    c[kCntDraws] += 6ull * (unsigned long long)W.n_trials + c_exp;
+    c[kCntAccepted] += n_acc;
     c[kCntExpTests] += c_exp;
-    c[kCntExactPath] += c_eval;
+    c[kCntExactPath] += c_exact;
     c[kCntExpFp64] += st.fp64;
     c[kCntExpCr] += st.cr;
     if (status != kStatusOk) *J.status = status;
@@ -170,9 +234,11 @@ __global__ void wl_average_kernel(const WlGroup* __restrict__ groups, WlWalker* 
 
 uint32_t wl_smem_bytes(const Geom& g, int nb) {
   uint32_t b = align_up((kMTN + kTbufWords) * 4, 16);
-  b += (uint32_t)(g.ns * g.ns * g.nsh) * 8 + 2u * (uint32_t)nb * 8 + (uint32_t)g.z * 4 +
-       (uint32_t)(g.nsh + 1) * 2;
+  const uint32_t nsp = (uint32_t)g.ns + 1, nF = nsp * (uint32_t)g.nsh * nsp;
+  b += (uint32_t)(g.ns * g.ns * g.nsh) * 8 + ((nF + 1) & ~1u) * 4 + 2u * (uint32_t)nb * 8 +
+       (uint32_t)g.z * 4 + (uint32_t)(g.nsh + 1) * 2;
   b = align_up(b, 16) + (uint32_t)g.n_sites;
+  b = align_up(b, 16) + 4u * (uint32_t)g.z * 8;  // staged exact-sum terms
   return align_up(b, 16);
 }
 

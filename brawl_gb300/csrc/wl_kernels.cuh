@@ -23,6 +23,8 @@ struct WlWalker {
   // done, and e_state (when set) carries e_unswapped between the launches.
   int64_t i0;
   double* e_state;
+  int32_t S;             // fixed-point shift of the chain's F table
+  int32_t pad;
 };
 
 // Walkers first..first+count-1 share a window and are averaged together.

@@ -254,7 +254,7 @@ int brawl_wl_destroy(brawl_wl *wl);
  * energy is outside its window (the reference would index outside its
  * histogram). */
 int brawl_wl_sweeps(brawl_wl *wl, int64_t n_trials, double wl_f, int hist_period,
-                    int64_t *accepted);
+                    int64_t *accepted);  /* n_trials < 2^31 */
 /* dos_average (src/wang-landau.F90:1127-1133): ln g averaged over the
  * walkers of each window (histograms untouched). */
 int brawl_wl_average(brawl_wl *wl);
