@@ -150,3 +150,13 @@ def test_flatness():
     assert O.wl_flatness([2.0, 4.0, 6.0]) == 2.0 / 4.0
     h = np.array([0.25, 0.5, 0.75, 1.0])
     assert O.wl_flatness(h) == 0.25 / (2.5 / 4)
+
+
+def test_windows_and_bins_follow_the_reference():
+    """divide_range / create_overlap / create_energy_bins for the golden
+    inputs (512 bins, 4 windows, 25% overlap, -96..0 meV/atom, 128 atoms)."""
+    from brawl_gb300 import wang_landau as W
+    assert W.divide_range(512, 4) == [[1, 128], [129, 256], [257, 384], [385, 512]]
+    assert W.create_overlap(W.divide_range(512, 4), 0.25) == [[1, 128], [97, 256], [217, 384], [343, 512]]
+    e = W.create_energy_bins(128, -96.0, 0.0, 512)
+    assert e.size == 513 and e[0] == -96.0 * 128 / (13.605693122 * 1000.0) and abs(e[-1]) < 1e-15
