@@ -270,6 +270,17 @@ def serving_leg(args) -> dict:
     }
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest x over the ranks (the job's time is its slowest rank's)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -395,10 +406,7 @@ def main() -> int:
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     dev_s = sum(step_ms) / 1000.0
     c1 = batch.counters()
-    if world > 1:
-        t = torch.tensor([dev_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t.item())
+    dev_s = max_over_ranks(dev_s, world, "cuda")
     d = (c1 - c0).sum(axis=0)
     T_all, T_eval, draws = int(d[0]), int(d[1]), int(d[2])
     assert T_all == trials_per_step * args.steps, (T_all, trials_per_step * args.steps)
@@ -427,7 +435,7 @@ def main() -> int:
         acc = batch.metropolis(trials)         # launch + wait + accept counts (d2h)
         batch.get_configs(host_grids)          # d2h: every replica's config
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
     e2e_value = world * trials_per_step * e2e_steps / e2e_s
     h2d = grid_bytes + 8 * args.replicas
     d2h = grid_bytes + 8 * args.replicas * 9

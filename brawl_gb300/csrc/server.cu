@@ -752,8 +752,11 @@ int launch_round(brawl_server* S, int kind) {
   SV_CUDA(cudaEventRecord(P.ev, P.s));
   P.inflight = true;
   P.t_launched = S->now();
+  int64_t work = 0;
+  for (auto& j : P.launched) work += j->quantum * (kind == kWl ? j->d.wl_walkers : 1);
+  std::lock_guard<std::mutex> lk(S->mu);  // telemetry is read by brawl_serve_profile
   P.launch_s += P.t_launched - t0;
-  for (auto& j : P.launched) P.work += j->quantum * (kind == kWl ? j->d.wl_walkers : 1);
+  P.work += work;
   return BRAWL_OK;
 }
 
@@ -965,8 +968,6 @@ void scheduler(brawl_server* S) {
         P.inflight = false;
         progressed = true;
         const double t_done = S->now();
-        P.busy_s += t_done - P.t_launched;
-        P.n_rounds += 1;
         Ended ended;
         int rc = q == cudaSuccess ? BRAWL_OK : api_fail(BRAWL_ECUDA, cudaGetErrorString(q));
         if (rc == BRAWL_OK)
@@ -976,8 +977,10 @@ void scheduler(brawl_server* S) {
           continue;
         }
         end_jobs(S, P, ended);
-        P.settle_s += S->now() - t_done;
         std::lock_guard<std::mutex> lk(S->mu);
+        P.busy_s += t_done - P.t_launched;
+        P.n_rounds += 1;
+        P.settle_s += S->now() - t_done;
         S->rounds += 1;
       }
       if (!P.inflight && !P.jobs.empty()) {
@@ -1046,7 +1049,6 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
   if (!(S->o.round_ms > 0.0)) S->o.round_ms = 20.0;
   if (S->o.max_trials < 0) S->o.max_trials = 0;
   if (S->o.max_iterations < 0) S->o.max_iterations = 0;
-  cudaGetDevice(&S->device);
   cudaDeviceGetAttribute(&S->max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, S->device);
   {
     // keep freed stream-ordered memory in this process's pool for reuse
