@@ -41,6 +41,16 @@ int fail(int code, const std::string& msg) {
 // cudaFreeAsync on the object's own stream): creating and destroying an
 // object never waits for kernels of other streams, so a serving loop keeps
 // other jobs' work in flight while objects come and go.
+// Objects' own streams (set-up, read-back, single calls) run at the
+// device's highest priority: a serving loop keeps long rounds of batched
+// kernels queued on low-priority streams, and the short work of admitting
+// or finishing a job should not wait behind them.
+inline cudaError_t object_stream(cudaStream_t* s) {
+  int lo = 0, hi = 0;
+  cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, hi);
+}
+
 template <typename T>
 cudaError_t dalloc(T** p, size_t bytes, cudaStream_t s) {
   return cudaMallocAsync(reinterpret_cast<void**>(p), bytes, s);
@@ -596,7 +606,7 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
   total = al(total + (size_t)n_chains * 4);
   const size_t off_energy = total;
   total = al(total + (size_t)n_chains * 8);
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (object_stream(&b->stream) != cudaSuccess)
     return cleanup(fail(BRAWL_ECUDA, "stream create failed"));
   cudaError_t e = dalloc(&b->arena, total, b->stream);
   if (e != cudaSuccess) {
@@ -1179,7 +1189,7 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
     brawl_ns_destroy(ns);
     return rc;
   };
-  if (cudaStreamCreateWithFlags(&ns->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (object_stream(&ns->stream) != cudaSuccess)
     return cleanup(fail(BRAWL_ECUDA, "stream create failed"));
   int max_optin = 0, dev = 0;
   cudaGetDevice(&dev);

@@ -1060,7 +1060,10 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
   }
   for (int k = 0; k < kKinds; ++k) {
     Pipe& P = S->pipe[k];
-    if (cudaStreamCreateWithFlags(&P.s, cudaStreamNonBlocking) != cudaSuccess ||
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    // rounds run at the lowest priority: set-up and read-back of jobs go first
+    if (cudaStreamCreateWithPriority(&P.s, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
         cudaEventCreateWithFlags(&P.ev, cudaEventDisableTiming) != cudaSuccess ||
         grow_host(P.h_stage, P.h_stage_cap, kPinnedStage) != BRAWL_OK ||
         grow_host(P.h_eout, P.h_eout_cap, kPinnedEntries) != BRAWL_OK ||
