@@ -37,6 +37,12 @@ import time
 
 import numpy as np
 
+# More hardware work queues than the default 8: the serving leg keeps long
+# rounds of kernels in flight on a few streams, and jobs' set-up and
+# read-back on their own streams must not queue behind them.  Read when the
+# CUDA context is created, so it is set before torch is imported.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)

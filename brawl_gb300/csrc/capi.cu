@@ -1738,7 +1738,8 @@ void api_batch_beta(brawl_batch* b, int c, ChainJob& j, double beta) { set_beta(
 
 int api_batch_set_rng(brawl_batch* b, int c, const uint32_t state[625]) {
   if (!b || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad chain");
-  CUDA_TRY(cudaMemcpy(b->jobs[c].rng, state, (kMTN + 1) * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpyAsync(b->jobs[c].rng, state, (kMTN + 1) * 4, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
   return BRAWL_OK;
 }
 

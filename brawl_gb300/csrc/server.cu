@@ -61,7 +61,7 @@ enum { kAnneal = 0, kWl = 1, kNs = 2, kKinds = 3 };
 // threads building admitted jobs' device objects and reading back ended
 // ones (a nested-sampling run's walker initialisation is one warp's
 // sequential work, so several run at once)
-constexpr int kWorkers = 16;
+constexpr int kWorkers = 8;
 // initial capacity of the pinned buffers: growing one (a pinned allocation)
 // waits for the whole device, so it should be rare
 constexpr size_t kPinnedEntries = 4096;
@@ -1039,6 +1039,11 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
   std::memset(&S->o, 0, sizeof(S->o));
   if (opts) S->o = *opts;
   cudaGetDevice(&S->device);
+  // The worker threads wait on their objects' streams; spinning waits (the
+  // runtime's default with few threads) would take the cores the scheduler
+  // thread needs, so host waits in this process block instead.
+  cudaSetDeviceFlags(cudaDeviceScheduleBlockingSync);
+  cudaGetLastError();
   if (S->o.hbm_budget == 0) {
     // 60% of the device memory free now
     size_t free_b = 0, total_b = 0;
@@ -1056,6 +1061,10 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
     if (cudaDeviceGetDefaultMemPool(&pool, S->device) == cudaSuccess) {
       uint64_t keep = S->o.hbm_budget;
       cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      // no reuse that makes one stream wait for another: a job's set-up
+      // would otherwise wait for a whole round of another pipeline
+      int no = 0;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
     }
   }
   for (int k = 0; k < kKinds; ++k) {

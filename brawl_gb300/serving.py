@@ -13,8 +13,15 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 
 import numpy as np
+
+# The server keeps long rounds of kernels in flight on a few streams while
+# jobs are set up and read back on their own; with the default 8 hardware
+# work queues those would often share a queue with a round and wait for it.
+# Takes effect if this module is imported before the CUDA context exists.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import BrawlError, K_B_IN_RY, LATTICES, RY_TO_EV, Setup, _Setup, _check, _ptr, _v_array, load
 
