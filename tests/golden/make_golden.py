@@ -9,7 +9,8 @@ Run in a container that has the reference checked out:
 Inputs (*.inp, *.vij) are copied verbatim; text outputs (*.dat, *.energies)
 are stored gzip-compressed byte-for-byte; netCDF outputs are converted to
 .npz with the variables' data (the reference's comparator, tests/ci_test.py,
-compares variable data only).
+compares variable data only), and a few are also kept verbatim under
+netcdf/ for the file writer's byte-for-byte tests.
 """
 from __future__ import annotations
 
@@ -24,6 +25,13 @@ from scipy.io import netcdf_file
 HERE = os.path.dirname(os.path.abspath(__file__))
 TESTS = ["01_serial_metropolis", "02_parallel_metropolis", "03_serial_nested_sampling",
          "04_parallel_wang-landau"]
+# netCDF outputs also kept verbatim, one of each kind the sampling path
+# writes, for byte-for-byte checks of the file writer
+RAW_NC = [("01_serial_metropolis", "proc_0000_final_config_at_0300.0.nc"),
+          ("01_serial_metropolis", "proc_0000_rho_of_T.nc"),
+          ("02_parallel_metropolis", "proc_0002_initial_config_at_0300.0.nc"),
+          ("02_parallel_metropolis", "av_radial_density.nc"),
+          ("04_parallel_wang-landau", "wl_dos.nc")]
 
 
 def main(ref_root: str) -> None:
@@ -45,6 +53,10 @@ def main(ref_root: str) -> None:
                 arrays = {k.replace(" ", "_"): np.array(v.data) for k, v in d.variables.items()}
                 d.close()
                 np.savez_compressed(os.path.join(dst, f[:-3] + ".npz"), **arrays)
+    raw = os.path.join(HERE, "netcdf")
+    os.makedirs(raw, exist_ok=True)
+    for t, f in RAW_NC:
+        shutil.copyfile(os.path.join(ref_root, "tests", "99_ref", t, f), os.path.join(raw, t[:2] + "_" + f))
     print("golden fixtures written to", HERE)
 
 

@@ -9,6 +9,7 @@ import pytest
 import brawl_gb300 as B
 from brawl_gb300 import inputs as I
 from brawl_gb300 import metropolis as anneal
+from brawl_gb300 import netcdf_io as NC
 from brawl_gb300 import output as OUT
 from oracle import oracle as O
 from tests import golden_io as G
@@ -46,7 +47,7 @@ MET = [("01_serial_metropolis", 0)] + [("02_parallel_metropolis", r) for r in ra
 
 
 @pytest.mark.parametrize("test,rank", MET)
-def test_golden_anneal_on_gpu(test, rank):
+def test_golden_anneal_on_gpu(test, rank, tmp_path):
     p, V = G.load_inputs(test)
     m = I.read_metropolis_file(G.path(test, "metropolis.inp"))
     ch = B.Chain(B.Setup.from_run_params(p), V)
@@ -73,6 +74,12 @@ def test_golden_anneal_on_gpu(test, rank):
         diag = OUT.diagnostics_lines(out["temperature"], out["energies_of_T"], out["C_of_T"],
                                      out["acceptance_of_T"])
         assert diag == G.text(test, tag + "_energy_diagnostics.dat")
+    if test.startswith("02") and rank == 2:
+        # the configuration file itself, byte for byte
+        path = tmp_path / "init.nc"
+        NC.write_config(str(path), out["initial_configs"][0], p)
+        with open(G.path("netcdf", "02_proc_0002_initial_config_at_0300.0.nc"), "rb") as f:
+            assert path.read_bytes() == f.read()
 
 
 # ---------------------------------------------------------------------------
