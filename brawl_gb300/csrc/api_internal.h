@@ -9,6 +9,7 @@
 #include "../../include/brawl_gpu.h"
 #include "chain_engine.cuh"
 #include "kernels.cuh"
+#include "lazy_exact.cuh"
 #include "ns_kernels.cuh"
 #include "wl_kernels.cuh"
 

@@ -1205,9 +1205,12 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
     if (rc != BRAWL_OK) return cleanup(fail(rc, "run " + std::to_string(r) + ": " + g_err));
     if (d.n_walkers < 1 || d.n_steps < 0 || !d.species_concentrations)
       return cleanup(fail(BRAWL_EINVAL, "run " + std::to_string(r) + ": bad n_walkers/n_steps/concentrations"));
-    ns->smem = std::max(ns->smem, ns_smem_bytes(m.g));
     NsRun& R = ns->runs[r];
     std::memset(&R, 0, sizeof(R));
+    R.lazy_cap = lazy_cap_for(m.g, ns_smem_bytes(m.g, 0), (uint32_t)max_optin);
+    if (R.lazy_cap == 0)
+      return cleanup(fail(BRAWL_EINVAL, "run " + std::to_string(r) + ": lattice too large for shared memory"));
+    ns->smem = std::max(ns->smem, ns_smem_bytes(m.g, R.lazy_cap));
     std::vector<double> conc(d.species_concentrations, d.species_concentrations + m.g.ns + 1);
     rc = make_init_job(m, conc.data(), d.species_numbers, R.init);
     if (rc != BRAWL_OK) return cleanup(fail(rc, "run " + std::to_string(r) + ": " + g_err));
@@ -1507,7 +1510,10 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
     W.e1 = wl->e1;
     W.range = wl->range;
     hoff += W.end - W.start + 1;
-    wl->smem = std::max(wl->smem, wl_smem_bytes(W.job.g, W.end - W.start + 1));
+    const uint32_t base = wl_smem_bytes(W.job.g, W.end - W.start + 1, 0);
+    W.lazy_cap = lazy_cap_for(W.job.g, base, (uint32_t)max_optin);
+    if (W.lazy_cap == 0) return cleanup(fail(BRAWL_EINVAL, "window or lattice too large for shared memory"));
+    wl->smem = std::max(wl->smem, wl_smem_bytes(W.job.g, W.end - W.start + 1, W.lazy_cap));
     if (c == 0 || walkers[c].window != walkers[c - 1].window) wl->groups.push_back({c, 0});
     wl->groups.back().count += 1;
   }

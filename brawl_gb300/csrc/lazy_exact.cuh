@@ -1,0 +1,195 @@
+// lazy_exact.cuh -- deferred reference-order energies for walkers that carry
+// their energy in FP64 (Wang-Landau sweeps, nested-sampling walks).
+//
+// The reference updates a walker's energy on every accepted move from the
+// two FP64 pair energies, each a chain of dependent FP64 adds in neighbour
+// list order.  Most decisions only need an interval that contains that
+// energy: the fixed-point delta gives one (band quanta wide per move), and a
+// bin or a ceiling is usually far from its edges.  So an accepted move whose
+// decision the interval settles is logged -- the species of the two sites
+// and of their neighbours as they were at the move -- and the FP64 sums of
+// the logged moves run later, together: one chain per (move, site, before or
+// after, shell), several chains per lane so the FP64 adds overlap, then the
+// walker's energy folded through the moves in order exactly as the
+// reference does.  Same values, same order, same roundings: identical
+// energies; only when they are computed changes.  A decision the interval
+// does not settle flushes the log first and then takes the exact path.
+#pragma once
+
+#include "chain_engine.cuh"
+
+namespace brawl {
+
+constexpr int kLazyMaxCap = 64;
+constexpr int kLazyPartner = 0x40;  // the neighbour is the other site of the pair
+constexpr int kLazySelf = 0x80;     // the neighbour is the site itself (small lattices)
+
+// Shared-memory bytes of a log of `cap` moves: neighbour codes (2 z bytes a
+// move), the pair's species (2), the chain sums (4 nsh doubles) and the pair
+// energies (2 doubles).
+__host__ __device__ inline uint32_t lazy_bytes(const Geom& g, int cap) {
+  const uint32_t c = (uint32_t)cap;
+  uint32_t b = align_up(c * 2u * (uint32_t)g.z, 16);
+  b += align_up(c * 2u, 16);
+  b += c * 4u * (uint32_t)g.nsh * 8u;
+  b += c * 2u * 8u;
+  return align_up(b, 16);
+}
+
+// The largest log (a power of two, at most kLazyMaxCap) that fits beside
+// `base` bytes within `limit`; 0 when not even one move fits.
+inline int lazy_cap_for(const Geom& g, uint32_t base, uint32_t limit) {
+  for (int cap = kLazyMaxCap; cap >= 1; cap >>= 1)
+    if (base + lazy_bytes(g, cap) <= limit) return cap;
+  return 0;
+}
+
+struct LazyLog {
+  uint8_t* codes;  // [cap][2][z]: species | kLazyPartner | kLazySelf
+  int8_t* spec;    // [cap][2]: species of site 1 and site 2 before the move
+  double* part;    // [cap][4][nsh]: shell sums, then site energies
+  double* pair;    // [cap][2]: pair energy before and after
+  int cap;
+};
+
+__device__ inline LazyLog lazy_layout(const Geom& g, unsigned char* base, int cap) {
+  LazyLog L;
+  const uint32_t c = (uint32_t)cap;
+  L.codes = base;
+  base += align_up(c * 2u * (uint32_t)g.z, 16);
+  L.spec = reinterpret_cast<int8_t*>(base);
+  base += align_up(c * 2u, 16);
+  L.part = reinterpret_cast<double*>(base);
+  base += c * 4u * (uint32_t)g.nsh * 8u;
+  L.pair = reinterpret_cast<double*>(base);
+  L.cap = cap;
+  return L;
+}
+
+// compact_fixed_delta, also writing the neighbour codes of both sites to
+// rec[0, 2z) (site 1's entries first).
+__device__ __forceinline__ int compact_fixed_delta_rec(const Geom& g, const int8_t* lat,
+                                                       const int32_t* F, const uint32_t* ents,
+                                                       const SitePair& p, int lane, uint8_t* rec) {
+  const bool h = lane >= 16;
+  const int cx = h ? p.bx : p.ax, cy = h ? p.by : p.ay, cz = h ? p.bz : p.az;
+  const int own = h ? p.bi : p.ai, other = h ? p.ai : p.bi;
+  const int so = h ? p.sb : p.sa, sn = h ? p.sa : p.sb;
+  const int nsp = g.ns + 1;
+  const int rowN = sn * g.nsh * nsp, rowO = so * g.nsh * nsp;
+  uint8_t* out = rec + (h ? g.z : 0);
+  int acc = 0;
+  for (int k = lane & 15; k < g.z; k += 16) {
+    int dx, dy, dz, sh;
+    unpack_entry(ents[k], dx, dy, dz, sh);
+    const int ni = neighbour_index(g, cx, cy, cz, dx, dy, dz);
+    const int sb = lat[ni];
+    const int sa = ni == other ? so : (ni == own ? sn : sb);
+    out[k] = (uint8_t)(sb | (ni == other ? kLazyPartner : 0) | (ni == own ? kLazySelf : 0));
+    acc += F[rowN + sh * nsp + sa] - F[rowO + sh * nsp + sb];
+  }
+  return __reduce_add_sync(kFull, acc);
+}
+
+// Copies a move's codes between log slots (all lanes).
+__device__ __forceinline__ void lazy_copy_slot(const Geom& g, const uint8_t* from, uint8_t* to,
+                                               int lane) {
+  for (int k = lane; k < 2 * g.z; k += 32) to[k] = from[k];
+  __syncwarp();
+}
+
+enum LazyFold : int {
+  kFoldWangLandau = 0,  // e = (e - pair_before) + pair_after
+  kFoldNested = 1,      // e = e + (pair_after - pair_before)
+};
+
+constexpr int kLazyIlp = 8;  // chains per lane in flight
+
+// The exact energies of the n logged moves folded into e (the walker's
+// exact energy before the first of them).  All lanes; returns the same value
+// in every lane.
+static __device__ __noinline__ double lazy_flush(const Geom& g, const double* V, const int16_t* sstart,
+                                          LazyLog L, int n, double e, int fold, int lane) {
+  const int z = g.z, nsh = g.nsh, ns = g.ns;
+  const int nch = 4 * n;  // chains per shell: (move, evaluation)
+  for (int sh = 0; sh < nsh; ++sh) {
+    const int k0 = sstart[sh], len = sstart[sh + 1] - k0;
+    const double* Vsh = V + ns * ns * sh;
+    for (int c0 = 0; c0 < nch; c0 += 32 * kLazyIlp) {
+      double sum[kLazyIlp];
+      int row[kLazyIlp], cs[kLazyIlp], s_before[kLazyIlp], s_after[kLazyIlp];
+      bool on[kLazyIlp], after[kLazyIlp];
+#pragma unroll
+      for (int i = 0; i < kLazyIlp; ++i) {
+        const int c = c0 + 32 * i + lane;
+        on[i] = c < nch;
+        const int m = on[i] ? c >> 2 : 0, ev = c & 3;
+        const bool site2 = ev & 1;
+        after[i] = ev >= 2;
+        const int sa = L.spec[2 * m], sb = L.spec[2 * m + 1];
+        s_before[i] = site2 ? sb : sa;  // the site's own species before the move
+        s_after[i] = site2 ? sa : sb;
+        cs[i] = after[i] ? s_after[i] : s_before[i];
+        row[i] = m * 2 * z + (site2 ? z : 0) + k0;
+        sum[i] = 0.0;
+      }
+      for (int k = 0; k < len; ++k) {
+#pragma unroll
+        for (int i = 0; i < kLazyIlp; ++i) {
+          if (!on[i]) continue;
+          const int code = L.codes[row[i] + k];
+          int s = code & 0x3f;
+          if (after[i]) {
+            if (code & kLazyPartner) s = s_before[i];  // the partner now holds our old species
+            else if (code & kLazySelf) s = s_after[i];
+          }
+          sum[i] = __dadd_rn(sum[i], Vsh[(cs[i] - 1) + ns * (s - 1)]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kLazyIlp; ++i) {
+        const int c = c0 + 32 * i + lane;
+        if (on[i]) L.part[c * nsh + sh] = sum[i];
+      }
+    }
+  }
+  __syncwarp();
+  // site energies: shell 1 + shell 2 + ... left to right
+  for (int c0 = 0; c0 < nch; c0 += 32 * kLazyIlp) {
+    double acc[kLazyIlp];
+#pragma unroll
+    for (int i = 0; i < kLazyIlp; ++i) {
+      const int c = c0 + 32 * i + lane;
+      acc[i] = c < nch ? L.part[c * nsh] : 0.0;
+    }
+    for (int sh = 1; sh < nsh; ++sh) {
+#pragma unroll
+      for (int i = 0; i < kLazyIlp; ++i) {
+        const int c = c0 + 32 * i + lane;
+        if (c < nch) acc[i] = __dadd_rn(acc[i], L.part[c * nsh + sh]);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < kLazyIlp; ++i) {
+      const int c = c0 + 32 * i + lane;
+      if (c < nch) L.part[c * nsh] = acc[i];
+    }
+  }
+  __syncwarp();
+  // pair energies: site 1 + site 2, before and after
+  for (int i = lane; i < 2 * n; i += 32) {
+    const int m = i >> 1, aft = i & 1;
+    const double* e4 = L.part + (size_t)(4 * m + 2 * aft) * nsh;
+    L.pair[i] = __dadd_rn(e4[0], e4[nsh]);
+  }
+  __syncwarp();
+  for (int m = 0; m < n; ++m) {
+    const double pb = L.pair[2 * m], pa = L.pair[2 * m + 1];
+    e = fold == kFoldWangLandau ? __dadd_rn(__dsub_rn(e, pb), pa) : __dadd_rn(e, __dsub_rn(pa, pb));
+  }
+  __syncwarp();
+  return e;
+}
+
+}  // namespace brawl

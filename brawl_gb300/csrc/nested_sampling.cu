@@ -5,13 +5,16 @@
 // random swaps, each accepted iff E + dE stays below the ceiling.
 //
 // One warp per independent run.  The walkers live in HBM (compact, one byte
-// per site); the active walker is staged in shared memory for its walk.  A
-// walk step's dE is needed exactly whenever the move may be accepted (the
-// walker's energy is carried in FP64), so the fixed-point tier only rejects
-// moves that certainly climb over the ceiling; the others take the
+// per site); the active walker is staged in shared memory for its walk.  The
+// walker's energy is carried in FP64 as the reference does; the kernel keeps
+// an interval that contains it, and the fixed-point delta settles most
+// steps: certainly over the ceiling (rejected) or certainly under it
+// (accepted, logged, its FP64 sums run later with others, lazy_exact.cuh).
+// A step the interval does not settle flushes the log and takes the
 // reference-order FP64 sums.
 #include "halo_engine.cuh"
 #include "kernels.cuh"
+#include "lazy_exact.cuh"
 #include "ns_kernels.cuh"
 
 namespace brawl {
@@ -66,7 +69,19 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
-// Fixed-point lower bound of the ceiling gap: Gup >= (limit - E) * 2^S.
+// Fixed-point lower bound of the room under the ceiling: Gdn <= (pred(limit)
+// - E) * 2^S, pred(limit) the largest double below it; a step with
+// dE + band <= Gdn certainly lands strictly below the ceiling.
+__device__ __forceinline__ long long gap_dn(double limit, double E, int S) {
+  const double gd = __dsub_rd(nextafter(limit, -__longlong_as_double(0x7ff0000000000000LL)), E);
+  const double m = __dsub_rd(gd, __dmul_ru(fabs(gd), 8.881784197001252e-16));  // - |gd| 2^-50
+  const double s = ldexp(m, S);
+  if (!(s > -9.0e18)) return -0x7fffffffffffffffll;
+  if (s > 9.0e18) return 0x7fffffffffffffffll;
+  return (long long)floor(s);
+}
+
+// Fixed-point upper bound of the ceiling gap: Gup >= (limit - E) * 2^S.
 __device__ __forceinline__ long long gap_up(double limit, double E, int S) {
   const double gd = __dsub_rn(limit, E);
   const double m = __dadd_rn(gd, __dmul_rn(fabs(gd), 8.881784197001252e-16));  // + |gd| 2^-50
@@ -98,6 +113,8 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
       smem + align_up((uint32_t)((reinterpret_cast<unsigned char*>(sstart + g.nsh + 1)) - smem), 16));
   double* vbuf = reinterpret_cast<double*>(smem + align_up((uint32_t)(lat - reinterpret_cast<int8_t*>(smem)) +
                                                                 (uint32_t)g.n_sites, 16));
+  const LazyLog LG = lazy_layout(g, reinterpret_cast<unsigned char*>(vbuf + 4 * g.z), R.lazy_cap);
+  const double q = ldexp(1.0, -R.S);
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
   for (int i = lane; i < nF; i += 32) F[i] = J.F[i];
@@ -155,12 +172,25 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
     if (irnd < 1) irnd = 1;
     const int8_t* src = R.walkers + (size_t)(irnd - 1) * n;
     for (int i = lane; i < n; i += 32) lat[i] = src[i];
+    // E: the walker's exact energy before the n_log logged steps;
+    // [E_lo, E_hi] contains it after them
     double E = R.energies[irnd - 1];
+    double E_lo = E, E_hi = E;
+    int n_log = 0;
     __syncwarp();
-    long long gup = gap_up(limit, E, S);
+    long long gup = gap_up(limit, E, S), gdn = gap_dn(limit, E, S);
+    auto flush = [&]() {
+      if (n_log == 0) return;
+      E = lazy_flush(g, V, sstart, LG, n_log, E, kFoldNested, lane);
+      if (!(E >= E_lo && E <= E_hi)) status = kStatusBandViolated;
+      E_lo = E_hi = E;
+      n_log = 0;
+      gup = gap_up(limit, E, S);
+      gdn = gap_dn(limit, E, S);
+    };
     n_acc = 0;
     const long long steps = (long long)R.n_steps + extra_steps;
-    for (long long st = 0; st < steps; ++st) {
+    for (long long st = 0; st < steps && status == kStatusOk; ++st) {
       ring_ensure(mt, tbuf, ring, 3, lane);
       SitePair p;
       draw_site(g, tbuf[ring.idx], tbuf[ring.idx + 1], tbuf[ring.idx + 2], p.ax, p.ay, p.az);
@@ -183,26 +213,53 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
       if (status != kStatusOk) break;
       c_draws += 3;
       ++c_steps;
-      const int dE = compact_fixed_delta(g, lat, F, ents, p, lane);
+      uint8_t* rec = LG.codes + (size_t)n_log * 2 * g.z;
+      const int dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
       // certainly E + dE >= ceiling: rejected without the FP64 sums
       if ((long long)dE - band >= gup) continue;
-      ++c_exact;
-      double e_un, e_sw;
-      exact_pair_energies_staged(g, CompactLat{lat}, V, ents, sstart, p, lane, e_un, e_sw, vbuf);
-      const double delta_e = __dsub_rn(e_sw, e_un);
-      const double e_new = __dadd_rn(E, delta_e);
-      if (e_new < limit) {
-        E = e_new;
-        ++n_acc;
-        ++c_acc;
-        if (lane == 0) {
-          lat[p.ai] = (int8_t)p.sb;
-          lat[p.bi] = (int8_t)p.sa;
-        }
+      bool logged = false;
+      if ((long long)dE + band > gdn && n_log > 0) {
+        // not settled with the logged steps' interval: their exact energy
+        // may settle it; this step's codes move to the log's first slot
         __syncwarp();
-        gup = gap_up(limit, E, S);
+        flush();
+        lazy_copy_slot(g, rec, LG.codes, lane);
+        if ((long long)dE - band >= gup) continue;
       }
+      if ((long long)dE + band <= gdn) {
+        // certainly below the ceiling: accepted, the FP64 sums deferred
+        if (lane == 0) {
+          LG.spec[2 * n_log] = (int8_t)p.sa;
+          LG.spec[2 * n_log + 1] = (int8_t)p.sb;
+        }
+        ++n_log;
+        E_lo = __dadd_rd(E_lo, __dmul_rn((double)((long long)dE - band), q));
+        E_hi = __dadd_ru(E_hi, __dmul_rn((double)((long long)dE + band), q));
+        gup = gap_up(limit, E_lo, S);
+        gdn = gap_dn(limit, E_hi, S);
+        logged = true;
+      } else {
+        // the exact step, as the reference takes it (the log is empty)
+        ++c_exact;
+        double e_un, e_sw;
+        exact_pair_energies_staged(g, CompactLat{lat}, V, ents, sstart, p, lane, e_un, e_sw, vbuf);
+        const double delta_e = __dsub_rn(e_sw, e_un);
+        const double e_new = __dadd_rn(E, delta_e);
+        if (!(e_new < limit)) continue;
+        E = E_lo = E_hi = e_new;
+        gup = gap_up(limit, E, S);
+        gdn = gap_dn(limit, E, S);
+      }
+      ++n_acc;
+      ++c_acc;
+      if (lane == 0) {
+        lat[p.ai] = (int8_t)p.sb;
+        lat[p.bi] = (int8_t)p.sa;
+      }
+      __syncwarp();
+      if (logged && n_log == LG.cap) flush();
     }
+    flush();
     if (status != kStatusOk) break;
     int8_t* dst = R.walkers + (size_t)imax * n;
     for (int i = lane; i < n; i += 32) dst[i] = lat[i];
@@ -225,14 +282,15 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
   }
 }
 
-uint32_t ns_smem_bytes(const Geom& g) {
+uint32_t ns_smem_bytes(const Geom& g, int lazy_cap) {
   const uint32_t nsp = (uint32_t)g.ns + 1;
   uint32_t b = align_up((kMTN + kTbufWords) * 4, 16);
   b += (uint32_t)(g.ns * g.ns * g.nsh) * 8 + nsp * (uint32_t)g.nsh * nsp * 4 + (uint32_t)g.z * 4 +
        (uint32_t)(g.nsh + 1) * 2;
   b = align_up(b, 16) + (uint32_t)g.n_sites;
   b = align_up(b, 16) + 4u * (uint32_t)g.z * 8;  // staged exact-sum terms
-  return align_up(b, 16);
+  b = align_up(b, 16);
+  return lazy_cap > 0 ? b + lazy_bytes(g, lazy_cap) : b;
 }
 
 void launch_ns_init(NsRun* d_runs, int n_runs, cudaStream_t stream) {

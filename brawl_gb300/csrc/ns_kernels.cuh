@@ -20,10 +20,12 @@ struct NsRun {
   int64_t n_acc;       // accepted steps of the latest walk
   int64_t iter;        // iterations done
   int32_t n_iter;      // iterations of the current launch
-  int32_t pad;
+  int32_t lazy_cap;    // steps the deferred-energy log holds (>= 1)
 };
 
-uint32_t ns_smem_bytes(const Geom& g);
+// Shared memory of a run's walks; lazy_cap 0 gives the bytes without the
+// deferred-energy log.
+uint32_t ns_smem_bytes(const Geom& g, int lazy_cap);
 void launch_ns_init(NsRun* d_runs, int n_runs, cudaStream_t stream);
 void launch_ns_jitter(NsRun* d_runs, int n_runs, int max_K, cudaStream_t stream);
 void launch_ns_iterate(NsRun* d_runs, int n_runs, uint32_t smem_bytes, cudaStream_t stream);

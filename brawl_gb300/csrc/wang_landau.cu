@@ -5,13 +5,18 @@
 // division by their number.
 //
 // One warp per walker.  Each trial's bins depend on the walker's running
-// FP64 energy, so a trial whose two species differ takes the reference-order
-// FP64 pair energies (e_swapped = e_unswapped - pair_unswapped +
-// pair_swapped); the acceptance test log(genrand()) < lng(i) - lng(j) is
-// decided in FP32 first (exact_fp.cuh).  The window's ln g and histogram
-// slices are staged in shared memory.
+// FP64 energy (e_swapped = e_unswapped - pair_unswapped + pair_swapped, the
+// pair energies summed in the reference's order).  The kernel carries an
+// interval that contains it: a trial's bin comes from the fixed-point delta
+// when the interval lies in one bin, and accepted moves are logged and
+// their FP64 sums run together later (lazy_exact.cuh); a bin the interval
+// does not settle flushes the log and takes the exact sums.  The acceptance
+// test log(genrand()) < lng(i) - lng(j) is decided in FP32 first
+// (exact_fp.cuh).  The window's ln g and histogram slices are staged in
+// shared memory.
 #include "halo_engine.cuh"
 #include "kernels.cuh"
+#include "lazy_exact.cuh"
 #include "wl_kernels.cuh"
 
 namespace brawl {
@@ -78,6 +83,7 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
       smem + align_up((uint32_t)((reinterpret_cast<unsigned char*>(sstart + g.nsh + 1)) - smem), 16));
   double* vbuf = reinterpret_cast<double*>(smem + align_up((uint32_t)(lat - reinterpret_cast<int8_t*>(smem)) +
                                                                 (uint32_t)g.n_sites, 16));
+  const LazyLog LG = lazy_layout(g, reinterpret_cast<unsigned char*>(vbuf + 4 * g.z), W.lazy_cap);
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
   for (int i = lane; i < nF; i += 32) F[i] = J.F[i];
@@ -99,13 +105,25 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   const int band = J.band;
   const double q = ldexp(1.0, -W.S);               // one fixed-point quantum
   const double pair_bound = ldexp(1.0, 30 - W.S);   // >= 4 z max|V|: bounds |pair energy|
-  double e_un = (W.i0 > 0 && W.e_state) ? *W.e_state : (W.e0_src ? *W.e0_src : W.e0);
-  int ibin = wl_bin_index(e_un, e1, range, bins);
+  // e_ex: the reference's e_unswapped before the n_log logged moves;
+  // [e_lo, e_hi] contains it after them
+  double e_ex = (W.i0 > 0 && W.e_state) ? *W.e_state : (W.e0_src ? *W.e0_src : W.e0);
+  double e_lo = e_ex, e_hi = e_ex;
+  int n_log = 0;
+  int ibin = wl_bin_index(e_ex, e1, range, bins);
   int status = (ibin < start || ibin > end) ? kStatusWalkerOutsideWindow : kStatusOk;
   unsigned int c_eval = 0, c_exp = 0, c_exact = 0, n_acc = 0;
   DecideStats st = {0u, 0u};
   // histogram ticks at trials i with i % period == 0
   long long until = period > 0 ? period - (W.i0 % period) : -1;
+  // folds the logged moves into e_ex; their energy must be in [e_lo, e_hi]
+  auto flush = [&]() {
+    if (n_log == 0) return;
+    e_ex = lazy_flush(g, V, sstart, LG, n_log, e_ex, kFoldWangLandau, lane);
+    if (!(e_ex >= e_lo && e_ex <= e_hi)) status = kStatusBandViolated;
+    e_lo = e_hi = e_ex;
+    n_log = 0;
+  };
 
   const int n_tr = (int)W.n_trials;
   for (int it = 0; it < n_tr && status == kStatusOk; ++it) {
@@ -121,27 +139,42 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
     const bool differ = p.sa != p.sb;
     int jbin = ibin;
     bool exact_done = false;
-    double e_sw = e_un;
+    double e_sw = e_ex, s_lo = e_lo, s_hi = e_hi;
+    uint8_t* rec = LG.codes + (size_t)n_log * 2 * g.z;
     if (differ) {
       ++c_eval;
       // The reference's e_swapped lies within band quanta of e_un + dE q
-      // (pair sums) plus the two roundings of e_un - p_un + p_sw; its bin is
-      // decided without the FP64 sums when that interval sits in one bin.
-      const int dE = compact_fixed_delta(g, lat, F, ents, p, lane);
+      // (pair sums) plus the two roundings of e_un - p_un + p_sw, for any
+      // e_un in [e_lo, e_hi]; its bin is decided without the FP64 sums when
+      // that interval sits in one bin.
+      const int dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
       const double lo_d = __dmul_rn((double)(dE - band), q), hi_d = __dmul_rn((double)(dE + band), q);
-      const double w = (2.0 * fabs(e_un) + fabs(lo_d) + fabs(hi_d) + pair_bound) * 2.3e-16;
-      const double elo = __dsub_rd(__dadd_rd(e_un, lo_d), w);
-      const double ehi = __dadd_ru(__dadd_ru(e_un, hi_d), w);
-      const float tlo = __fmul_rd(__double2float_rd(__dsub_rd(elo, e1)), rf);
-      const float thi = __fmul_ru(__double2float_ru(__dsub_ru(ehi, e1)), rf);
-      const float blo = truncf(__fsub_rd(tlo, fabsf(tlo) * 2.5e-7f + 1.0e-30f));
-      const float bhi = truncf(__fadd_ru(thi, fabsf(thi) * 2.5e-7f + 1.0e-30f));
-      if (blo == bhi && fabsf(tlo) < 5.0e8f && fabsf(thi) < 5.0e8f) {
-        jbin = (int)blo + 1;
-      } else {
+      bool settled = false;
+      for (int pass = 0; pass < 2 && !settled; ++pass) {
+        const double w = (2.0 * fmax(fabs(e_lo), fabs(e_hi)) + fabs(lo_d) + fabs(hi_d) + pair_bound) * 2.3e-16;
+        s_lo = __dsub_rd(__dadd_rd(e_lo, lo_d), w);
+        s_hi = __dadd_ru(__dadd_ru(e_hi, hi_d), w);
+        const float tlo = __fmul_rd(__double2float_rd(__dsub_rd(s_lo, e1)), rf);
+        const float thi = __fmul_ru(__double2float_ru(__dsub_ru(s_hi, e1)), rf);
+        const float blo = truncf(__fsub_rd(tlo, fabsf(tlo) * 2.5e-7f + 1.0e-30f));
+        const float bhi = truncf(__fadd_ru(thi, fabsf(thi) * 2.5e-7f + 1.0e-30f));
+        if (blo == bhi && fabsf(tlo) < 5.0e8f && fabsf(thi) < 5.0e8f) {
+          jbin = (int)blo + 1;
+          settled = true;
+        } else if (pass == 0 && n_log > 0) {
+          // the logged moves' exact energy may settle it; this move's codes
+          // move to the log's first slot
+          flush();
+          lazy_copy_slot(g, rec, LG.codes, lane);
+          rec = LG.codes;
+        } else {
+          break;
+        }
+      }
+      if (!settled) {
         ++c_exact;
         exact_done = true;
-        e_sw = wl_exact_e_sw(g, lat, V, ents, sstart, p, lane, e_un, vbuf);
+        e_sw = wl_exact_e_sw(g, lat, V, ents, sstart, p, lane, e_ex, vbuf);
         jbin = wl_bin_index_fast(e_sw, e1, range, bins, rf);
       }
     }
@@ -153,16 +186,23 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
       const double d = __dsub_rn(lng[ibin - start], lng[jbin - start]);
       if (log_u_lt(wu, d, st)) {
         ++n_acc;
-        if (differ && !exact_done) {
-          // accepted: the walker's energy takes the reference's exact value
-          ++c_exact;
-          e_sw = wl_exact_e_sw(g, lat, V, ents, sstart, p, lane, e_un, vbuf);
-          if (wl_bin_index_fast(e_sw, e1, range, bins, rf) != jbin) status = kStatusBandViolated;
-        }
-        e_un = e_sw;
-        if (differ && lane == 0) {
-          lat[p.ai] = (int8_t)p.sb;
-          lat[p.bi] = (int8_t)p.sa;
+        if (differ) {
+          if (exact_done) {
+            e_ex = e_lo = e_hi = e_sw;  // the log is empty here
+          } else {
+            // logged: the energy after it is in [s_lo, s_hi]
+            if (lane == 0) {
+              LG.spec[2 * n_log] = (int8_t)p.sa;
+              LG.spec[2 * n_log + 1] = (int8_t)p.sb;
+            }
+            ++n_log;
+            e_lo = s_lo;
+            e_hi = s_hi;
+          }
+          if (lane == 0) {
+            lat[p.ai] = (int8_t)p.sb;
+            lat[p.bi] = (int8_t)p.sa;
+          }
         }
         ibin = jbin;
       } else {
@@ -177,8 +217,11 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
     }
     if (lane == 0) lng[jbin - start] = __dadd_rn(lng[jbin - start], f);
     __syncwarp();
+    if (n_log == LG.cap) flush();
     ring_consume(ring, consumed);
   }
+  flush();
+  const double e_un = e_ex;
 
   __syncwarp();
   for (int i = lane; i < nb; i += 32) {
@@ -232,14 +275,15 @@ __global__ void wl_average_kernel(const WlGroup* __restrict__ groups, WlWalker* 
   }
 }
 
-uint32_t wl_smem_bytes(const Geom& g, int nb) {
+uint32_t wl_smem_bytes(const Geom& g, int nb, int lazy_cap) {
   uint32_t b = align_up((kMTN + kTbufWords) * 4, 16);
   const uint32_t nsp = (uint32_t)g.ns + 1, nF = nsp * (uint32_t)g.nsh * nsp;
   b += (uint32_t)(g.ns * g.ns * g.nsh) * 8 + ((nF + 1) & ~1u) * 4 + 2u * (uint32_t)nb * 8 +
        (uint32_t)g.z * 4 + (uint32_t)(g.nsh + 1) * 2;
   b = align_up(b, 16) + (uint32_t)g.n_sites;
   b = align_up(b, 16) + 4u * (uint32_t)g.z * 8;  // staged exact-sum terms
-  return align_up(b, 16);
+  b = align_up(b, 16);
+  return lazy_cap > 0 ? b + lazy_bytes(g, lazy_cap) : b;
 }
 
 void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, cudaStream_t stream) {

@@ -24,7 +24,7 @@ struct WlWalker {
   int64_t i0;
   double* e_state;
   int32_t S;             // fixed-point shift of the chain's F table
-  int32_t pad;
+  int32_t lazy_cap;      // moves the deferred-energy log holds (>= 1)
 };
 
 // Walkers first..first+count-1 share a window and are averaged together.
@@ -32,7 +32,9 @@ struct WlGroup {
   int32_t first, count;
 };
 
-uint32_t wl_smem_bytes(const Geom& g, int nb);
+// Shared memory of a walker's sweep; lazy_cap 0 gives the bytes without the
+// deferred-energy log.
+uint32_t wl_smem_bytes(const Geom& g, int nb, int lazy_cap);
 void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, cudaStream_t stream);
 void launch_wl_average(const WlGroup* d_groups, int n_groups, WlWalker* d_walkers, int bins,
                        int with_hist, cudaStream_t stream);
