@@ -98,6 +98,38 @@ __device__ __forceinline__ void lazy_copy_slot(const Geom& g, const uint8_t* fro
   __syncwarp();
 }
 
+// An upper bound of |E| in quanta 2^-S (saturated far below overflow).
+__device__ __forceinline__ long long quanta_bound(double E, int S) {
+  const double s = ldexp(fabs(E), S);
+  return s < 1.0e18 ? (long long)ceil(s) + 1 : 1000000000000000000ll;
+}
+
+// E lies in E0 + [lo, hi] quanta (the check of a deferred energy).
+__device__ __forceinline__ bool in_quanta(double E, double E0, long long lo, long long hi, double q) {
+  const double a = __dadd_rd(E0, __dmul_rd(__ll2double_rd(lo), q));
+  const double b = __dadd_ru(E0, __dmul_ru(__ll2double_ru(hi), q));
+  return E >= a && E <= b;
+}
+
+// The bin (int(t) + 1, as bin_index) of every energy in E0 + [lo, hi]
+// quanta, from t0 = float((E0 - e1) * bins / range) and qrf = float(q * bins /
+// range), when one bin holds them all.  t0 is within 6e-8 |t0| of the exact
+// coordinate, the offsets within 1.8e-7 |offset| (three roundings), their
+// sums within 6e-8 |t|, and the reference's own t within 5e-16 |t|; m
+// doubles that.  Far outside (|t| >= 5e8) is left to the exact path.
+__device__ __forceinline__ bool bin_from_quanta(float t0, float qrf, long long lo, long long hi,
+                                                int& bin) {
+  const float plo = __fmul_rn(__ll2float_rn(lo), qrf), phi = __fmul_rn(__ll2float_rn(hi), qrf);
+  const float tlo = __fadd_rn(t0, plo), thi = __fadd_rn(t0, phi);
+  if (!(fabsf(tlo) < 5.0e8f && fabsf(thi) < 5.0e8f)) return false;
+  const float m = (fabsf(t0) + fmaxf(fabsf(tlo), fabsf(thi))) * 1.2e-7f +
+                  fmaxf(fabsf(plo), fabsf(phi)) * 3.6e-7f + 1.0e-30f;
+  const float blo = truncf(__fsub_rd(tlo, m)), bhi = truncf(__fadd_ru(thi, m));
+  if (blo != bhi) return false;
+  bin = (int)blo + 1;
+  return true;
+}
+
 enum LazyFold : int {
   kFoldWangLandau = 0,  // e = (e - pair_before) + pair_after
   kFoldNested = 1,      // e = e + (pair_after - pair_before)

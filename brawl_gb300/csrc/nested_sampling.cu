@@ -172,21 +172,28 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
     if (irnd < 1) irnd = 1;
     const int8_t* src = R.walkers + (size_t)(irnd - 1) * n;
     for (int i = lane; i < n; i += 32) lat[i] = src[i];
-    // E: the walker's exact energy before the n_log logged steps;
-    // [E_lo, E_hi] contains it after them
+    // E: the walker's exact energy before the n_log logged steps; after
+    // them it lies in E + [Dlo - Rs, Dhi + Rs] quanta (Rs: the roundings of
+    // the logged updates), so the ceiling tests are integer compares against
+    // gaps taken once per exact energy
     double E = R.energies[irnd - 1];
-    double E_lo = E, E_hi = E;
+    long long Dlo = 0, Dhi = 0, Rs = 0, Eq = 0, gup = 0, gdn = 0;
     int n_log = 0;
     __syncwarp();
-    long long gup = gap_up(limit, E, S), gdn = gap_dn(limit, E, S);
-    auto flush = [&]() {
-      if (n_log == 0) return;
-      E = lazy_flush(g, V, sstart, LG, n_log, E, kFoldNested, lane);
-      if (!(E >= E_lo && E <= E_hi)) status = kStatusBandViolated;
-      E_lo = E_hi = E;
-      n_log = 0;
+    auto rebase = [&]() {
       gup = gap_up(limit, E, S);
       gdn = gap_dn(limit, E, S);
+      Eq = quanta_bound(E, S);
+      Dlo = Dhi = Rs = 0;
+    };
+    rebase();
+    auto flush = [&]() {
+      if (n_log == 0) return;
+      const double E0 = E;
+      E = lazy_flush(g, V, sstart, LG, n_log, E, kFoldNested, lane);
+      if (!in_quanta(E, E0, Dlo - Rs, Dhi + Rs, q)) status = kStatusBandViolated;
+      n_log = 0;
+      rebase();
     };
     n_acc = 0;
     const long long steps = (long long)R.n_steps + extra_steps;
@@ -215,28 +222,34 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
       ++c_steps;
       uint8_t* rec = LG.codes + (size_t)n_log * 2 * g.z;
       const int dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
-      // certainly E + dE >= ceiling: rejected without the FP64 sums
-      if ((long long)dE - band >= gup) continue;
+      // E + dE lies in E_exact + [lo, hi] quanta; rounding the sum to a double
+      // keeps it on the same side of the ceiling (a double) or of the
+      // double below it
+      long long lo = Dlo - Rs + dE - band, hi = Dhi + Rs + dE + band;
+      if (lo >= gup) continue;  // certainly at or over the ceiling: rejected
       bool logged = false;
-      if ((long long)dE + band > gdn && n_log > 0) {
+      if (hi > gdn && n_log > 0) {
         // not settled with the logged steps' interval: their exact energy
         // may settle it; this step's codes move to the log's first slot
         __syncwarp();
         flush();
         lazy_copy_slot(g, rec, LG.codes, lane);
-        if ((long long)dE - band >= gup) continue;
+        lo = (long long)dE - band;
+        hi = (long long)dE + band;
+        if (lo >= gup) continue;
       }
-      if ((long long)dE + band <= gdn) {
+      if (hi <= gdn) {
         // certainly below the ceiling: accepted, the FP64 sums deferred
         if (lane == 0) {
           LG.spec[2 * n_log] = (int8_t)p.sa;
           LG.spec[2 * n_log + 1] = (int8_t)p.sb;
         }
         ++n_log;
-        E_lo = __dadd_rd(E_lo, __dmul_rn((double)((long long)dE - band), q));
-        E_hi = __dadd_ru(E_hi, __dmul_rn((double)((long long)dE + band), q));
-        gup = gap_up(limit, E_lo, S);
-        gdn = gap_dn(limit, E_hi, S);
+        Dlo += (long long)dE - band;
+        Dhi += (long long)dE + band;
+        // the update E + delta_e rounds by at most |E + delta_e| 2^-53
+        const long long B = Eq + max(llabs(Dlo), llabs(Dhi)) + Rs;
+        Rs += (B >> 53) + 1;
         logged = true;
       } else {
         // the exact step, as the reference takes it (the log is empty)
@@ -246,9 +259,8 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
         const double delta_e = __dsub_rn(e_sw, e_un);
         const double e_new = __dadd_rn(E, delta_e);
         if (!(e_new < limit)) continue;
-        E = E_lo = E_hi = e_new;
-        gup = gap_up(limit, E, S);
-        gdn = gap_dn(limit, E, S);
+        E = e_new;
+        rebase();
       }
       ++n_acc;
       ++c_acc;

@@ -100,15 +100,25 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
 
   const double e1 = W.e1, range = W.range, f = W.wl_f;
   const int bins = W.bins, start = W.start, end = W.end;
-  const float rf = __double2float_rn(__ddiv_rn((double)bins, range));
+  const double rbins = __ddiv_rn((double)bins, range);
+  const float rf = __double2float_rn(rbins);
   const int period = W.hist_period;
   const int band = J.band;
   const double q = ldexp(1.0, -W.S);               // one fixed-point quantum
-  const double pair_bound = ldexp(1.0, 30 - W.S);   // >= 4 z max|V|: bounds |pair energy|
-  // e_ex: the reference's e_unswapped before the n_log logged moves;
-  // [e_lo, e_hi] contains it after them
+  // e_ex: the reference's e_unswapped before the n_log logged moves; after
+  // them it lies in e_ex + [Dlo - Rs, Dhi + Rs] quanta (Rs: the roundings of
+  // the logged updates), and bins follow from float offsets of t0, the bin
+  // coordinate of e_ex, taken once per exact energy
   double e_ex = (W.i0 > 0 && W.e_state) ? *W.e_state : (W.e0_src ? *W.e0_src : W.e0);
-  double e_lo = e_ex, e_hi = e_ex;
+  const float qrf = __double2float_rn(__dmul_rn(q, rbins));
+  long long Dlo = 0, Dhi = 0, Rs = 0, Eq = 0;
+  float t0 = 0.0f;
+  auto rebase = [&]() {
+    Eq = quanta_bound(e_ex, W.S);
+    t0 = __double2float_rn(__dmul_rn(__dsub_rn(e_ex, e1), rbins));
+    Dlo = Dhi = Rs = 0;
+  };
+  rebase();
   int n_log = 0;
   int ibin = wl_bin_index(e_ex, e1, range, bins);
   int status = (ibin < start || ibin > end) ? kStatusWalkerOutsideWindow : kStatusOk;
@@ -116,13 +126,14 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   DecideStats st = {0u, 0u};
   // histogram ticks at trials i with i % period == 0
   long long until = period > 0 ? period - (W.i0 % period) : -1;
-  // folds the logged moves into e_ex; their energy must be in [e_lo, e_hi]
+  // folds the logged moves into e_ex; their energy must be in the interval
   auto flush = [&]() {
     if (n_log == 0) return;
+    const double e0 = e_ex;
     e_ex = lazy_flush(g, V, sstart, LG, n_log, e_ex, kFoldWangLandau, lane);
-    if (!(e_ex >= e_lo && e_ex <= e_hi)) status = kStatusBandViolated;
-    e_lo = e_hi = e_ex;
+    if (!in_quanta(e_ex, e0, Dlo - Rs, Dhi + Rs, q)) status = kStatusBandViolated;
     n_log = 0;
+    rebase();
   };
 
   const int n_tr = (int)W.n_trials;
@@ -139,35 +150,30 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
     const bool differ = p.sa != p.sb;
     int jbin = ibin;
     bool exact_done = false;
-    double e_sw = e_ex, s_lo = e_lo, s_hi = e_hi;
+    double e_sw = e_ex;
+    long long r1 = 0;
+    int dE = 0;
     uint8_t* rec = LG.codes + (size_t)n_log * 2 * g.z;
     if (differ) {
       ++c_eval;
-      // The reference's e_swapped lies within band quanta of e_un + dE q
-      // (pair sums) plus the two roundings of e_un - p_un + p_sw, for any
-      // e_un in [e_lo, e_hi]; its bin is decided without the FP64 sums when
-      // that interval sits in one bin.
-      const int dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
-      const double lo_d = __dmul_rn((double)(dE - band), q), hi_d = __dmul_rn((double)(dE + band), q);
+      // The reference's e_swapped = (e_un - p_un) + p_sw lies within band
+      // quanta of e_un + dE q plus the two roundings, each at most 2^-53 of
+      // |e_un - p_un| <= |e_un| + 2^30 q or of |e_swapped|; its bin is
+      // decided without the FP64 sums when that interval sits in one bin.
+      dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
       bool settled = false;
       for (int pass = 0; pass < 2 && !settled; ++pass) {
-        const double w = (2.0 * fmax(fabs(e_lo), fabs(e_hi)) + fabs(lo_d) + fabs(hi_d) + pair_bound) * 2.3e-16;
-        s_lo = __dsub_rd(__dadd_rd(e_lo, lo_d), w);
-        s_hi = __dadd_ru(__dadd_ru(e_hi, hi_d), w);
-        const float tlo = __fmul_rd(__double2float_rd(__dsub_rd(s_lo, e1)), rf);
-        const float thi = __fmul_ru(__double2float_ru(__dsub_ru(s_hi, e1)), rf);
-        const float blo = truncf(__fsub_rd(tlo, fabsf(tlo) * 2.5e-7f + 1.0e-30f));
-        const float bhi = truncf(__fadd_ru(thi, fabsf(thi) * 2.5e-7f + 1.0e-30f));
-        if (blo == bhi && fabsf(tlo) < 5.0e8f && fabsf(thi) < 5.0e8f) {
-          jbin = (int)blo + 1;
-          settled = true;
-        } else if (pass == 0 && n_log > 0) {
+        const long long B = 2 * (Eq + max(llabs(Dlo), llabs(Dhi)) + Rs) + (1ll << 30) +
+                            llabs((long long)dE) + band;
+        r1 = Rs + (B >> 53) + 1;
+        settled = bin_from_quanta(t0, qrf, Dlo + dE - band - r1, Dhi + dE + band + r1, jbin);
+        if (!settled && pass == 0 && n_log > 0) {
           // the logged moves' exact energy may settle it; this move's codes
           // move to the log's first slot
           flush();
           lazy_copy_slot(g, rec, LG.codes, lane);
           rec = LG.codes;
-        } else {
+        } else if (!settled) {
           break;
         }
       }
@@ -188,16 +194,18 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
         ++n_acc;
         if (differ) {
           if (exact_done) {
-            e_ex = e_lo = e_hi = e_sw;  // the log is empty here
+            e_ex = e_sw;  // the log is empty here
+            rebase();
           } else {
-            // logged: the energy after it is in [s_lo, s_hi]
+            // logged: the energy after it is in e_ex + [Dlo - Rs, Dhi + Rs]
             if (lane == 0) {
               LG.spec[2 * n_log] = (int8_t)p.sa;
               LG.spec[2 * n_log + 1] = (int8_t)p.sb;
             }
             ++n_log;
-            e_lo = s_lo;
-            e_hi = s_hi;
+            Dlo += (long long)dE - band;
+            Dhi += (long long)dE + band;
+            Rs = r1;
           }
           if (lane == 0) {
             lat[p.ai] = (int8_t)p.sb;
