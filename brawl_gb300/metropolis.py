@@ -1,12 +1,14 @@
-"""Host driver of the Metropolis simulated annealing over the GPU chain.
+"""Host drivers of the Metropolis modes over the GPU chain.
 
-Mirrors metropolis_simulated_annealing (src/metropolis.F90:84-558): per
+simulated_annealing mirrors metropolis_simulated_annealing
+(src/metropolis.F90:84-558): per
 temperature, the optional burn-in, the sample at step 0, n_sweeps blocks of
 n_sweep_steps swap trials on the device, and after each block the energy
 (total_energy), the ASRO sample (radial_densities) and the trajectory rows.
 The per-temperature averages use the reference's arithmetic: E and E^2
 accumulated in FP64 sample by sample, n_save_* = floor(real/real) in single
-precision, C clamped at zero.
+precision, C clamped at zero.  decorrelated_samples mirrors
+metropolis_decorrelated_samples (:560-738).
 """
 from __future__ import annotations
 
@@ -96,4 +98,45 @@ def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs:
     out["traj_step"] = np.array(out["traj_step"], dtype=np.int64)
     out["traj_energy"] = np.array(out["traj_energy"])
     out["traj_asro"] = np.array(out["traj_asro"])
+    return out
+
+
+def decorrelated_samples(chain: Chain, metropolis, record_configs: bool = True):
+    """metropolis_decorrelated_samples (src/metropolis.F90:560-738) on a
+    chain whose configuration and stream are already set.  As the reference
+    does it: the burn-in (when burn_in) runs at every temperature
+    T + (j-1) delta_T in turn, then one sampling loop of n_mc_steps trials at
+    the last temperature's beta, with a sample every n_sample_steps trials --
+    the energy (full_energy) and the configuration (written as xyz by the
+    reference) -- and the acceptance counter reset at each sample.  Returns
+    the burn-in acceptances per temperature and the samples."""
+    m = metropolis
+    if m.T_steps < 1:
+        raise ValueError("decorrelated_samples needs T_steps >= 1")
+    temps = np.array([m.T + float(j) * m.delta_T for j in range(m.T_steps)])
+    out = {"temperature": temps, "burn_in_accepted": np.zeros(m.T_steps, dtype=np.int64),
+           "sample_step": [], "sample_energy": [], "sample_accepted": [], "configs": []}
+    beta = float("inf")
+    for j, temp in enumerate(temps):
+        sim_temp = temp * K_B_IN_RY
+        beta = 1.0 / sim_temp if sim_temp != 0.0 else float("inf")
+        if m.burn_in and m.n_burn_in_steps > 0:
+            out["burn_in_accepted"][j] = chain.metropolis(beta, m.n_burn_in_steps, m.nbr_swap)
+    step = 0
+    accepted = 0
+    while step < m.n_mc_steps:
+        # up to the next multiple of n_sample_steps (or the end of the loop)
+        chunk = min(m.n_sample_steps - step % m.n_sample_steps, m.n_mc_steps - step)
+        accepted += chain.metropolis(beta, chunk, m.nbr_swap)
+        step += chunk
+        if step % m.n_sample_steps == 0:
+            out["sample_step"].append(step)
+            out["sample_energy"].append(chain.total_energy())
+            out["sample_accepted"].append(accepted)
+            if record_configs:
+                out["configs"].append(chain.config())
+            accepted = 0
+    out["sample_step"] = np.array(out["sample_step"], dtype=np.int64)
+    out["sample_energy"] = np.array(out["sample_energy"])
+    out["sample_accepted"] = np.array(out["sample_accepted"], dtype=np.int64)
     return out

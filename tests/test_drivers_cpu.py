@@ -1,0 +1,87 @@
+"""Host logic of the Metropolis drivers without a GPU: the drivers run over
+a chain backed by the oracle, and must make the calls the reference's loops
+imply (src/metropolis.F90:560-738 for decorrelated_samples), checked
+against a trial-by-trial restatement of that loop."""
+from __future__ import annotations
+
+import numpy as np
+
+import brawl_gb300 as B
+from brawl_gb300 import inputs as I
+from brawl_gb300 import metropolis as M
+from oracle import oracle as O
+
+
+class OracleChain:
+    """The chain interface the drivers use, over the oracle."""
+
+    def __init__(self, mod, cfg, rng):
+        self.mod, self.cfg, self.rng = mod, cfg, rng
+
+    def metropolis(self, beta, n_trials, nbr_swap=False):
+        acc, _ = self.mod.mc_run(self.cfg, self.rng, beta, n_trials, nbr_swap)
+        return acc
+
+    def total_energy(self):
+        return self.mod.total_energy(self.cfg)
+
+    def config(self):
+        return self.cfg.copy()
+
+
+def small_system(seed):
+    rng = np.random.default_rng(seed)
+    V = np.zeros((3, 3, 2))
+    for sh in range(2):
+        a = rng.uniform(-0.05, 0.05, size=(3, 3))
+        V[:, :, sh] = (np.triu(a) + np.triu(a, 1).T) / 13.605693122
+    mod = O.OracleModel("bcc", 3, 3, 3, V)
+    r = O.OracleRng(seed)
+    conc = np.array([0.0, 1 / 3, 1 / 3, 1 / 3])
+    cfg, _ = mod.initial_setup(r, conc, np.array([18, 18, 18]))
+    return mod, cfg, r, V
+
+
+def reference_loop(mod, cfg, rng, m):
+    """metropolis_decorrelated_samples, one trial at a time."""
+    beta = None
+    burn = []
+    for j in range(m.T_steps):
+        temp = m.T + float(j) * m.delta_T
+        beta = 1.0 / (temp * B.K_B_IN_RY)
+        acc = 0
+        if m.burn_in:
+            for _ in range(m.n_burn_in_steps):
+                acc += mod.mc_run(cfg, rng, beta, 1, m.nbr_swap)[0]
+        burn.append(acc)
+    steps, energies, accs, cfgs = [], [], [], []
+    acc = 0
+    for i in range(1, m.n_mc_steps + 1):
+        acc += mod.mc_run(cfg, rng, beta, 1, m.nbr_swap)[0]
+        if i % m.n_sample_steps == 0:
+            steps.append(i)
+            energies.append(mod.total_energy(cfg))
+            accs.append(acc)
+            cfgs.append(cfg.copy())
+            acc = 0
+    return burn, steps, energies, accs, cfgs
+
+
+def test_decorrelated_samples_host_logic():
+    m = I.MetropolisParams(mode="decorrelated_samples", n_mc_steps=2300, n_sample_steps=300,
+                           burn_in=True, n_burn_in_steps=150, T=1200.0, T_steps=3, delta_T=-400.0)
+    mod, cfg, r, _ = small_system(7)
+    # the same start for both: copy the configuration and the stream
+    cfg_a, cfg_b = cfg.copy(), cfg.copy()
+    ra, rb = O.OracleRng(1), O.OracleRng(1)
+    ra.set_state_words(r.state_words())
+    rb.set_state_words(r.state_words())
+    burn, steps, energies, accs, cfgs = reference_loop(mod, cfg_a, ra, m)
+    out = M.decorrelated_samples(OracleChain(mod, cfg_b, rb), m)
+    assert list(out["burn_in_accepted"]) == burn
+    assert list(out["sample_step"]) == steps == [300 * k for k in range(1, 8)]
+    assert list(out["sample_energy"]) == energies
+    assert list(out["sample_accepted"]) == accs
+    assert all(np.array_equal(a, b) for a, b in zip(out["configs"], cfgs))
+    assert np.array_equal(cfg_a, cfg_b)  # the 200 trials after the last sample ran too
+    assert np.array_equal(ra.state_words(), rb.state_words())

@@ -329,3 +329,28 @@ def test_invalid_inputs_return_status():
         ch.set_config(bad)          # occupied sites must hold a species
     with pytest.raises(B.BrawlError):
         ch.initial_setup(np.array([0.0, 0.0, 0.0]))   # counts cannot reach n_atoms
+
+
+@pytest.mark.parametrize("nbr_swap", [False, True])
+def test_decorrelated_samples_match_oracle(nbr_swap):
+    """metropolis_decorrelated_samples through the C ABI against the
+    reference's loop on the oracle, trial by trial: burn-in acceptances,
+    sampled energies, acceptances and configurations, final stream."""
+    from tests.test_drivers_cpu import reference_loop, small_system
+    m = I.MetropolisParams(mode="decorrelated_samples", n_mc_steps=5000, n_sample_steps=700,
+                           burn_in=True, n_burn_in_steps=400, T=1500.0, T_steps=4, delta_T=-300.0,
+                           nbr_swap=nbr_swap)
+    mod, cfg, r, V = small_system(11)
+    ch = B.Chain(B.Setup("bcc", 3, 3, 3, 3, 2), V)
+    ch.set_config(cfg)
+    ch.set_rng_state(r.state_words())
+    burn, steps, energies, accs, cfgs = reference_loop(mod, cfg, r, m)
+    out = anneal.decorrelated_samples(ch, m)
+    assert list(out["burn_in_accepted"]) == burn
+    assert list(out["sample_step"]) == steps
+    assert list(out["sample_energy"]) == energies
+    assert list(out["sample_accepted"]) == accs
+    assert all(np.array_equal(a, b) for a, b in zip(out["configs"], cfgs))
+    g = O.OracleRng(1)
+    g.set_state_words(ch.rng_state())
+    assert [g.uniform() for _ in range(700)] == [r.uniform() for _ in range(700)]
