@@ -175,12 +175,16 @@ __device__ __forceinline__ void halo_write_pair(const HaloGeom& H, int8_t* lat_p
 // a (minimum-image displacement within the largest offsets on every axis).
 __device__ __forceinline__ bool pair_near(const Geom& g, const HaloGeom& H, int ax, int ay,
                                           int az, int bx, int by, int bz) {
-  int dx = bx - ax, dy = by - ay, dz = bz - az;
-  const int W1 = 2 * g.n1, W2 = 2 * g.n2, W3 = 2 * g.n3;
+  // z first: most pairs are already apart there
+  int dz = bz - az;
+  const int W3 = 2 * g.n3;
+  dz = dz > g.n3 ? dz - W3 : (dz < -g.n3 ? dz + W3 : dz);
+  if (abs(dz) > H.dmz) return false;
+  int dx = bx - ax, dy = by - ay;
+  const int W1 = 2 * g.n1, W2 = 2 * g.n2;
   dx = dx > g.n1 ? dx - W1 : (dx < -g.n1 ? dx + W1 : dx);
   dy = dy > g.n2 ? dy - W2 : (dy < -g.n2 ? dy + W2 : dy);
-  dz = dz > g.n3 ? dz - W3 : (dz < -g.n3 ? dz + W3 : dz);
-  return abs(dx) <= H.dmx && abs(dy) <= H.dmy && abs(dz) <= H.dmz;
+  return abs(dx) <= H.dmx && abs(dy) <= H.dmy;
 }
 
 // Per-lane entry plan of the halo tier: for entry j of this lane's site, the

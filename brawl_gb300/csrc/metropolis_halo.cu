@@ -121,11 +121,16 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   // 32-bit tallies (a launch runs fewer than 2^31 trials per chain, see
   // launch_metropolis_halo); the words drawn follow from them: n_base per
   // trial plus the uniforms
-  unsigned int b_eval = 0, b_acc = 0, b_exp = 0, b_exact = 0;
+  unsigned int b_eval = 0, b_acc = 0, b_exact = 0;
   unsigned int c_fp64 = 0, c_cr = 0;
   const int nt = (int)n_trials;
+  // the uniforms drawn follow from the words consumed: n_base a trial plus
+  // one per uniform, counted through the ring's generated blocks
+  const int avail0 = R.avail;
+  unsigned int gens = 0;
 
   for (int t = 0; t < nt; ++t) {
+    gens += R.avail < n_peek ? 1u : 0u;
     ring_ensure(mt, tbuf, R, n_peek, lane);
     const int wb = tb + R.idx;
     SitePair p;
@@ -142,16 +147,15 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
     if (p.sa != p.sb) {
       ++b_eval;
       const bool near = pair_near(g, H, p.ax, p.ay, p.az, p.bx, p.by, p.bz);
-      p.ai = p.az * g.sz + Ya * g.sy + Xa;
-      p.bi = p.bz * g.sz + Yb * g.sy + Xb;
       int dE;
       if (!near) {
         const bool par_a = bcc ? (p.az & 1) : (p.ax & 1);
         const bool par_b = bcc ? (p.bz & 1) : (p.bx & 1);
         dE = halo_delta<NJ>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
       } else {
-        dE = halo_delta_general(Jg, (int)L.ents, I_off, L.F_off, hl, p.ax, p.ay, p.az, p.ai,
-                                p.bx, p.by, p.bz, p.bi, p.sa, p.sb, lane);
+        dE = halo_delta_general(Jg, (int)L.ents, I_off, L.F_off, hl, p.ax, p.ay, p.az,
+                                p.az * g.sz + Ya * g.sy + Xa, p.bx, p.by, p.bz,
+                                p.bz * g.sz + Yb * g.sy + Xb, p.sa, p.sb, lane);
       }
       const uint32_t wu = s_u32[wb + n_base];
       accept = -1;
@@ -163,20 +167,23 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
       }
       if (accept < 0) {
         ++b_exact;
-        const int r = halo_exact_decision(Jg, hl, V, ents, sstart, p.ax, p.ay, p.az, p.ai, p.bx,
-                                          p.by, p.bz, p.bi, p.sa, p.sb, lane, wu);
+        const int r = halo_exact_decision(Jg, hl, V, ents, sstart, p.ax, p.ay, p.az,
+                                          p.az * g.sz + Ya * g.sy + Xa, p.bx, p.by, p.bz,
+                                          p.bz * g.sz + Yb * g.sy + Xb, p.sa, p.sb, lane, wu);
         accept = r & 1;
         consumed = (r & 2) ? n_base + 1 : n_base;
         c_fp64 += (r >> 2) & 1;
         c_cr += (r >> 3) & 1;
       }
-      if (consumed > n_base) ++b_exp;
       if (accept) halo_write_pair(H, lat, lane, p.az, Ya, Xa, p.sb, p.bz, Yb, Xb, p.sa);
     }
     b_acc += accept;
     ring_consume(R, consumed);
   }
-  const unsigned long long c_eval = b_eval, c_acc = b_acc, c_exp = b_exp, c_exact = b_exact;
+  const unsigned long long words =
+      (unsigned long long)(avail0 - R.avail) + (unsigned long long)kMTN * gens;
+  const unsigned long long c_exp = words - (unsigned long long)n_base * (unsigned long long)nt;
+  const unsigned long long c_eval = b_eval, c_acc = b_acc, c_exact = b_exact;
   const unsigned long long c_draws = (unsigned long long)n_base * (unsigned long long)n_trials + c_exp;
 
   // ---- write back ---------------------------------------------------------
