@@ -353,7 +353,7 @@ struct brawl_batch {
   // chains run by the halo kernel, and its shared-memory size / unrolling
   std::vector<int> halo;
   uint32_t halo_smem = 0;
-  int halo_max_z = 0;
+  int halo_min_z = 0, halo_max_z = 0;
   std::vector<ChainJob> staged;          // jobs in launch order
   int n_halo_launch = 0;
   std::vector<unsigned long long> last_counters;
@@ -487,7 +487,7 @@ int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accept
   if (serial) {
     for (int k = 0; k < n; ++k) {
       if (k < nh)
-        launch_halo_chains(b->d_jobs + k, 1, b->halo_smem, b->halo_max_z, b->spec_nc, b->max_optin,
+        launch_halo_chains(b->d_jobs + k, 1, b->halo_smem, b->halo_min_z, b->halo_max_z, b->spec_nc, b->max_optin,
                            stream);
       else
         launch_metropolis(b->d_jobs + k, 1, b->smem_lat, b->use_D, b->smem_bytes, b->max_z,
@@ -497,7 +497,8 @@ int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accept
     }
   } else {
     if (nh > 0)
-      launch_halo_chains(b->d_jobs, nh, b->halo_smem, b->halo_max_z, b->spec_nc, b->max_optin, stream);
+      launch_halo_chains(b->d_jobs, nh, b->halo_smem, b->halo_min_z, b->halo_max_z, b->spec_nc,
+                         b->max_optin, stream);
     if (n - nh > 0)
       launch_metropolis(b->d_jobs + nh, n - nh, b->smem_lat, b->use_D, b->smem_bytes, b->max_z,
                         stream);
@@ -564,6 +565,7 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
     if (ok && halo_layout(m.g, H).total <= (uint32_t)max_optin) {
       b->halo[c] = 1;
       b->halo_smem = std::max(b->halo_smem, halo_layout(m.g, H).total);
+      b->halo_min_z = b->halo_max_z == 0 ? (int)m.g.z : std::min(b->halo_min_z, (int)m.g.z);
       b->halo_max_z = std::max(b->halo_max_z, (int)m.g.z);
       continue;
     }

@@ -171,6 +171,26 @@ __device__ __forceinline__ void halo_write_pair(const HaloGeom& H, int8_t* lat_p
   __syncwarp();
 }
 
+// draw_site for fcc and bcc, also giving the site's compact (Y', X') =
+// (y >> ys, x >> 1) without going through the doubled coordinates.
+__device__ __forceinline__ void draw_site_halo(const Geom& g, bool bcc, uint32_t w0, uint32_t w1,
+                                               uint32_t w2, int& x, int& y, int& z, int& Yc,
+                                               int& Xc) {
+  z = (int)umulhi32(w0, 2u * g.n3);
+  if (bcc) {
+    const int p = z & 1;
+    Xc = (int)umulhi32(w1, (uint32_t)g.n1);
+    Yc = (int)umulhi32(w2, (uint32_t)g.n2);
+    x = 2 * Xc + p;
+    y = 2 * Yc + p;
+  } else {
+    x = (int)umulhi32(w1, 2u * g.n1);
+    y = 2 * (int)umulhi32(w2, (uint32_t)g.n2) + ((x + z) & 1);
+    Yc = y;
+    Xc = x >> 1;
+  }
+}
+
 // Conservative test that site b may be within the interaction range of site
 // a (minimum-image displacement within the largest offsets on every axis).
 __device__ __forceinline__ bool pair_near(const Geom& g, const HaloGeom& H, int ax, int ay,
@@ -223,8 +243,9 @@ __device__ __forceinline__ void make_halo_plan(const Geom& g, const HaloGeom& H,
 }
 
 // Fixed-point swap delta for a pair that is not near: neighbours never
-// include the partner or the site itself.
-template <int NJ>
+// include the partner or the site itself.  FULL: every lane entry is a
+// neighbour (z = 16 NJ), so none is masked.
+template <int NJ, bool FULL = false>
 __device__ __forceinline__ int halo_delta(const Geom& g, int lat_off, int D_off_abs,
                                           const HaloPlan<NJ>& P, int base_a, int base_b, int par_a,
                                           int par_b, int sa, int sb, int lane) {
@@ -241,7 +262,7 @@ __device__ __forceinline__ int halo_delta(const Geom& g, int lat_off, int D_off_
   for (int j = 0; j < NJ; ++j) {
     const int s = s_i8[base + (par ? P.d1[j] : P.d0[j])];
     const int t = s_i32[rowD + P.shp[j] + s];
-    acc += ((P.valid >> j) & 1u) ? t : 0;
+    acc += (FULL || ((P.valid >> j) & 1u)) ? t : 0;
   }
   return __reduce_add_sync(kFull, acc);
 }

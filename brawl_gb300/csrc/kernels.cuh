@@ -83,10 +83,11 @@ void launch_metropolis_spec(const ChainJob* d_jobs, int n_jobs, uint32_t smem_by
 uint32_t spec_static_smem(int nc);
 // The halo chains: speculative rounds of nc trials when nc >= 2 and the
 // slots fit beside the dynamic shared memory, the one-trial kernel otherwise.
-void launch_halo_chains(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z, int nc,
-                        int max_optin, cudaStream_t stream);
-void launch_metropolis_halo(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z,
-                            cudaStream_t stream);
+// min_z/max_z: the smallest and largest neighbour count of the chains.
+void launch_halo_chains(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int min_z, int max_z,
+                        int nc, int max_optin, cudaStream_t stream);
+void launch_metropolis_halo(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int min_z,
+                            int max_z, cudaStream_t stream);
 
 // Metropolis swap trials, one warp (CTA) per chain; max_z is the largest
 // neighbour count in the batch (it selects the unrolling of the fast tier).

@@ -68,7 +68,7 @@ __device__ __noinline__ int halo_exact_decision(const ChainJob* __restrict__ Jg,
   return acc | 2 | (st.fp64 ? 4 : 0) | (st.cr ? 8 : 0);
 }
 
-template <int NJ>
+template <int NJ, bool FULL>
 __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __restrict__ jobs) {
   extern __shared__ __align__(16) unsigned char smem[];
   extern __shared__ uint32_t s_u32[];
@@ -134,10 +134,15 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
     ring_ensure(mt, tbuf, R, n_peek, lane);
     const int wb = tb + R.idx;
     SitePair p;
-    draw_site(g, s_u32[wb], s_u32[wb + 1], s_u32[wb + 2], p.ax, p.ay, p.az);
-    if (nbr_swap) draw_nbr(g, s_u32[wb + 3], p.ax, p.ay, p.az, p.bx, p.by, p.bz);
-    else draw_site(g, s_u32[wb + 3], s_u32[wb + 4], s_u32[wb + 5], p.bx, p.by, p.bz);
-    const int Ya = p.ay >> ys, Xa = p.ax >> 1, Yb = p.by >> ys, Xb = p.bx >> 1;
+    int Ya, Xa, Yb, Xb;
+    draw_site_halo(g, bcc, s_u32[wb], s_u32[wb + 1], s_u32[wb + 2], p.ax, p.ay, p.az, Ya, Xa);
+    if (nbr_swap) {
+      draw_nbr(g, s_u32[wb + 3], p.ax, p.ay, p.az, p.bx, p.by, p.bz);
+      Yb = p.by >> ys;
+      Xb = p.bx >> 1;
+    } else {
+      draw_site_halo(g, bcc, s_u32[wb + 3], s_u32[wb + 4], s_u32[wb + 5], p.bx, p.by, p.bz, Yb, Xb);
+    }
     const int pa = H.origin + p.az * H.SZ + Ya * H.SY + Xa;
     const int pb = H.origin + p.bz * H.SZ + Yb * H.SY + Xb;
     p.sa = s_i8[lat_off + pa];
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
       if (!near) {
         const bool par_a = bcc ? (p.az & 1) : (p.ax & 1);
         const bool par_b = bcc ? (p.bz & 1) : (p.bx & 1);
-        dE = halo_delta<NJ>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
+        dE = halo_delta<NJ, FULL>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
       } else {
         dE = halo_delta_general(Jg, (int)L.ents, I_off, L.F_off, hl, p.ax, p.ay, p.az,
                                 p.az * g.sz + Ya * g.sy + Xa, p.bx, p.by, p.bz,
@@ -204,24 +209,30 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   }
 }
 
-template <int NJ>
+template <int NJ, bool FULL>
 static void launch_halo_nj(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes,
                            cudaStream_t stream) {
-  cudaFuncSetAttribute(metropolis_halo_kernel<NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(metropolis_halo_kernel<NJ, FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes);
-  BRAWL_CARVEOUT(metropolis_halo_kernel<NJ>);
-  metropolis_halo_kernel<NJ><<<n_jobs, 32, smem_bytes, stream>>>(d_jobs);
+  BRAWL_CARVEOUT((metropolis_halo_kernel<NJ, FULL>));
+  metropolis_halo_kernel<NJ, FULL><<<n_jobs, 32, smem_bytes, stream>>>(d_jobs);
 }
 
-void launch_metropolis_halo(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z,
-                            cudaStream_t stream) {
+void launch_metropolis_halo(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int min_z,
+                            int max_z, cudaStream_t stream) {
   if (n_jobs <= 0) return;
-  switch (lane_entries_for(max_z)) {
-    case 2: launch_halo_nj<2>(d_jobs, n_jobs, smem_bytes, stream); break;
-    case 4: launch_halo_nj<4>(d_jobs, n_jobs, smem_bytes, stream); break;
-    case 6: launch_halo_nj<6>(d_jobs, n_jobs, smem_bytes, stream); break;
-    case 8: launch_halo_nj<8>(d_jobs, n_jobs, smem_bytes, stream); break;
-    default: launch_halo_nj<11>(d_jobs, n_jobs, smem_bytes, stream); break;
+  const int nj = lane_entries_for(max_z);
+  // every chain with z = 64 (bcc, 6 shells): no lane entry to mask
+  const bool full = min_z == max_z && max_z == 16 * nj;
+  switch (nj) {
+    case 2: launch_halo_nj<2, false>(d_jobs, n_jobs, smem_bytes, stream); break;
+    case 4:
+      if (full) launch_halo_nj<4, true>(d_jobs, n_jobs, smem_bytes, stream);
+      else launch_halo_nj<4, false>(d_jobs, n_jobs, smem_bytes, stream);
+      break;
+    case 6: launch_halo_nj<6, false>(d_jobs, n_jobs, smem_bytes, stream); break;
+    case 8: launch_halo_nj<8, false>(d_jobs, n_jobs, smem_bytes, stream); break;
+    default: launch_halo_nj<11, false>(d_jobs, n_jobs, smem_bytes, stream); break;
   }
 }
 

@@ -360,12 +360,12 @@ static void launch_spec_nc(const ChainJob* d_jobs, int n_jobs, uint32_t smem_byt
   }
 }
 
-void launch_halo_chains(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z, int nc,
-                        int max_optin, cudaStream_t stream) {
+void launch_halo_chains(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int min_z, int max_z,
+                        int nc, int max_optin, cudaStream_t stream) {
   if (nc >= 2 && smem_bytes + spec_static_smem(nc) <= (uint32_t)max_optin)
     launch_metropolis_spec(d_jobs, n_jobs, smem_bytes, max_z, nc, stream);
   else
-    launch_metropolis_halo(d_jobs, n_jobs, smem_bytes, max_z, stream);
+    launch_metropolis_halo(d_jobs, n_jobs, smem_bytes, min_z, max_z, stream);
 }
 
 void launch_metropolis_spec(const ChainJob* d_jobs, int n_jobs, uint32_t smem_bytes, int max_z, int nc,

@@ -583,7 +583,7 @@ int launch_anneal(brawl_server* S, Pipe& P) {
   std::vector<EnergyJob> ej;
   P.launched.clear();
   uint32_t halo_smem = 0, lat_smem = 0, glob_smem = 0;
-  int halo_z = 0, table_z = 0;
+  int halo_min_z = 0, halo_z = 0, table_z = 0;
   bool use_D = true;
   SV_TRY(grow(P.d_tns, P.tns_cap, std::max<size_t>(P.jobs.size(), 1), P.s));
   const double t_round = round_ns(S, P.jobs);
@@ -603,6 +603,7 @@ int launch_anneal(brawl_server* S, Pipe& P) {
       }
       if (pass == 0) {
         halo_smem = std::max(halo_smem, j->slot.halo_smem);
+        halo_min_z = halo_z == 0 ? (int)c.g.z : std::min(halo_min_z, (int)c.g.z);
         halo_z = std::max(halo_z, (int)c.g.z);
       } else {
         lat_smem = std::max(lat_smem, j->slot.smem_lat_bytes);
@@ -616,7 +617,8 @@ int launch_anneal(brawl_server* S, Pipe& P) {
   const int n = (int)staged.size();
   SV_TRY(grow(P.d_chain, P.chain_cap, (size_t)n, P.s));
   SV_TRY(stage_copy(P, P.d_chain, staged.data(), n * sizeof(ChainJob)));
-  if (nh > 0) launch_halo_chains(P.d_chain, nh, halo_smem, halo_z, kDefaultSpeculation, S->max_optin, P.s);
+  if (nh > 0)
+    launch_halo_chains(P.d_chain, nh, halo_smem, halo_min_z, halo_z, kDefaultSpeculation, S->max_optin, P.s);
   if (n - nh > 0) {
     const bool smem_lat = lat_smem <= (uint32_t)S->max_optin;
     launch_metropolis(P.d_chain + nh, n - nh, smem_lat, use_D, smem_lat ? lat_smem : glob_smem, table_z, P.s);

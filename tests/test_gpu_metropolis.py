@@ -245,6 +245,36 @@ def test_batch_equals_individual_and_serial():
         assert energies[k] == e
 
 
+def test_batched_replica_shape_matches_oracle():
+    """The batched-replica workload's shape in small: bcc chains of several
+    sizes, 4 species, 6 shells (every lane entry a neighbour), log-spaced
+    temperatures, seeds 110179 + 11 r, in one launch; each chain equals the
+    oracle."""
+    rng = np.random.default_rng(64)
+    V = random_V(rng, 4, 6)
+    Ls = [3, 4, 5, 4, 6, 3, 5, 7]
+    chains, expect = [], []
+    for r, L in enumerate(Ls):
+        T = 100.0 * 30.0 ** (r / (len(Ls) - 1))
+        setup = B.Setup("bcc", L, L, L, 4, 6)
+        seed = 110179 + 11 * r
+        chains.append(dict(setup=setup, V=V, seed=seed, beta=1.0 / (T * B.K_B_IN_RY),
+                           species_concentrations=conc_vector(4)))
+        trials = 10 * setup.n_atoms
+        mod, cfg, r_, acc, c, _ = _oracle_run("bcc", (L, L, L), V, seed, T, trials, False,
+                                              conc_vector(4), None)
+        expect.append((trials, cfg, acc, c))
+    b = B.Batch(chains)
+    acc = b.metropolis(np.array([e[0] for e in expect]))
+    cnt = b.counters()
+    for k, (t, cfg, a, c) in enumerate(expect):
+        assert acc[k] == a, Ls[k]
+        assert np.array_equal(b.config(k), cfg), Ls[k]
+        row = dict(zip(B.COUNTER_NAMES, cnt[k]))
+        # exp_tests is counted from the words the kernel consumed
+        assert row["evaluated"] == c.evaluated and row["exp_tests"] == c.exp_tests
+
+
 def test_initial_setup_modes_match_oracle():
     rng = np.random.default_rng(11)
     for lat, n, ns in (("fcc", (4, 3, 2), 5), ("bcc", (5, 5, 5), 3), ("simple_cubic", (2, 2, 3), 4)):
