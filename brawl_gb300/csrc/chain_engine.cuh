@@ -624,6 +624,29 @@ __device__ __forceinline__ int fast_exp_decision(const ChainJob& J, int dE, uint
   return -1;
 }
 
+// The base-2 filter below with the hardware 2^x (ex2.approx, whose error is
+// far inside the 4e-6 relative allowed for it here) and the per-chain part of
+// the margin taken once: c0 = 1.01 beta_band + 4.5e-6 when that is under
+// 0.0099, else +inf (every test undecided).  Only x2 in [-57.5, 0] is
+// decided with 2^x2; below, u = w 2^-32 >= 2^-32 is above 2^x2 for w > 0.
+__device__ __forceinline__ float exp2_filter_c0(float beta_band) {
+  const float c0 = beta_band * 1.01f + 4.5e-6f;
+  return c0 < 0.0099f ? c0 : INFINITY;
+}
+
+__device__ __forceinline__ int fast_ex2_decision(float nbql2, float c0, int dE, uint32_t w) {
+  const float x2 = __fmul_rn(nbql2, __int2float_rn(dE));
+  if (!(x2 >= -57.5f && x2 <= 0.0f)) return (x2 < -57.5f && w != 0u && c0 < 1.0f) ? 0 : -1;
+  const float M = __fmaf_rn(-x2, 1.5e-7f, c0);
+  float e;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x2));
+  const float thr = __fmul_rn(e, 4294967296.0f);
+  const float wf = __uint2float_rn(w);
+  if (wf < __fmul_rn(thr, 1.0f - M)) return 1;
+  if (wf > __fmul_rn(thr, 1.0f + M)) return 0;
+  return -1;
+}
+
 // The same filter in the base-2 domain: x2 = -beta*q*log2(e)*dE, 2^x2 with
 // exp2f (<= 2 ulp).  The argument's float rounding (3 roundings, relative
 // 1.8e-7 of |x2|, i.e. 1.25e-7 |x2| relative on 2^x2), the band term and the

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   const int ys = g.ys;
   const int nbr_swap = Jg->nbr_swap;
   const int band = Jg->band;
-  const float bql2 = Jg->beta_q_l2, bband = Jg->beta_band;
+  const float nbql2 = -Jg->beta_q_l2, c0 = exp2_filter_c0(Jg->beta_band);
   const int64_t n_trials = Jg->n_trials;
   const int n_peek = nbr_swap ? 5 : 7;
   const int n_base = nbr_swap ? 4 : 6;
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
         accept = 1;
       } else if (dE > band) {
         consumed = n_base + 1;
-        accept = fast_exp2_decision(bql2, bband, dE, wu);
+        accept = fast_ex2_decision(nbql2, c0, dE, wu);
       }
       if (accept < 0) {
         ++b_exact;
