@@ -276,6 +276,87 @@ def serving_leg(args) -> dict:
     }
 
 
+def walker_legs(args) -> dict:
+    """Wang-Landau and nested-sampling throughput at the shapes of the
+    reference's WL and NS workloads (seeded synthetic inputs).  Both APIs
+    block until the device is done, so each leg is timed on the host around
+    its calls, with the device synchronised on both sides.
+
+    * WL: bcc 12^3, 4 species, 4 shells, V uniform +-0.05 eV, 128 walkers
+      (32 groups of 4 averaged together) from random configurations, each
+      in a 1000-bin window around those configurations' energies, wl_f = 1;
+      sweeps() calls of 10^4 trials per walker (the exchange interval).
+    * NS: fcc 6^3, 5 species, 3 shells, V uniform +-0.08 eV, K = 1024
+      walkers, 2000-step walks; a bounded sample of iterations.
+    """
+    import torch
+    import brawl_gb300 as B
+    from brawl_gb300 import serving as SV
+    out = {}
+    if "wl" in args.walker_legs:
+        rng = np.random.default_rng(20261)
+        ns, nsh, L, nw, bins = 4, 4, 12, 128, 1000
+        V = SV.symmetric_V(rng, ns, nsh, 0.05)
+        setup = B.Setup("bcc", L, L, L, ns, nsh)
+        conc = np.array([0.0] + [0.25] * 4)
+        tmp = B.Batch([dict(setup=setup, V=V, seed=110179 + 11 * k, beta=0.0, species_concentrations=conc)
+                       for k in range(nw)])
+        cfgs = [tmp.config(k) for k in range(nw)]
+        E = tmp.total_energy()
+        tmp.close()
+        c, hw = float(E.mean()), float(np.abs(E - E.mean()).max() * 1.2 + 1e-3)
+        edges = (c - hw) + np.arange(bins + 1) * (2 * hw / bins)
+        walkers = [dict(setup=setup, V=V, seed=110179 + 11 * k, config=cfgs[k], start_idx=1, end_idx=bins,
+                        window=k // 4) for k in range(nw)]
+        wl = B.WangLandauWalkers(walkers, edges)
+        n, calls = 10000, args.wl_calls
+        period = int(0.02 * float(np.float32(setup.n_atoms)))
+        wl.sweeps(n, 1.0, period)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            wl.sweeps(n, 1.0, period)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        cnt = {}
+        for w in range(nw):
+            for k, v in wl.counters(w).items():
+                cnt[k] = cnt.get(k, 0) + int(v)
+        wl.close()
+        out["wang_landau"] = {
+            "metric": "WL trials/s", "value": nw * n * calls / dt, "unit": "trials/s",
+            "workload": "bcc 12^3, 4 species, 4 shells, 128 walkers, 1000-bin windows, "
+                        f"{calls} sweeps() calls of 10^4 trials per walker",
+            "us_per_trial_per_walker": dt / (n * calls) * 1e6,
+            "accepted_fraction": cnt["accepted"] / max(1, cnt["trials"]),
+            "exact_now_fraction": cnt["exact_path"] / max(1, cnt["evaluated"]),
+        }
+    if "ns" in args.walker_legs:
+        rng = np.random.default_rng(20263)
+        ns, nsh = 5, 3
+        V = SV.symmetric_V(rng, ns, nsh, 0.08)
+        setup = B.Setup("fcc", 6, 6, 6, ns, nsh)
+        conc = np.array([0.0] + [0.2] * 5)
+        run = B.NestedSampling([dict(setup=setup, V=V, seed=7, n_walkers=1024, n_steps=2000,
+                                     species_concentrations=conc)])
+        run.iterate(5)
+        c0 = run.counters(0)["trials"]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run.iterate(args.ns_iterations)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        steps = run.counters(0)["trials"] - c0
+        run.close()
+        out["nested_sampling"] = {
+            "metric": "NS walk steps/s", "value": steps / dt, "unit": "steps/s",
+            "workload": f"fcc 6^3, 5 species, 3 shells, K = 1024, 2000-step walks, "
+                        f"{args.ns_iterations} iterations after 5",
+            "iterations_per_s": args.ns_iterations / dt,
+        }
+    return out
+
+
 def max_over_ranks(x: float, world: int, device=None) -> float:
     """The largest x over the ranks (the job's time is its slowest rank's)."""
     if world <= 1:
@@ -342,6 +423,12 @@ def main() -> int:
     ap.add_argument("--serve-L-max", type=int, default=16)
     ap.add_argument("--serve-sweeps-max", type=int, default=500)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--walker-legs", default="wl,ns",
+                    help="Wang-Landau / nested-sampling legs to run (wl, ns; empty for none)")
+    ap.add_argument("--walker-legs-only", action="store_true",
+                    help="run only the walker legs and print their JSON")
+    ap.add_argument("--wl-calls", type=int, default=5)
+    ap.add_argument("--ns-iterations", type=int, default=50)
     ap.add_argument("--speculation", type=int, default=0,
                     help="trials per speculative round of the Metropolis kernel (0: library default)")
     args = ap.parse_args()
@@ -350,6 +437,13 @@ def main() -> int:
     world, rank, local = dist_setup()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+
+    args.walker_legs = [x for x in args.walker_legs.split(",") if x]
+    if args.walker_legs_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps(walker_legs(args)))
+        return 0
 
     wl = make_workload(args.replicas, rank=rank)
     # CPU baseline workers first: spawned before any CUDA call
@@ -477,6 +571,7 @@ def main() -> int:
     serving = None
     if rank == 0 and world == 1 and not args.no_serve and args.serve_jobs > 0:
         serving = serving_leg(args)
+    walkers = walker_legs(args) if rank == 0 and world == 1 and args.walker_legs else {}
 
     if rank == 0:
         line = {
@@ -503,6 +598,8 @@ def main() -> int:
                           "sample": f"{len(sample)} replicas, 1 sweep each, one launch per replica"},
             "batched_over_plain": value / plain_value,
             "serving": serving,
+            "wang_landau": walkers.get("wang_landau"),
+            "nested_sampling": walkers.get("nested_sampling"),
             "clocks": clk,
             "gpu_launches": args.steps,
             "counters": {"trials": T_all, "evaluated": T_eval, "draws": draws,
