@@ -276,6 +276,53 @@ def serving_leg(args) -> dict:
     }
 
 
+# neighbours within the first k shells (k = 1, 2, ...)
+Z_CUMULATIVE = {"bcc": (8, 14, 26, 50, 58, 64, 88, 112, 136, 168), "fcc": (12, 18, 42, 54, 78, 86)}
+
+
+def _wl_cpu(setup, V, cfg, edges, bins, period, seconds: float = 3.0) -> dict:
+    """The oracle's sweeps() for one walker on one host core, a bounded
+    sample of about `seconds`."""
+    from oracle import oracle as O
+    mod = O.OracleModel("bcc", *setup.n, V)
+    cfg = np.ascontiguousarray(cfg, dtype=np.int8).copy()
+    rng = O.OracleRng(110179)
+    lng = np.zeros(bins)
+    hist = np.zeros(bins)
+    e = mod.total_energy(cfg)
+    n = 20000
+    t0 = time.perf_counter()
+    _, e, _ = mod.wl_sweep(cfg, rng, edges, lng, hist, e, bins, 1, bins, n, 1.0, period)
+    est = n / max(1e-6, time.perf_counter() - t0)
+    n2 = max(n, int(est * seconds))
+    t0 = time.perf_counter()
+    mod.wl_sweep(cfg, rng, edges, lng, hist, e, bins, 1, bins, n2, 1.0, period)
+    dt = time.perf_counter() - t0
+    return {"value": n2 / dt, "unit": "trials/s", "cores": 1, "kind": "port",
+            "sample": f"one walker, {n2} trials of sweeps() on the oracle, {dt:.1f} s"}
+
+
+def _ns_cpu(V, conc, seconds: float = 3.0) -> dict:
+    """The oracle's nested-sampling run (same shape) on one host core: the
+    iterations' walks after the walkers are set up, a bounded sample."""
+    from oracle import oracle as O
+    mod = O.OracleModel("fcc", 6, 6, 6, V)
+    t0 = time.perf_counter()
+    mod.ns_run(O.OracleRng(7), conc, None, 1024, 2000, 1)
+    t1 = time.perf_counter()
+    mod.ns_run(O.OracleRng(7), conc, None, 1024, 2000, 3)
+    t2 = time.perf_counter()
+    per_iter = max(1e-6, (t2 - t1 - (t1 - t0)) / 2.0)
+    m = int(min(400, max(3, seconds / per_iter)))
+    t3 = time.perf_counter()
+    mod.ns_run(O.OracleRng(7), conc, None, 1024, 2000, m + 1)
+    dt = time.perf_counter() - t3 - (t1 - t0)
+    # fewer than K/2 iterations: every walk is exactly 2000 steps
+    return {"value": m * 2000 / dt, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"K = 1024, {m} iterations of 2000-step walks on the oracle "
+                      f"(set-up and first iteration subtracted), {dt:.1f} s"}
+
+
 def walker_legs(args) -> dict:
     """Wang-Landau and nested-sampling throughput at the shapes of the
     reference's WL and NS workloads (seeded synthetic inputs).  Both APIs
@@ -318,11 +365,19 @@ def walker_legs(args) -> dict:
             wl.sweeps(n, 1.0, period)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        cnt = {}
+        c0 = {}
         for w in range(nw):
             for k, v in wl.counters(w).items():
-                cnt[k] = cnt.get(k, 0) + int(v)
+                c0[k] = c0.get(k, 0) + int(v)
         wl.close()
+        # the timed calls' share of the counters (the warm-up call is the other)
+        cnt = {k: v * calls // (calls + 1) for k, v in c0.items()}
+        z = Z_CUMULATIVE["bcc"][nsh - 1]
+        # algorithmic bytes: every trial reads its two species and the pair's
+        # z neighbours with one V row each (2 + 2z + 16z), an evaluated trial
+        # the same again after the swap (16z), 4 bytes per stream word
+        alg = cnt["trials"] * (2 + 18 * z) + cnt["evaluated"] * 16 * z + 4 * cnt["draws"]
+        peaks = measured_peaks()
         out["wang_landau"] = {
             "metric": "WL trials/s", "value": nw * n * calls / dt, "unit": "trials/s",
             "workload": "bcc 12^3, 4 species, 4 shells, 128 walkers, 1000-bin windows, "
@@ -330,6 +385,10 @@ def walker_legs(args) -> dict:
             "us_per_trial_per_walker": dt / (n * calls) * 1e6,
             "accepted_fraction": cnt["accepted"] / max(1, cnt["trials"]),
             "exact_now_fraction": cnt["exact_path"] / max(1, cnt["evaluated"]),
+            "roofline": {"bound": "hbm", "achieved": alg / dt / 1e9, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": alg / dt / 1e9 / peaks["hbm_gbs"],
+                         "note": "algorithmic bytes over host-timed calls; latency-bound walkers"},
+            "cpu_baseline": _wl_cpu(setup, V, cfgs[0], edges, bins, period),
         }
     if "ns" in args.walker_legs:
         rng = np.random.default_rng(20263)
@@ -346,13 +405,24 @@ def walker_legs(args) -> dict:
         run.iterate(args.ns_iterations)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        steps = run.counters(0)["trials"] - c0
+        cnt1 = run.counters(0)
+        steps = cnt1["trials"] - c0
         run.close()
+        z = Z_CUMULATIVE["fcc"][nsh - 1]
+        # every step evaluates its pair before and after (2 + 2z + 32z bytes);
+        # the stream words drawn for the iteration's steps, 4 bytes each
+        draws = cnt1["draws"] * steps // max(1, cnt1["trials"])
+        alg = steps * (2 + 34 * z) + 4 * draws
+        peaks = measured_peaks()
         out["nested_sampling"] = {
             "metric": "NS walk steps/s", "value": steps / dt, "unit": "steps/s",
             "workload": f"fcc 6^3, 5 species, 3 shells, K = 1024, 2000-step walks, "
                         f"{args.ns_iterations} iterations after 5",
             "iterations_per_s": args.ns_iterations / dt,
+            "roofline": {"bound": "hbm", "achieved": alg / dt / 1e9, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": alg / dt / 1e9 / peaks["hbm_gbs"],
+                         "note": "algorithmic bytes over host-timed calls; one sequential run"},
+            "cpu_baseline": _ns_cpu(V, conc),
         }
     return out
 

@@ -39,8 +39,11 @@ cudaStream_t api_batch_stream(brawl_batch* b);
 brawl_batch* api_wl_batch(brawl_wl* wl);
 std::vector<WlWalker>& api_wl_walkers(brawl_wl* wl);
 uint32_t api_wl_smem(brawl_wl* wl);
+// the sweep kernel's variant for the walkers: largest z, every D staged
+void api_wl_variant(brawl_wl* wl, int* max_z, bool* all_D);
 NsRun* api_ns_device_run(brawl_ns* ns, int r);
 uint32_t api_ns_smem(brawl_ns* ns);
+void api_ns_variant(brawl_ns* ns, int* max_z, bool* all_D);
 std::string api_last_error();
 
 }  // namespace brawl

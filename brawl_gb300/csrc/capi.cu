@@ -1167,6 +1167,8 @@ struct brawl_ns {
   size_t limits_cap = 0;
   cudaStream_t stream = nullptr;
   uint32_t smem = 0;
+  int max_z = 0;        // the kernel variant: entries per lane and D staged
+  bool all_D = true;
 };
 
 extern "C" int brawl_ns_destroy(brawl_ns* ns) {
@@ -1213,6 +1215,8 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
     if (R.lazy_cap == 0)
       return cleanup(fail(BRAWL_EINVAL, "run " + std::to_string(r) + ": lattice too large for shared memory"));
     ns->smem = std::max(ns->smem, ns_smem_bytes(m.g, R.lazy_cap));
+    ns->max_z = std::max(ns->max_z, (int)m.g.z);
+    ns->all_D = ns->all_D && walker_layout(m.g, 0, R.lazy_cap).use_D;
     std::vector<double> conc(d.species_concentrations, d.species_concentrations + m.g.ns + 1);
     rc = make_init_job(m, conc.data(), d.species_numbers, R.init);
     if (rc != BRAWL_OK) return cleanup(fail(rc, "run " + std::to_string(r) + ": " + g_err));
@@ -1345,7 +1349,7 @@ extern "C" int brawl_ns_iterate(brawl_ns* ns, int n_iter, double* limits) {
     cur[r].n_iter = n_iter;
   }
   CUDA_TRY(cudaMemcpyAsync(ns->d_runs, cur.data(), n_runs * sizeof(NsRun), cudaMemcpyHostToDevice, ns->stream));
-  launch_ns_iterate(ns->d_runs, n_runs, ns->smem, ns->stream);
+  launch_ns_iterate(ns->d_runs, n_runs, ns->smem, ns->max_z, ns->all_D, ns->stream);
   CUDA_TRY(cudaGetLastError());
   if (limits)
     CUDA_TRY(cudaMemcpyAsync(limits, ns->d_limits, need, cudaMemcpyDeviceToHost, ns->stream));
@@ -1403,6 +1407,8 @@ struct brawl_wl {
   double* d_lng = nullptr;
   double* d_hist = nullptr;
   uint32_t smem = 0;
+  int max_z = 0;        // the kernel variant: entries per lane and D staged
+  bool all_D = true;
   // exchange / flatness / combine scratch
   int per_window = 0;                    // walkers per window when all windows have as many
   int* d_ibin = nullptr;
@@ -1516,6 +1522,8 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
     W.lazy_cap = lazy_cap_for(W.job.g, base, (uint32_t)max_optin);
     if (W.lazy_cap == 0) return cleanup(fail(BRAWL_EINVAL, "window or lattice too large for shared memory"));
     wl->smem = std::max(wl->smem, wl_smem_bytes(W.job.g, W.end - W.start + 1, W.lazy_cap));
+    wl->max_z = std::max(wl->max_z, (int)W.job.g.z);
+    wl->all_D = wl->all_D && walker_layout(W.job.g, W.end - W.start + 1, W.lazy_cap).use_D;
     if (c == 0 || walkers[c].window != walkers[c - 1].window) wl->groups.push_back({c, 0});
     wl->groups.back().count += 1;
   }
@@ -1553,7 +1561,7 @@ extern "C" int brawl_wl_sweeps(brawl_wl* wl, int64_t n_trials, double wl_f, int 
     W.hist_period = hist_period;
   }
   CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), n * sizeof(WlWalker), cudaMemcpyHostToDevice, b->stream));
-  launch_wl_sweeps(wl->d_w, n, wl->smem, b->stream);
+  launch_wl_sweeps(wl->d_w, n, wl->smem, wl->max_z, wl->all_D, b->stream);
   launch_wl_average(wl->d_groups, (int)wl->groups.size(), wl->d_w, wl->bins, 1, b->stream);
   CUDA_TRY(cudaGetLastError());
   std::vector<WlWalker> res(n);
@@ -1755,9 +1763,17 @@ cudaStream_t api_batch_stream(brawl_batch* b) { return b->stream; }
 brawl_batch* api_wl_batch(brawl_wl* wl) { return wl->b; }
 std::vector<WlWalker>& api_wl_walkers(brawl_wl* wl) { return wl->w; }
 uint32_t api_wl_smem(brawl_wl* wl) { return wl->smem; }
+void api_wl_variant(brawl_wl* wl, int* max_z, bool* all_D) {
+  *max_z = wl->max_z;
+  *all_D = wl->all_D;
+}
 
 NsRun* api_ns_device_run(brawl_ns* ns, int r) { return ns->d_runs + r; }
 uint32_t api_ns_smem(brawl_ns* ns) { return ns->smem; }
+void api_ns_variant(brawl_ns* ns, int* max_z, bool* all_D) {
+  *max_z = ns->max_z;
+  *all_D = ns->all_D;
+}
 int api_last_error_set(int code, const std::string& msg) { return fail(code, msg); }
 std::string api_last_error() { return g_err; }
 

@@ -46,6 +46,50 @@ __host__ __device__ inline SmemLayout smem_layout(const Geom& g, bool lattice_in
   return L;
 }
 
+// Builds the wrapping and identity axis tables (see AxisTables).
+__device__ inline void build_axis_tables(const Geom& g, int32_t* tabs, const uint32_t* tab_len,
+                                         int lane, AxisTables& T) {
+  // tabs: the start of the int32 region I
+  int32_t* base = tabs;
+  const int n[3] = {g.n1, g.n2, g.n3};
+  const int W[3] = {g.W1, g.W2, g.W3};
+  for (int a = 0; a < 3; ++a) {
+    const int len = (int)tab_len[a];
+    int32_t* wrap = base;
+    int32_t* ident = base + len;
+    for (int i = lane; i < len; i += 32) {
+      const int t = i - kHalo;
+      int w = t % W[a];
+      w = w < 0 ? w + W[a] : w;
+      int vw, vi;
+      const int ti = t < 0 ? 0 : (t >= 2 * n[a] ? 2 * n[a] - 1 : t);
+      if (a == 0) {
+        vw = w >> g.xs;
+        vi = ti >> g.xs;
+      } else if (a == 1) {
+        vw = (w >> g.ys) * g.sy;
+        vi = (ti >> g.ys) * g.sy;
+      } else {
+        vw = w * g.sz;
+        vi = ti * g.sz;
+      }
+      wrap[i] = vw;
+      ident[i] = vi;
+    }
+    if (a == 0) {
+      T.tx[0] = wrap;
+      T.tx[1] = ident;
+    } else if (a == 1) {
+      T.ty[0] = wrap;
+      T.ty[1] = ident;
+    } else {
+      T.tz[0] = wrap;
+      T.tz[1] = ident;
+    }
+    base += 2 * len;
+  }
+}
+
 // Shared-memory layout of a chain staged with a halo (halo_engine.cuh).
 struct HaloLayout {
   uint32_t mt, tbuf, V, ents, sstart, I, lat, total;

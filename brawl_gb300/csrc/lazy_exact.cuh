@@ -17,6 +17,7 @@
 #pragma once
 
 #include "chain_engine.cuh"
+#include "kernels.cuh"
 
 namespace brawl {
 
@@ -64,6 +65,83 @@ __device__ inline LazyLog lazy_layout(const Geom& g, unsigned char* base, int ca
   L.pair = reinterpret_cast<double*>(base);
   L.cap = cap;
   return L;
+}
+
+// Shared memory of a walker kernel (a Wang-Landau walker's sweep, nested-
+// sampling walks): the stream and its tempered ring, V, the int32 region I
+// (axis tables, F, D when it fits, as in smem_layout), nb bins of ln g and of
+// the histogram (Wang-Landau), the neighbour entries and shell starts, the
+// compact lattice, the staged exact-sum terms (4 z doubles) and the log.
+struct WalkerLayout {
+  uint32_t mt, tbuf, V, I, slices, ents, sstart, lat, vbuf, lazy, total;
+  uint32_t tab_len[3];
+  int32_t F_off, D_off, use_D, nI;
+};
+
+__host__ __device__ inline WalkerLayout walker_layout(const Geom& g, int nb, int lazy_cap) {
+  WalkerLayout L;
+  const uint32_t nsp = (uint32_t)g.ns + 1;
+  const uint32_t nF = nsp * (uint32_t)g.nsh * nsp;
+  const uint32_t nD = nsp * nsp * (uint32_t)g.nsh * nsp;
+  L.mt = 0;
+  L.tbuf = kMTN * 4;
+  L.V = align_up((kMTN + kTbufWords) * 4, 16);
+  L.I = align_up(L.V + (uint32_t)(g.ns * g.ns * g.nsh) * 8, 16);
+  L.tab_len[0] = 2 * (uint32_t)g.n1 + 2 * kHalo;
+  L.tab_len[1] = 2 * (uint32_t)g.n2 + 2 * kHalo;
+  L.tab_len[2] = 2 * (uint32_t)g.n3 + 2 * kHalo;
+  const uint32_t ntab = 2 * (L.tab_len[0] + L.tab_len[1] + L.tab_len[2]);
+  L.use_D = nD * 4 <= kMaxDBytes ? 1 : 0;
+  L.F_off = (int32_t)ntab;
+  L.D_off = (int32_t)(ntab + nF);
+  L.nI = (int32_t)(ntab + nF + (L.use_D ? nD : 0));
+  L.slices = align_up(L.I + (uint32_t)L.nI * 4, 16);
+  L.ents = L.slices + 2u * (uint32_t)nb * 8;
+  L.sstart = L.ents + (uint32_t)g.z * 4;
+  L.lat = align_up(L.sstart + (uint32_t)(g.nsh + 1) * 2, 16);
+  L.vbuf = align_up(L.lat + (uint32_t)g.n_sites, 16);
+  L.lazy = align_up(L.vbuf + 4u * (uint32_t)g.z * 8, 16);
+  L.total = L.lazy + (lazy_cap > 0 ? lazy_bytes(g, lazy_cap) : 0);
+  return L;
+}
+
+// fixed_delta (chain_engine.cuh) on a compact lattice in shared memory, also
+// writing each neighbour's species to the log slot at byte offset rec_off
+// (site 1's entries first).  Valid when the pair is not near and no site is
+// its own neighbour; otherwise the caller takes compact_fixed_delta_rec.
+template <int NJ, bool kUseD>
+__device__ __forceinline__ int fixed_delta_rec(const Geom& g, int lat_off, int I_off, int F_off,
+                                               int D_off, const LanePlan<NJ>& P,
+                                               const SitePair& p, int lane, int rec_off,
+                                               bool& near) {
+  extern __shared__ int32_t s_i32[];
+  extern __shared__ int8_t s_i8[];
+  extern __shared__ uint8_t s_u8[];
+  const bool h = lane >= 16;
+  const int cx = h ? p.bx : p.ax, cy = h ? p.by : p.ay, cz = h ? p.bz : p.az;
+  const int other = h ? p.ai : p.bi;
+  const int so = h ? p.sb : p.sa, sn = h ? p.sa : p.sb;
+  const int nsp = g.ns + 1;
+  const int rowD = I_off + D_off + (so * nsp + sn) * g.nsh * nsp;
+  const int rowN = I_off + F_off + sn * g.nsh * nsp;
+  const int rowO = I_off + F_off + so * g.nsh * nsp;
+  const int bx = I_off + cx, by = I_off + cy, bz = I_off + cz;
+  const int out = rec_off + (h ? g.z : 0) + (lane & 15);
+  int acc = 0;
+  bool hit = false;
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int ni = s_i32[P.ax[j] + bx] + s_i32[P.ay[j] + by] + s_i32[P.az[j] + bz];
+    const int s_before = (int)s_i8[lat_off + ni];
+    const int t = kUseD ? s_i32[rowD + P.shp[j] + s_before]
+                        : s_i32[rowN + P.shp[j] + s_before] - s_i32[rowO + P.shp[j] + s_before];
+    hit |= ni == other;
+    const bool v = (P.valid >> j) & 1u;
+    if (v) s_u8[out + 16 * j] = (uint8_t)s_before;
+    acc += v ? t : 0;
+  }
+  near = __any_sync(kFull, hit);
+  return __reduce_add_sync(kFull, acc);
 }
 
 // compact_fixed_delta, also writing the neighbour codes of both sites to

@@ -11,50 +11,6 @@
 
 namespace brawl {
 
-// Builds the wrapping and identity axis tables (see AxisTables).
-__device__ inline void build_axis_tables(const Geom& g, int32_t* tabs, const SmemLayout& L,
-                                         int lane, AxisTables& T) {
-  // tabs: the start of the int32 region I
-  int32_t* base = tabs;
-  const int n[3] = {g.n1, g.n2, g.n3};
-  const int W[3] = {g.W1, g.W2, g.W3};
-  for (int a = 0; a < 3; ++a) {
-    const int len = (int)L.tab_len[a];
-    int32_t* wrap = base;
-    int32_t* ident = base + len;
-    for (int i = lane; i < len; i += 32) {
-      const int t = i - kHalo;
-      int w = t % W[a];
-      w = w < 0 ? w + W[a] : w;
-      int vw, vi;
-      const int ti = t < 0 ? 0 : (t >= 2 * n[a] ? 2 * n[a] - 1 : t);
-      if (a == 0) {
-        vw = w >> g.xs;
-        vi = ti >> g.xs;
-      } else if (a == 1) {
-        vw = (w >> g.ys) * g.sy;
-        vi = (ti >> g.ys) * g.sy;
-      } else {
-        vw = w * g.sz;
-        vi = ti * g.sz;
-      }
-      wrap[i] = vw;
-      ident[i] = vi;
-    }
-    if (a == 0) {
-      T.tx[0] = wrap;
-      T.tx[1] = ident;
-    } else if (a == 1) {
-      T.ty[0] = wrap;
-      T.ty[1] = ident;
-    } else {
-      T.tz[0] = wrap;
-      T.tz[1] = ident;
-    }
-    base += 2 * len;
-  }
-}
-
 // The reference-order FP64 decision for one trial (rare: only when the
 // fixed-point value is within the band).  Kept out of line so the hot loop
 // stays small; reads the job from global memory.  Returns bit 0 accept,
@@ -115,7 +71,7 @@ __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restri
     for (int i = (n16 << 4) + lane; i < g.n_sites; i += 32) lat[i] = J.lat[i];
   }
   AxisTables T;
-  build_axis_tables(g, I, L, lane, T);
+  build_axis_tables(g, I, L.tab_len, lane, T);
   int pos = (int)J.rng[kMTN];
   __syncwarp();
 

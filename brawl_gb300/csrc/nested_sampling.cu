@@ -92,7 +92,8 @@ __device__ __forceinline__ long long gap_up(double limit, double E, int S) {
 }
 
 
-__global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs) {
+template <int NJ, bool kUseD>
+__global__ void __launch_bounds__(32, 1) ns_iterate_kernel(NsRun* __restrict__ runs) {
   extern __shared__ __align__(16) unsigned char smem[];
   NsRun& R = runs[blockIdx.x];
   const ChainJob& J = R.job;
@@ -100,27 +101,32 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
   const int lane = threadIdx.x;
   const unsigned long long t_start = global_ns();
   const int n = g.n_sites;
-  const int nsp = g.ns + 1;
-  const int nF = nsp * g.nsh * nsp, nV = g.ns * g.ns * g.nsh;
-  // layout: mt | tbuf | V | F | ents | sstart | lattice | vbuf
-  uint32_t* mt = reinterpret_cast<uint32_t*>(smem);
-  uint32_t* tbuf = mt + kMTN;
-  double* V = reinterpret_cast<double*>(smem + align_up((kMTN + kTbufWords) * 4, 16));
-  int32_t* F = reinterpret_cast<int32_t*>(V + nV);
-  uint32_t* ents = reinterpret_cast<uint32_t*>(F + nF);
-  int16_t* sstart = reinterpret_cast<int16_t*>(ents + g.z);
-  int8_t* lat = reinterpret_cast<int8_t*>(
-      smem + align_up((uint32_t)((reinterpret_cast<unsigned char*>(sstart + g.nsh + 1)) - smem), 16));
-  double* vbuf = reinterpret_cast<double*>(smem + align_up((uint32_t)(lat - reinterpret_cast<int8_t*>(smem)) +
-                                                                (uint32_t)g.n_sites, 16));
-  const LazyLog LG = lazy_layout(g, reinterpret_cast<unsigned char*>(vbuf + 4 * g.z), R.lazy_cap);
+  const int nV = g.ns * g.ns * g.nsh;
+  const WalkerLayout WLy = walker_layout(g, 0, R.lazy_cap);
+  uint32_t* mt = reinterpret_cast<uint32_t*>(smem + WLy.mt);
+  uint32_t* tbuf = reinterpret_cast<uint32_t*>(smem + WLy.tbuf);
+  double* V = reinterpret_cast<double*>(smem + WLy.V);
+  int32_t* I = reinterpret_cast<int32_t*>(smem + WLy.I);
+  int32_t* F = I + WLy.F_off;
+  uint32_t* ents = reinterpret_cast<uint32_t*>(smem + WLy.ents);
+  int16_t* sstart = reinterpret_cast<int16_t*>(smem + WLy.sstart);
+  int8_t* lat = reinterpret_cast<int8_t*>(smem + WLy.lat);
+  double* vbuf = reinterpret_cast<double*>(smem + WLy.vbuf);
+  const LazyLog LG = lazy_layout(g, smem + WLy.lazy, R.lazy_cap);
   const double q = ldexp(1.0, -R.S);
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
-  for (int i = lane; i < nF; i += 32) F[i] = J.F[i];
+  for (int i = lane; i < WLy.nI - WLy.F_off; i += 32) F[i] = J.F[i];
   for (int i = lane; i < g.z; i += 32) ents[i] = J.entries[i];
   for (int i = lane; i <= g.nsh; i += 32) sstart[i] = J.shell_start[i];
+  AxisTables T;
+  build_axis_tables(g, I, WLy.tab_len, lane, T);
   __syncwarp();
+  LanePlan<NJ> P;
+  make_lane_plan<NJ>(g, ents, I, T, lane, P);
+  const int lat_off = (int)WLy.lat, I_off = (int)(WLy.I / 4);
+  const int log_off = (int)(LG.codes - smem);
+  const bool self_map = g.W1 <= kHalo || g.W2 <= kHalo || g.W3 <= kHalo;
   Ring ring;
   ring_init(mt, tbuf, (int)J.rng[kMTN], lane, ring);
 
@@ -221,7 +227,10 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
       c_draws += 3;
       ++c_steps;
       uint8_t* rec = LG.codes + (size_t)n_log * 2 * g.z;
-      const int dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
+      bool near;
+      int dE = fixed_delta_rec<NJ, kUseD>(g, lat_off, I_off, WLy.F_off, WLy.D_off, P, p, lane,
+                                          log_off + n_log * 2 * g.z, near);
+      if (near || self_map) dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
       // E + dE lies in E_exact + [lo, hi] quanta; rounding the sum to a double
       // keeps it on the same side of the ceiling (a double) or of the
       // double below it
@@ -295,14 +304,7 @@ __global__ void __launch_bounds__(32) ns_iterate_kernel(NsRun* __restrict__ runs
 }
 
 uint32_t ns_smem_bytes(const Geom& g, int lazy_cap) {
-  const uint32_t nsp = (uint32_t)g.ns + 1;
-  uint32_t b = align_up((kMTN + kTbufWords) * 4, 16);
-  b += (uint32_t)(g.ns * g.ns * g.nsh) * 8 + nsp * (uint32_t)g.nsh * nsp * 4 + (uint32_t)g.z * 4 +
-       (uint32_t)(g.nsh + 1) * 2;
-  b = align_up(b, 16) + (uint32_t)g.n_sites;
-  b = align_up(b, 16) + 4u * (uint32_t)g.z * 8;  // staged exact-sum terms
-  b = align_up(b, 16);
-  return lazy_cap > 0 ? b + lazy_bytes(g, lazy_cap) : b;
+  return walker_layout(g, 0, lazy_cap).total;
 }
 
 void launch_ns_init(NsRun* d_runs, int n_runs, cudaStream_t stream) {
@@ -316,11 +318,30 @@ void launch_ns_jitter(NsRun* d_runs, int n_runs, int max_K, cudaStream_t stream)
   ns_jitter_kernel<<<grid, 256, 0, stream>>>(d_runs, n_runs);
 }
 
-void launch_ns_iterate(NsRun* d_runs, int n_runs, uint32_t smem_bytes, cudaStream_t stream) {
-  cudaFuncSetAttribute(ns_iterate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <int NJ, bool kUseD>
+static void launch_ns_nj(NsRun* d_runs, int n_runs, uint32_t smem_bytes, cudaStream_t stream) {
+  cudaFuncSetAttribute(ns_iterate_kernel<NJ, kUseD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes);
-  BRAWL_CARVEOUT(ns_iterate_kernel);
-  ns_iterate_kernel<<<n_runs, 32, smem_bytes, stream>>>(d_runs);
+  BRAWL_CARVEOUT(ns_iterate_kernel<NJ, kUseD>);
+  ns_iterate_kernel<NJ, kUseD><<<n_runs, 32, smem_bytes, stream>>>(d_runs);
+}
+
+template <bool kUseD>
+static void launch_ns_d(NsRun* d_runs, int n_runs, uint32_t smem_bytes, int max_z, cudaStream_t stream) {
+  switch (lane_entries_for(max_z)) {
+    case 2: launch_ns_nj<2, kUseD>(d_runs, n_runs, smem_bytes, stream); break;
+    case 4: launch_ns_nj<4, kUseD>(d_runs, n_runs, smem_bytes, stream); break;
+    case 6: launch_ns_nj<6, kUseD>(d_runs, n_runs, smem_bytes, stream); break;
+    case 8: launch_ns_nj<8, kUseD>(d_runs, n_runs, smem_bytes, stream); break;
+    default: launch_ns_nj<11, kUseD>(d_runs, n_runs, smem_bytes, stream); break;
+  }
+}
+
+void launch_ns_iterate(NsRun* d_runs, int n_runs, uint32_t smem_bytes, int max_z, bool all_D,
+                       cudaStream_t stream) {
+  if (n_runs <= 0) return;
+  if (all_D) launch_ns_d<true>(d_runs, n_runs, smem_bytes, max_z, stream);
+  else launch_ns_d<false>(d_runs, n_runs, smem_bytes, max_z, stream);
 }
 
 }  // namespace brawl

@@ -28,6 +28,9 @@ struct NsRun {
 uint32_t ns_smem_bytes(const Geom& g, int lazy_cap);
 void launch_ns_init(NsRun* d_runs, int n_runs, cudaStream_t stream);
 void launch_ns_jitter(NsRun* d_runs, int n_runs, int max_K, cudaStream_t stream);
-void launch_ns_iterate(NsRun* d_runs, int n_runs, uint32_t smem_bytes, cudaStream_t stream);
+// max_z: the largest neighbour count of the runs; all_D: every run's
+// difference table D is staged (walker_layout's use_D).
+void launch_ns_iterate(NsRun* d_runs, int n_runs, uint32_t smem_bytes, int max_z, bool all_D,
+                       cudaStream_t stream);
 
 }  // namespace brawl

@@ -642,7 +642,8 @@ int launch_wl(brawl_server* S, Pipe& P) {
   std::vector<EnergyJob> ej;
   std::vector<int> ej_walker;
   uint32_t smem = 0;
-  int max_bins = 0;
+  int max_bins = 0, max_z = 0;
+  bool all_D = true;
   P.launched = P.jobs;
   P.call_ends.assign(P.launched.size(), 0);
   size_t n_all = 0;
@@ -678,6 +679,11 @@ int launch_wl(brawl_server* S, Pipe& P) {
       staged.push_back(W);
     }
     smem = std::max(smem, api_wl_smem(j.wl));
+    int jz = 0;
+    bool jd = true;
+    api_wl_variant(j.wl, &jz, &jd);
+    max_z = std::max(max_z, jz);
+    all_D = all_D && jd;
     max_bins = std::max(max_bins, j.d.wl_bins);
   }
   const int n = (int)staged.size();
@@ -691,7 +697,7 @@ int launch_wl(brawl_server* S, Pipe& P) {
   SV_TRY(grow_host(P.h_flat, P.h_flat_cap, (size_t)n));
   SV_TRY(stage_copy(P, P.d_wl, staged.data(), n * sizeof(WlWalker)));
   if (!groups.empty()) SV_TRY(stage_copy(P, P.d_groups, groups.data(), groups.size() * sizeof(WlGroup)));
-  launch_wl_sweeps(P.d_wl, n, smem, P.s);
+  launch_wl_sweeps(P.d_wl, n, smem, max_z, all_D, P.s);
   if (!groups.empty()) launch_wl_average(P.d_groups, (int)groups.size(), P.d_wl, max_bins, 1, P.s);
   launch_wl_flatness(P.d_wl, n, P.d_flat, P.s);
   SV_CUDA(cudaGetLastError());
@@ -708,7 +714,8 @@ int launch_ns(brawl_server* S, Pipe& P) {
   std::vector<NsRun*> src(n);
   std::vector<int> ints(2 * n);
   uint32_t smem = 0;
-  int total = 0;
+  int total = 0, max_z = 0;
+  bool all_D = true;
   const double t_round = round_ns(S, P.launched);
   for (int k = 0; k < n; ++k) {
     Job& j = *P.launched[k];
@@ -718,6 +725,11 @@ int launch_ns(brawl_server* S, Pipe& P) {
     ints[n + k] = total;
     total += (int)j.quantum;
     smem = std::max(smem, api_ns_smem(j.ns));
+    int jz = 0;
+    bool jd = true;
+    api_ns_variant(j.ns, &jz, &jd);
+    max_z = std::max(max_z, jz);
+    all_D = all_D && jd;
   }
   P.lim_off.assign(ints.begin() + n, ints.end());
   SV_TRY(grow(P.d_ns, P.ns_cap, (size_t)n, P.s));
@@ -731,7 +743,7 @@ int launch_ns(brawl_server* S, Pipe& P) {
   BRAWL_CARVEOUT(ns_stage_kernel);
   ns_stage_kernel<<<(n + 63) / 64, 64, 0, P.s>>>(P.d_ns, P.d_ns_src, n, P.d_limits, P.d_ns_int, P.d_ns_int + n,
                                                   P.d_tns);
-  launch_ns_iterate(P.d_ns, n, smem, P.s);
+  launch_ns_iterate(P.d_ns, n, smem, max_z, all_D, P.s);
   BRAWL_CARVEOUT(ns_unstage_kernel);
   ns_unstage_kernel<<<(n + 63) / 64, 64, 0, P.s>>>(P.d_ns, P.d_ns_src, n);
   SV_CUDA(cudaGetLastError());

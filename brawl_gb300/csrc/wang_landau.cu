@@ -59,7 +59,8 @@ __device__ __noinline__ double wl_exact_e_sw(const Geom& g, const int8_t* lat, c
   return __dadd_rn(__dsub_rn(e_un, p_un), p_sw);
 }
 
-__global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ walkers) {
+template <int NJ, bool kUseD>
+__global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ walkers) {
   extern __shared__ __align__(16) unsigned char smem[];
   WlWalker& W = walkers[blockIdx.x];
   const ChainJob& J = W.job;
@@ -67,26 +68,23 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   const int lane = threadIdx.x;
   const unsigned long long t_start = global_ns();
   const int nV = g.ns * g.ns * g.nsh;
-  const int nsp = g.ns + 1;
-  const int nF = nsp * g.nsh * nsp;
   const int nb = W.end - W.start + 1;
-  // layout: mt | tbuf | V | F | lng slice | hist slice | ents | sstart | lattice | vbuf
-  uint32_t* mt = reinterpret_cast<uint32_t*>(smem);
-  uint32_t* tbuf = mt + kMTN;
-  double* V = reinterpret_cast<double*>(smem + align_up((kMTN + kTbufWords) * 4, 16));
-  int32_t* F = reinterpret_cast<int32_t*>(V + nV);
-  double* lng = reinterpret_cast<double*>(F + ((nF + 1) & ~1));
+  const WalkerLayout WLy = walker_layout(g, nb, W.lazy_cap);
+  uint32_t* mt = reinterpret_cast<uint32_t*>(smem + WLy.mt);
+  uint32_t* tbuf = reinterpret_cast<uint32_t*>(smem + WLy.tbuf);
+  double* V = reinterpret_cast<double*>(smem + WLy.V);
+  int32_t* I = reinterpret_cast<int32_t*>(smem + WLy.I);
+  int32_t* F = I + WLy.F_off;
+  double* lng = reinterpret_cast<double*>(smem + WLy.slices);
   double* hist = lng + nb;
-  uint32_t* ents = reinterpret_cast<uint32_t*>(hist + nb);
-  int16_t* sstart = reinterpret_cast<int16_t*>(ents + g.z);
-  int8_t* lat = reinterpret_cast<int8_t*>(
-      smem + align_up((uint32_t)((reinterpret_cast<unsigned char*>(sstart + g.nsh + 1)) - smem), 16));
-  double* vbuf = reinterpret_cast<double*>(smem + align_up((uint32_t)(lat - reinterpret_cast<int8_t*>(smem)) +
-                                                                (uint32_t)g.n_sites, 16));
-  const LazyLog LG = lazy_layout(g, reinterpret_cast<unsigned char*>(vbuf + 4 * g.z), W.lazy_cap);
+  uint32_t* ents = reinterpret_cast<uint32_t*>(smem + WLy.ents);
+  int16_t* sstart = reinterpret_cast<int16_t*>(smem + WLy.sstart);
+  int8_t* lat = reinterpret_cast<int8_t*>(smem + WLy.lat);
+  double* vbuf = reinterpret_cast<double*>(smem + WLy.vbuf);
+  const LazyLog LG = lazy_layout(g, smem + WLy.lazy, W.lazy_cap);
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
-  for (int i = lane; i < nF; i += 32) F[i] = J.F[i];
+  for (int i = lane; i < WLy.nI - WLy.F_off; i += 32) F[i] = J.F[i];
   for (int i = lane; i < nb; i += 32) {
     lng[i] = W.lng[W.start - 1 + i];
     hist[i] = W.hist[i];
@@ -94,7 +92,16 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
   for (int i = lane; i < g.z; i += 32) ents[i] = J.entries[i];
   for (int i = lane; i <= g.nsh; i += 32) sstart[i] = J.shell_start[i];
   for (int i = lane; i < g.n_sites; i += 32) lat[i] = J.lat[i];
+  AxisTables T;
+  build_axis_tables(g, I, WLy.tab_len, lane, T);
   __syncwarp();
+  LanePlan<NJ> P;
+  make_lane_plan<NJ>(g, ents, I, T, lane, P);
+  const int lat_off = (int)WLy.lat, I_off = (int)(WLy.I / 4);
+  const int log_off = (int)(LG.codes - smem);
+  // an entry can map a site onto itself only when a wrap period is within
+  // the offsets' reach
+  const bool self_map = g.W1 <= kHalo || g.W2 <= kHalo || g.W3 <= kHalo;
   Ring ring;
   ring_init(mt, tbuf, (int)J.rng[kMTN], lane, ring);
 
@@ -160,7 +167,10 @@ __global__ void __launch_bounds__(32) wl_sweep_kernel(WlWalker* __restrict__ wal
       // quanta of e_un + dE q plus the two roundings, each at most 2^-53 of
       // |e_un - p_un| <= |e_un| + 2^30 q or of |e_swapped|; its bin is
       // decided without the FP64 sums when that interval sits in one bin.
-      dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
+      bool near;
+      dE = fixed_delta_rec<NJ, kUseD>(g, lat_off, I_off, WLy.F_off, WLy.D_off, P, p, lane,
+                                      log_off + n_log * 2 * g.z, near);
+      if (near || self_map) dE = compact_fixed_delta_rec(g, lat, F, ents, p, lane, rec);
       bool settled = false;
       for (int pass = 0; pass < 2 && !settled; ++pass) {
         const long long B = 2 * (Eq + max(llabs(Dlo), llabs(Dhi)) + Rs) + (1ll << 30) +
@@ -284,20 +294,32 @@ __global__ void wl_average_kernel(const WlGroup* __restrict__ groups, WlWalker* 
 }
 
 uint32_t wl_smem_bytes(const Geom& g, int nb, int lazy_cap) {
-  uint32_t b = align_up((kMTN + kTbufWords) * 4, 16);
-  const uint32_t nsp = (uint32_t)g.ns + 1, nF = nsp * (uint32_t)g.nsh * nsp;
-  b += (uint32_t)(g.ns * g.ns * g.nsh) * 8 + ((nF + 1) & ~1u) * 4 + 2u * (uint32_t)nb * 8 +
-       (uint32_t)g.z * 4 + (uint32_t)(g.nsh + 1) * 2;
-  b = align_up(b, 16) + (uint32_t)g.n_sites;
-  b = align_up(b, 16) + 4u * (uint32_t)g.z * 8;  // staged exact-sum terms
-  b = align_up(b, 16);
-  return lazy_cap > 0 ? b + lazy_bytes(g, lazy_cap) : b;
+  return walker_layout(g, nb, lazy_cap).total;
 }
 
-void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, cudaStream_t stream) {
-  cudaFuncSetAttribute(wl_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  BRAWL_CARVEOUT(wl_sweep_kernel);
-  wl_sweep_kernel<<<n, 32, smem, stream>>>(d_walkers);
+template <int NJ, bool kUseD>
+static void launch_wl_nj(WlWalker* d_walkers, int n, uint32_t smem, cudaStream_t stream) {
+  cudaFuncSetAttribute(wl_sweep_kernel<NJ, kUseD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  BRAWL_CARVEOUT(wl_sweep_kernel<NJ, kUseD>);
+  wl_sweep_kernel<NJ, kUseD><<<n, 32, smem, stream>>>(d_walkers);
+}
+
+template <bool kUseD>
+static void launch_wl_d(WlWalker* d_walkers, int n, uint32_t smem, int max_z, cudaStream_t stream) {
+  switch (lane_entries_for(max_z)) {
+    case 2: launch_wl_nj<2, kUseD>(d_walkers, n, smem, stream); break;
+    case 4: launch_wl_nj<4, kUseD>(d_walkers, n, smem, stream); break;
+    case 6: launch_wl_nj<6, kUseD>(d_walkers, n, smem, stream); break;
+    case 8: launch_wl_nj<8, kUseD>(d_walkers, n, smem, stream); break;
+    default: launch_wl_nj<11, kUseD>(d_walkers, n, smem, stream); break;
+  }
+}
+
+void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, int max_z, bool all_D,
+                      cudaStream_t stream) {
+  if (n <= 0) return;
+  if (all_D) launch_wl_d<true>(d_walkers, n, smem, max_z, stream);
+  else launch_wl_d<false>(d_walkers, n, smem, max_z, stream);
 }
 
 void launch_wl_average(const WlGroup* d_groups, int n_groups, WlWalker* d_walkers, int bins,

@@ -35,7 +35,10 @@ struct WlGroup {
 // Shared memory of a walker's sweep; lazy_cap 0 gives the bytes without the
 // deferred-energy log.
 uint32_t wl_smem_bytes(const Geom& g, int nb, int lazy_cap);
-void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, cudaStream_t stream);
+// max_z: the largest neighbour count of the walkers; all_D: every walker's
+// difference table D is staged (walker_layout's use_D).
+void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, int max_z, bool all_D,
+                      cudaStream_t stream);
 void launch_wl_average(const WlGroup* d_groups, int n_groups, WlWalker* d_walkers, int bins,
                        int with_hist, cudaStream_t stream);
 uint32_t wl_exchange_smem_bytes(int per_window);
