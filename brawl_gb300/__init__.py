@@ -51,7 +51,7 @@ class _NsDesc(C.Structure):
 class _WlDesc(C.Structure):
     _fields_ = [("setup", _Setup), ("V_ex", C.c_void_p), ("seed", C.c_uint32),
                 ("config", C.c_void_p), ("start_idx", C.c_int), ("end_idx", C.c_int),
-                ("window", C.c_int)]
+                ("window", C.c_int), ("nbr_swap", C.c_int)]
 
 
 class _ChainDesc(C.Structure):
@@ -526,7 +526,7 @@ class WangLandauWalkers:
 
     def __init__(self, walkers: list[dict], bin_edges):
         """Each walker: dict(setup, V, seed, config, start_idx, end_idx,
-        window); bin_edges has bins+1 entries."""
+        window, nbr_swap=False); bin_edges has bins+1 entries."""
         n = len(walkers)
         descs = (_WlDesc * n)()
         keep = []
@@ -544,6 +544,7 @@ class WangLandauWalkers:
             d.start_idx = int(w["start_idx"])
             d.end_idx = int(w["end_idx"])
             d.window = int(w["window"])
+            d.nbr_swap = int(bool(w.get("nbr_swap", False)))
         self.bin_edges = np.ascontiguousarray(bin_edges, dtype=np.float64)
         self.bins = self.bin_edges.size - 1
         h = C.c_void_p()

@@ -1481,6 +1481,7 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
     d[c].V_ex = walkers[c].V_ex;
     d[c].seed = walkers[c].seed;
     d[c].config = walkers[c].config;
+    d[c].nbr_swap = walkers[c].nbr_swap ? 1 : 0;
   }
   brawl_wl* wl = new brawl_wl();
   auto cleanup = [&](int rc) {

@@ -144,12 +144,16 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   };
 
   const int n_tr = (int)W.n_trials;
+  // select_sites or select_sites_nbr (src/wang-landau.F90:1527-1539)
+  const bool nbr = J.nbr_swap != 0;
+  const int n_base = nbr ? 4 : 6;
   for (int it = 0; it < n_tr && status == kStatusOk; ++it) {
-    ring_ensure(mt, tbuf, ring, 7, lane);
+    ring_ensure(mt, tbuf, ring, n_base + 1, lane);
     const int wb = ring.idx;
     SitePair p;
     draw_site(g, tbuf[wb], tbuf[wb + 1], tbuf[wb + 2], p.ax, p.ay, p.az);
-    draw_site(g, tbuf[wb + 3], tbuf[wb + 4], tbuf[wb + 5], p.bx, p.by, p.bz);
+    if (nbr) draw_nbr(g, tbuf[wb + 3], p.ax, p.ay, p.az, p.bx, p.by, p.bz);
+    else draw_site(g, tbuf[wb + 3], tbuf[wb + 4], tbuf[wb + 5], p.bx, p.by, p.bz);
     p.ai = compact_index(g, p.ax, p.ay, p.az);
     p.bi = compact_index(g, p.bx, p.by, p.bz);
     p.sa = lat[p.ai];
@@ -194,11 +198,11 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
         jbin = wl_bin_index_fast(e_sw, e1, range, bins, rf);
       }
     }
-    int consumed = 6;
+    int consumed = n_base;
     if (jbin >= start && jbin <= end) {
-      consumed = 7;
+      consumed = n_base + 1;
       ++c_exp;
-      const uint32_t wu = tbuf[wb + 6];
+      const uint32_t wu = tbuf[wb + n_base];
       const double d = __dsub_rn(lng[ibin - start], lng[jbin - start]);
       if (log_u_lt(wu, d, st)) {
         ++n_acc;
@@ -255,7 +259,7 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
     unsigned long long* c = J.counters;
     c[kCntTrials] += (unsigned long long)W.n_trials;
     c[kCntEvaluated] += c_eval;
-    c[kCntDraws] += 6ull * (unsigned long long)W.n_trials + c_exp;
+    c[kCntDraws] += (unsigned long long)n_base * (unsigned long long)W.n_trials + c_exp;
     c[kCntAccepted] += n_acc;
     c[kCntExpTests] += c_exp;
     c[kCntExactPath] += c_exact;

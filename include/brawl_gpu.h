@@ -238,6 +238,9 @@ typedef struct brawl_wl_desc {
     const int8_t *config;                  /* start config (reference layout) */
     int start_idx, end_idx;                /* 1-based window bins (window_indices) */
     int window;                            /* walkers of a window are averaged together */
+    int nbr_swap;                          /* wl_params%nbr_swap: site 2 a random nearest
+                                              neighbour of site 1 (select_sites_nbr,
+                                              src/wang-landau.F90:1527-1532) */
 } brawl_wl_desc;
 
 /* Walkers of one Wang-Landau simulation; bin_edges has bins+1 entries

@@ -778,9 +778,11 @@ int64_t bo_wl_sweep(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
     double e_unswapped = *energy;
     for (int64_t i = 1; i <= p->n_trials; i++) {
         int a[3], b[3];
+        /* mc_select: select_sites or select_sites_nbr (src/wang-landau.F90:1527-1539) */
         bo_random_site(m, r, a);
-        bo_random_site(m, r, b);
-        if (c) { c->trials++; c->draws += 6; }
+        if (p->nbr_swap) bo_random_nbr(m, r, a, b);
+        else bo_random_site(m, r, b);
+        if (c) { c->trials++; c->draws += p->nbr_swap ? 4 : 6; }
         int8_t s1 = cfg[cfg_index(m, a[0], a[1], a[2])];
         int8_t s2 = cfg[cfg_index(m, b[0], b[1], b[2])];
         double e_swapped = e_unswapped;

@@ -153,6 +153,7 @@ typedef struct {
     int64_t n_trials;           /* mc_sweeps * n_atoms */
     double wl_f;
     int hist_period;            /* INT(0.02*REAL(n_atoms)) */
+    int nbr_swap;               /* select_sites_nbr: site 2 a random neighbour of site 1 */
 } bo_wl_params;
 
 /* One walker's sweeps() trial loop.  lng: bins entries (global indexing),

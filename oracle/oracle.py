@@ -69,7 +69,8 @@ class NsParams(C.Structure):
 
 class WlParams(C.Structure):
     _fields_ = [("bins", C.c_int), ("start_idx", C.c_int), ("end_idx", C.c_int),
-                ("n_trials", C.c_int64), ("wl_f", C.c_double), ("hist_period", C.c_int)]
+                ("n_trials", C.c_int64), ("wl_f", C.c_double), ("hist_period", C.c_int),
+                ("nbr_swap", C.c_int)]
 
 
 _lib = None
@@ -292,9 +293,9 @@ class OracleModel:
         return acc, float(e[0]), c
 
     def wl_sweep(self, cfg, rng, bin_edges, lng, hist, energy, bins, start_idx, end_idx, n_trials,
-                 wl_f, hist_period):
+                 wl_f, hist_period, nbr_swap=False):
         e = np.array([energy], dtype=np.float64)
-        p = WlParams(bins, start_idx, end_idx, n_trials, wl_f, hist_period)
+        p = WlParams(bins, start_idx, end_idx, n_trials, wl_f, hist_period, int(bool(nbr_swap)))
         c = Counters()
         acc = lib().bo_wl_sweep(C.byref(self.m), C.byref(p), _ptr(cfg), C.byref(rng.s), _ptr(bin_edges),
                                 _ptr(lng), _ptr(hist), _ptr(e), C.byref(c))

@@ -17,7 +17,8 @@ def _emulate(mods, cfgs, rngs, walkers, bin_edges, lngs, hists, n_trials, wl_f, 
     for k, w in enumerate(walkers):
         e = mods[k].total_energy(cfgs[k])
         a, _, _ = mods[k].wl_sweep(cfgs[k], rngs[k], bin_edges, lngs[k], hists[k], e, bins,
-                                   w["start_idx"], w["end_idx"], n_trials, wl_f, period)
+                                   w["start_idx"], w["end_idx"], n_trials, wl_f, period,
+                                   nbr_swap=w.get("nbr_swap", False))
         acc.append(a)
     windows = sorted(set(w["window"] for w in walkers))
     for win in windows:
@@ -35,11 +36,13 @@ def _emulate(mods, cfgs, rngs, walkers, bin_edges, lngs, hists, n_trials, wl_f, 
     return acc
 
 
-@pytest.mark.parametrize("lattice,n,ns,nsh,windows", [
-    ("bcc", (4, 4, 4), 4, 6, [(1, 30), (19, 48)]),
-    ("fcc", (3, 3, 3), 3, 3, [(10, 30), (20, 40), (18, 44)]),
+@pytest.mark.parametrize("lattice,n,ns,nsh,windows,nbr", [
+    ("bcc", (4, 4, 4), 4, 6, [(1, 30), (19, 48)], False),
+    ("fcc", (3, 3, 3), 3, 3, [(10, 30), (20, 40), (18, 44)], False),
+    ("bcc", (4, 4, 4), 4, 6, [(1, 30), (19, 48)], True),
+    ("fcc", (3, 3, 3), 3, 3, [(10, 30), (20, 40), (18, 44)], True),
 ])
-def test_wang_landau_sweeps_match_oracle(lattice, n, ns, nsh, windows):
+def test_wang_landau_sweeps_match_oracle(lattice, n, ns, nsh, windows, nbr):
     rng = np.random.default_rng(21)
     V = random_V(rng, ns, nsh)
     setup = B.Setup(lattice, *n, ns, nsh)
@@ -51,7 +54,7 @@ def test_wang_landau_sweeps_match_oracle(lattice, n, ns, nsh, windows):
             cfg, _ = mod0.initial_setup(r0, conc_vector(ns))
             seed = 110179 + 11 * len(walkers)
             walkers.append(dict(setup=setup, V=V, seed=seed, config=cfg.copy(), start_idx=lo,
-                                end_idx=hi, window=win))
+                                end_idx=hi, window=win, nbr_swap=nbr))
             mods.append(O.OracleModel(lattice, *n, V))
             cfgs.append(cfg.copy())
             rngs.append(O.OracleRng(seed))

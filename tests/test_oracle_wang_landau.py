@@ -160,3 +160,66 @@ def test_windows_and_bins_follow_the_reference():
     assert W.create_overlap(W.divide_range(512, 4), 0.25) == [[1, 128], [97, 256], [217, 384], [343, 512]]
     e = W.create_energy_bins(128, -96.0, 0.0, 512)
     assert e.size == 513 and e[0] == -96.0 * 128 / (13.605693122 * 1000.0) and abs(e[-1]) < 1e-15
+
+
+BCC_NBRS = [(1, 1, 1), (1, 1, -1), (1, -1, 1), (1, -1, -1), (-1, 1, 1), (-1, 1, -1), (-1, -1, 1),
+            (-1, -1, -1)]
+
+
+def _py_sweeps_nbr(mod, n, cfg, rng, edges, lng, hist, e, bins, start, end, n_trials, f, period):
+    """sweeps (src/wang-landau.F90:539-632) with select_sites_nbr (:1527-1532)
+    written out from the reference, on a bcc lattice n x n x n; the site draw
+    and the pair energies come from the oracle."""
+    W = 2 * n
+    acc = 0
+    for i in range(1, n_trials + 1):
+        a = mod.random_site(rng)
+        k = int(math.floor(8.0 * rng.uniform()))          # bcc_random_nbr: floor(8 u) + 1
+        d = BCC_NBRS[k]
+        b = tuple((a[c] + d[c]) % W for c in range(3))
+        s1, s2 = cfg[a[2], a[1], a[0]], cfg[b[2], b[1], b[0]]
+        p_un = mod.pair_energy(cfg, a, b)
+        cfg[a[2], a[1], a[0]], cfg[b[2], b[1], b[0]] = s2, s1
+        e_sw = e
+        if s1 != s2:
+            e_sw = e - p_un + mod.pair_energy(cfg, a, b)
+        ib, jb = _py_bin(e, edges, bins), _py_bin(e_sw, edges, bins)
+        if start - 1 < jb < end + 1 and math.log(rng.uniform()) < lng[ib - 1] - lng[jb - 1]:
+            acc += 1
+            e = e_sw
+        else:
+            cfg[a[2], a[1], a[0]], cfg[b[2], b[1], b[0]] = s1, s2
+            jb = ib
+        if period > 0 and i % period == 0:
+            hist[jb - start] += 1.0
+        lng[jb - 1] += f
+    return acc, e
+
+
+def test_sweeps_with_neighbour_swaps_match_python_restatement():
+    rng = np.random.default_rng(8)
+    ns, nsh, n = 3, 2, 3
+    V = np.zeros((ns, ns, nsh))
+    for sh in range(nsh):
+        a = rng.uniform(-0.05, 0.05, size=(ns, ns))
+        V[:, :, sh] = (np.triu(a) + np.triu(a, 1).T) / 13.605693122
+    mod = O.OracleModel("bcc", n, n, n, V)
+    cfg, _ = mod.initial_setup(O.OracleRng(3), np.array([0.0, 1 / 3, 1 / 3, 1 / 3]), np.array([18, 18, 18]))
+    e0 = mod.total_energy(cfg)
+    bins = 60
+    edges = (e0 - 0.02) + np.arange(bins + 1) * (0.04 / bins)
+    start, end, n_trials, period = 10, 50, 4000, 1
+    cfg_a, cfg_b = cfg.copy(), cfg.copy()
+    lng_a, lng_b = np.zeros(bins), np.zeros(bins)
+    hist_a, hist_b = np.zeros(end - start + 1), np.zeros(end - start + 1)
+    ra, rb = O.OracleRng(77), O.OracleRng(77)
+    acc_a, e_a, c = mod.wl_sweep(cfg_a, ra, edges, lng_a, hist_a, e0, bins, start, end, n_trials, 1.0, period,
+                                 nbr_swap=True)
+    acc_b, e_b = _py_sweeps_nbr(mod, n, cfg_b, rb, edges, lng_b, hist_b, e0, bins, start, end, n_trials,
+                                1.0, period)
+    assert acc_a == acc_b > 0
+    assert e_a == e_b
+    assert np.array_equal(cfg_a, cfg_b)
+    assert np.array_equal(lng_a, lng_b) and np.array_equal(hist_a, hist_b)
+    assert np.array_equal(ra.state_words(), rb.state_words())
+    assert c.draws == 4 * n_trials + c.exp_tests
