@@ -116,6 +116,9 @@ def load(rebuild: bool = False):
         "brawl_wl_swap_configs": ([vp, i, i], i),
         "brawl_wl_genrand": ([vp, i, i64, vp], i),
         "brawl_wl_counters": ([vp, i, vp], i),
+        "brawl_wl_radial_enable": ([vp, i, vp, i, i], i),
+        "brawl_wl_radial_set_done": ([vp, vp], i),
+        "brawl_wl_radial_get": ([vp, i, vp, vp, vp], i),
         "brawl_wl_replica_exchange": ([vp, vp, vp, vp], i),
         "brawl_wl_flatness": ([vp, vp], i),
         "brawl_wl_dos_combine": ([vp, vp], i),
@@ -640,3 +643,27 @@ class WangLandauWalkers:
         c = np.zeros(NUM_COUNTERS, dtype=np.int64)
         _check(load().brawl_wl_counters(self._h, w, _ptr(c)))
         return dict(zip(COUNTER_NAMES, (int(v) for v in c)))
+
+    # -- radial-density samples inside sweeps() (src/wang-landau.F90:566-586) --
+    def radial_enable(self, wc_range: int, shells, radial_samples: int, num_walkers: int) -> None:
+        sh = np.ascontiguousarray(shells, dtype=np.float64)
+        if sh.size != wc_range:
+            raise ValueError("shells needs wc_range entries")
+        _check(load().brawl_wl_radial_enable(self._h, int(wc_range), _ptr(sh), int(radial_samples),
+                                             int(num_walkers)))
+        self.radial_wc = int(wc_range)
+
+    def radial_set_done(self, done) -> None:
+        """radial_record_bool (bins); every bin set stops the sampling."""
+        d = np.ascontiguousarray(np.asarray(done, dtype=bool).astype(np.uint8))
+        _check(load().brawl_wl_radial_set_done(self._h, _ptr(d)))
+
+    def radial(self, w: int) -> tuple[np.ndarray, np.ndarray, int]:
+        """(radial_record (bins), rho_of_E shaped (bins, wc, ns, ns) -- the C
+        view of rho_of_E(i, j, l, bin) --, radial_mc_steps) of walker w."""
+        ns = self.walkers[w]["setup"].n_species
+        rec = np.zeros(self.bins, dtype=np.int32)
+        rho = np.zeros((self.bins, self.radial_wc, ns, ns), dtype=np.float64)
+        st = np.zeros(1, dtype=np.int32)
+        _check(load().brawl_wl_radial_get(self._h, w, _ptr(rec), _ptr(rho), _ptr(st)))
+        return rec, rho, int(st[0])

@@ -1409,6 +1409,15 @@ struct brawl_wl {
   uint32_t smem = 0;
   int max_z = 0;        // the kernel variant: entries per lane and D staged
   bool all_D = true;
+  // radial-density samples (brawl_wl_radial_enable)
+  int rad_wc = 0, rad_n_off = 0, rad_n_class = 0;
+  WlRadial* d_rad = nullptr;
+  uint32_t* d_rad_offsets = nullptr;
+  unsigned long long* d_rad_masks = nullptr;
+  uint8_t* d_rad_done = nullptr;
+  int32_t* d_rad_record = nullptr;
+  double* d_rad_rho = nullptr;
+  int32_t* d_rad_steps = nullptr;
   // exchange / flatness / combine scratch
   int per_window = 0;                    // walkers per window when all windows have as many
   int* d_ibin = nullptr;
@@ -1454,7 +1463,10 @@ extern "C" int brawl_wl_destroy(brawl_wl* wl) {
     for (const void* p : {(const void*)wl->d_w, (const void*)wl->d_groups, (const void*)wl->d_lng,
                           (const void*)wl->d_hist, (const void*)wl->d_ibin, (const void*)wl->d_ov,
                           (const void*)wl->d_partner, (const void*)wl->d_exchanged, (const void*)wl->d_nacc,
-                          (const void*)wl->d_flat, (const void*)wl->d_combined})
+                          (const void*)wl->d_flat, (const void*)wl->d_combined, (const void*)wl->d_rad,
+                          (const void*)wl->d_rad_offsets, (const void*)wl->d_rad_masks,
+                          (const void*)wl->d_rad_done, (const void*)wl->d_rad_record,
+                          (const void*)wl->d_rad_rho, (const void*)wl->d_rad_steps})
       dfree(p, wl->b->stream);
     brawl_batch_destroy(wl->b);
   }
@@ -1648,6 +1660,97 @@ extern "C" int brawl_wl_reset_hist(brawl_wl* wl) {
   for (const WlWalker& W : wl->w) total += W.end - W.start + 1;
   CUDA_TRY(cudaMemsetAsync(wl->d_hist, 0, total * 8, wl->b->stream));
   CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_radial_enable(brawl_wl* wl, int wc_range, const double* shells,
+                                      int radial_samples, int num_walkers) {
+  if (!wl || !shells || wc_range < 1 || wc_range > 64 || num_walkers < 1 || radial_samples < 0)
+    return fail(BRAWL_EINVAL, "bad argument");
+  brawl_batch* b = wl->b;
+  const int n = (int)wl->w.size();
+  const Geom& g0 = b->models[0].g;
+  for (int c = 1; c < n; ++c) {
+    const Geom& g = b->models[c].g;
+    if (g.lattice != g0.lattice || g.n1 != g0.n1 || g.n2 != g0.n2 || g.n3 != g0.n3 || g.ns != g0.ns)
+      return fail(BRAWL_EINVAL, "radial samples need walkers on one lattice");
+  }
+  if (wl->d_rad) return fail(BRAWL_EINVAL, "radial samples already enabled");
+  AsroPlan plan;
+  if (make_asro_plan(g0, wc_range, shells, plan) != 0) return fail(BRAWL_EINVAL, "bad ASRO shells");
+  int max_optin = 0;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  const int n_off = (int)plan.offsets.size(), n_class = plan.n_class;
+  uint32_t smem = 0;
+  for (const WlWalker& W : wl->w)
+    smem = std::max(smem, wl_smem_bytes(W.job.g, W.end - W.start + 1, W.lazy_cap, wl->bins, n_off, n_class));
+  if (smem > (uint32_t)max_optin) return fail(BRAWL_EINVAL, "radial-sample scratch does not fit in shared memory");
+  const size_t per = (size_t)g0.ns * g0.ns * wc_range;
+  cudaStream_t s = b->stream;
+  std::vector<unsigned long long> masks(plan.class_mask.begin(), plan.class_mask.end());
+  if (masks.empty()) masks.push_back(0ull);
+  if (dalloc(&wl->d_rad, sizeof(WlRadial), s) != cudaSuccess ||
+      dalloc(&wl->d_rad_offsets, std::max<size_t>(n_off, 1) * 4, s) != cudaSuccess ||
+      dalloc(&wl->d_rad_masks, masks.size() * 8, s) != cudaSuccess ||
+      dalloc(&wl->d_rad_done, (size_t)wl->bins, s) != cudaSuccess ||
+      dalloc(&wl->d_rad_record, (size_t)n * wl->bins * 4, s) != cudaSuccess ||
+      dalloc(&wl->d_rad_rho, (size_t)n * wl->bins * per * 8, s) != cudaSuccess ||
+      dalloc(&wl->d_rad_steps, (size_t)n * 4, s) != cudaSuccess)
+    return fail(BRAWL_ENOMEM, "radial-sample arrays");
+  WlRadial R;
+  R.offsets = wl->d_rad_offsets;
+  R.class_masks = wl->d_rad_masks;
+  R.done = wl->d_rad_done;
+  R.n_offsets = n_off;
+  R.n_class = n_class;
+  R.wc_range = wc_range;
+  R.cap = std::max(radial_samples / num_walkers, 1);
+  if (n_off > 0)
+    CUDA_TRY(cudaMemcpyAsync(wl->d_rad_offsets, plan.offsets.data(), (size_t)n_off * 4, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(wl->d_rad_masks, masks.data(), masks.size() * 8, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(wl->d_rad, &R, sizeof(R), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemsetAsync(wl->d_rad_done, 0, (size_t)wl->bins, s));
+  CUDA_TRY(cudaMemsetAsync(wl->d_rad_record, 0, (size_t)n * wl->bins * 4, s));
+  CUDA_TRY(cudaMemsetAsync(wl->d_rad_rho, 0, (size_t)n * wl->bins * per * 8, s));
+  CUDA_TRY(cudaMemsetAsync(wl->d_rad_steps, 0, (size_t)n * 4, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  wl->rad_wc = wc_range;
+  wl->rad_n_off = n_off;
+  wl->rad_n_class = n_class;
+  wl->smem = std::max(wl->smem, smem);
+  for (int c = 0; c < n; ++c) {
+    WlWalker& W = wl->w[c];
+    W.radial = wl->d_rad;
+    W.radial_record = wl->d_rad_record + (size_t)c * wl->bins;
+    W.rho_of_E = wl->d_rad_rho + (size_t)c * wl->bins * per;
+    W.radial_steps = wl->d_rad_steps + c;
+    W.rad_n_offsets = n_off;
+    W.rad_n_class = n_class;
+  }
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_radial_set_done(brawl_wl* wl, const uint8_t* done) {
+  if (!wl || !done) return fail(BRAWL_EINVAL, "bad argument");
+  if (!wl->d_rad) return fail(BRAWL_EINVAL, "radial samples not enabled");
+  bool all = true;
+  for (int k = 0; k < wl->bins; ++k) all = all && done[k] != 0;
+  CUDA_TRY(cudaMemcpyAsync(wl->d_rad_done, done, (size_t)wl->bins, cudaMemcpyHostToDevice, wl->b->stream));
+  CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
+  if (all)  // rho_saved: the walkers stop sampling
+    for (WlWalker& W : wl->w) W.radial_record = nullptr;
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_radial_get(brawl_wl* wl, int c, int32_t* record, double* rho_of_E, int32_t* steps) {
+  if (!wl || c < 0 || c >= (int)wl->w.size() || !record) return fail(BRAWL_EINVAL, "bad argument");
+  if (!wl->d_rad) return fail(BRAWL_EINVAL, "radial samples not enabled");
+  const size_t per = (size_t)wl->b->models[0].g.ns * wl->b->models[0].g.ns * wl->rad_wc;
+  CUDA_TRY(cudaMemcpy(record, wl->d_rad_record + (size_t)c * wl->bins, (size_t)wl->bins * 4, cudaMemcpyDeviceToHost));
+  if (rho_of_E)
+    CUDA_TRY(cudaMemcpy(rho_of_E, wl->d_rad_rho + (size_t)c * wl->bins * per, (size_t)wl->bins * per * 8,
+                        cudaMemcpyDeviceToHost));
+  if (steps) CUDA_TRY(cudaMemcpy(steps, wl->d_rad_steps + c, 4, cudaMemcpyDeviceToHost));
   return BRAWL_OK;
 }
 

@@ -73,12 +73,18 @@ __device__ inline LazyLog lazy_layout(const Geom& g, unsigned char* base, int ca
 // the histogram (Wang-Landau), the neighbour entries and shell starts, the
 // compact lattice, the staged exact-sum terms (4 z doubles) and the log.
 struct WalkerLayout {
-  uint32_t mt, tbuf, V, I, slices, ents, sstart, lat, vbuf, lazy, total;
+  uint32_t mt, tbuf, V, I, slices, ents, sstart, lat, vbuf, lazy;
+  uint32_t rad, rad_offsets, rad_masks, rad_hist, total;  // radial-sample scratch
   uint32_t tab_len[3];
   int32_t F_off, D_off, use_D, nI;
 };
 
-__host__ __device__ inline WalkerLayout walker_layout(const Geom& g, int nb, int lazy_cap) {
+// rad_bins > 0: the radial-sample scratch follows the log -- one eligibility
+// bit per bin, the ASRO plan's offsets and class masks, and the
+// (species, species, class) and species counts.
+__host__ __device__ inline WalkerLayout walker_layout(const Geom& g, int nb, int lazy_cap,
+                                                      int rad_bins = 0, int rad_n_offsets = 0,
+                                                      int rad_n_class = 0) {
   WalkerLayout L;
   const uint32_t nsp = (uint32_t)g.ns + 1;
   const uint32_t nF = nsp * (uint32_t)g.nsh * nsp;
@@ -101,7 +107,17 @@ __host__ __device__ inline WalkerLayout walker_layout(const Geom& g, int nb, int
   L.lat = align_up(L.sstart + (uint32_t)(g.nsh + 1) * 2, 16);
   L.vbuf = align_up(L.lat + (uint32_t)g.n_sites, 16);
   L.lazy = align_up(L.vbuf + 4u * (uint32_t)g.z * 8, 16);
-  L.total = L.lazy + (lazy_cap > 0 ? lazy_bytes(g, lazy_cap) : 0);
+  L.rad = L.lazy + (lazy_cap > 0 ? lazy_bytes(g, lazy_cap) : 0);
+  L.rad_offsets = L.rad;
+  L.rad_masks = L.rad;
+  L.rad_hist = L.rad;
+  L.total = L.rad;
+  if (rad_bins > 0) {
+    L.rad_offsets = align_up(L.rad + (((uint32_t)rad_bins + 31) / 32) * 4, 16);
+    L.rad_masks = align_up(L.rad_offsets + (uint32_t)rad_n_offsets * 4, 16);
+    L.rad_hist = L.rad_masks + (uint32_t)rad_n_class * 8;
+    L.total = align_up(L.rad_hist + (nsp * nsp * (uint32_t)rad_n_class + nsp) * 4, 16);
+  }
   return L;
 }
 

@@ -59,6 +59,47 @@ __device__ __noinline__ double wl_exact_e_sw(const Geom& g, const int8_t* lat, c
   return __dadd_rn(__dsub_rn(e_un, p_un), p_sw);
 }
 
+// radial_densities (src/analytics.f90:293-404) of the staged lattice, added
+// to rho_of_E(:, :, :, bin): the (species, species, shell class) pair counts
+// through the ASRO plan (asro.cuh) in shared memory, then rho(i, j, l) =
+// count / particle_counts(i) per element, each added to its own FP64 sum.
+// Out of line: a sample is taken at most once every n_atoms trials.
+__device__ __noinline__ void wl_radial_sample(const Geom& g, const int8_t* lat, const uint32_t* offs,
+                                              const unsigned long long* masks, unsigned int* hist,
+                                              int n_off, int n_class, int wc, double* rho_bin,
+                                              int lane) {
+  const int nsp = g.ns + 1;
+  const int nh = nsp * nsp * n_class;
+  unsigned int* pcs = hist + nh;
+  for (int i = lane; i < nh + nsp; i += 32) hist[i] = 0u;
+  __syncwarp();
+  const int W1 = 2 * g.n1, W2 = 2 * g.n2, W3 = 2 * g.n3;
+  for (int site = lane; site < g.n_sites; site += 32) {
+    int x, y, z;
+    decode_site(g, site, x, y, z);
+    const int si = lat[site];
+    atomicAdd(&pcs[si], 1u);
+    const int row = si * nsp;
+    for (int o = 0; o < n_off; ++o) {
+      int dx, dy, dz, cls;
+      unpack_entry(offs[o], dx, dy, dz, cls);
+      const int sj = lat[compact_index(g, wrap_general(x, dx, W1), wrap_general(y, dy, W2),
+                                       wrap_general(z, dz, W3))];
+      atomicAdd(&hist[(row + sj) * n_class + cls], 1u);
+    }
+  }
+  __syncwarp();
+  const int ns = g.ns, per = ns * ns * wc;
+  for (int k = lane; k < per; k += 32) {
+    const int i = k % ns + 1, j = (k / ns) % ns + 1, l = k / (ns * ns);
+    unsigned int c = 0;
+    for (int cl = 0; cl < n_class; ++cl)
+      if ((masks[cl] >> l) & 1ull) c += hist[(i * nsp + j) * n_class + cl];
+    rho_bin[k] = __dadd_rn(rho_bin[k], __ddiv_rn((double)c, (double)pcs[i]));
+  }
+  __syncwarp();
+}
+
 template <int NJ, bool kUseD>
 __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ walkers) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -69,7 +110,9 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   const unsigned long long t_start = global_ns();
   const int nV = g.ns * g.ns * g.nsh;
   const int nb = W.end - W.start + 1;
-  const WalkerLayout WLy = walker_layout(g, nb, W.lazy_cap);
+  const bool rad_on = W.radial_record != nullptr;
+  const WalkerLayout WLy = walker_layout(g, nb, W.lazy_cap, rad_on ? W.bins : 0, W.rad_n_offsets,
+                                         W.rad_n_class);
   uint32_t* mt = reinterpret_cast<uint32_t*>(smem + WLy.mt);
   uint32_t* tbuf = reinterpret_cast<uint32_t*>(smem + WLy.tbuf);
   double* V = reinterpret_cast<double*>(smem + WLy.V);
@@ -92,6 +135,29 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   for (int i = lane; i < g.z; i += 32) ents[i] = J.entries[i];
   for (int i = lane; i <= g.nsh; i += 32) sstart[i] = J.shell_start[i];
   for (int i = lane; i < g.n_sites; i += 32) lat[i] = J.lat[i];
+  // radial samples: a bin is eligible while radial_record < cap and
+  // radial_record_bool is unset
+  uint32_t* elig = reinterpret_cast<uint32_t*>(smem + WLy.rad);
+  uint32_t* r_offs = reinterpret_cast<uint32_t*>(smem + WLy.rad_offsets);
+  unsigned long long* r_masks = reinterpret_cast<unsigned long long*>(smem + WLy.rad_masks);
+  unsigned int* r_hist = reinterpret_cast<unsigned int*>(smem + WLy.rad_hist);
+  int rsteps = 0, r_cap = 0, r_wc = 0;
+  if (rad_on) {
+    const WlRadial RP = *W.radial;
+    r_cap = RP.cap;
+    r_wc = RP.wc_range;
+    rsteps = *W.radial_steps;
+    for (int w = lane; w < (W.bins + 31) / 32; w += 32) {
+      uint32_t bits = 0u;
+      for (int b = 0; b < 32 && 32 * w + b < W.bins; ++b) {
+        const int k = 32 * w + b;
+        if (W.radial_record[k] < RP.cap && !RP.done[k]) bits |= 1u << b;
+      }
+      elig[w] = bits;
+    }
+    for (int i = lane; i < RP.n_offsets; i += 32) r_offs[i] = RP.offsets[i];
+    for (int i = lane; i < RP.n_class; i += 32) r_masks[i] = RP.class_masks[i];
+  }
   AxisTables T;
   build_axis_tables(g, I, WLy.tab_len, lane, T);
   __syncwarp();
@@ -198,6 +264,28 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
         jbin = wl_bin_index_fast(e_sw, e1, range, bins, rf);
       }
     }
+    // a radial sample of the trial configuration (the swap applied), before
+    // the decision, as the reference takes it
+    bool swapped = false;
+    if (rad_on && jbin >= 1 && jbin <= bins && ((elig[(jbin - 1) >> 5] >> ((jbin - 1) & 31)) & 1u)) {
+      if (++rsteps >= g.n_sites) {
+        rsteps = 0;
+        if (differ && lane == 0) {
+          lat[p.ai] = (int8_t)p.sb;
+          lat[p.bi] = (int8_t)p.sa;
+        }
+        swapped = differ;
+        __syncwarp();
+        wl_radial_sample(g, lat, r_offs, r_masks, r_hist, W.rad_n_offsets, W.rad_n_class, r_wc,
+                         W.rho_of_E + (size_t)(jbin - 1) * g.ns * g.ns * r_wc, lane);
+        if (lane == 0) {
+          const int rec = W.radial_record[jbin - 1] + 1;
+          W.radial_record[jbin - 1] = rec;
+          if (rec >= r_cap) elig[(jbin - 1) >> 5] &= ~(1u << ((jbin - 1) & 31));
+        }
+        __syncwarp();
+      }
+    }
     int consumed = n_base;
     if (jbin >= start && jbin <= end) {
       consumed = n_base + 1;
@@ -229,9 +317,17 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
         ibin = jbin;
       } else {
         jbin = ibin;
+        if (swapped && lane == 0) {  // the sampled swap undone
+          lat[p.ai] = (int8_t)p.sa;
+          lat[p.bi] = (int8_t)p.sb;
+        }
       }
     } else {
       jbin = ibin;
+      if (swapped && lane == 0) {
+        lat[p.ai] = (int8_t)p.sa;
+        lat[p.bi] = (int8_t)p.sb;
+      }
     }
     if (--until == 0) {
       if (lane == 0) hist[jbin - start] = __dadd_rn(hist[jbin - start], 1.0);
@@ -255,6 +351,7 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   if (lane == 0) {
     W.e_out = e_un;
     if (W.e_state) *W.e_state = e_un;
+    if (rad_on) *W.radial_steps = rsteps;
     W.accepted = n_acc;
     unsigned long long* c = J.counters;
     c[kCntTrials] += (unsigned long long)W.n_trials;
@@ -297,8 +394,9 @@ __global__ void wl_average_kernel(const WlGroup* __restrict__ groups, WlWalker* 
   }
 }
 
-uint32_t wl_smem_bytes(const Geom& g, int nb, int lazy_cap) {
-  return walker_layout(g, nb, lazy_cap).total;
+uint32_t wl_smem_bytes(const Geom& g, int nb, int lazy_cap, int rad_bins, int rad_n_offsets,
+                       int rad_n_class) {
+  return walker_layout(g, nb, lazy_cap, rad_bins, rad_n_offsets, rad_n_class).total;
 }
 
 template <int NJ, bool kUseD>

@@ -5,6 +5,18 @@
 
 namespace brawl {
 
+// The radial-density samples that sweeps() takes per bin
+// (src/wang-landau.F90:566-586), shared by the walkers of a batch: the
+// ASRO plan (packed offsets with their shell class, asro.cuh), the per-walker
+// cap MAX(radial_samples / num_walkers, 1) and radial_record_bool.
+struct WlRadial {
+  const uint32_t* offsets;
+  const unsigned long long* class_masks;
+  const uint8_t* done;   // bins
+  int32_t n_offsets, n_class;
+  int32_t wc_range, cap;
+};
+
 struct WlWalker {
   ChainJob job;          // geometry, tables, stream, counters, status, lattice
   double* lng;           // ln g over all bins (the reference's wl_logdos)
@@ -25,6 +37,14 @@ struct WlWalker {
   double* e_state;
   int32_t S;             // fixed-point shift of the chain's F table
   int32_t lazy_cap;      // moves the deferred-energy log holds (>= 1)
+  // radial-density samples (all null when off): the plan, this walker's
+  // radial_record (bins), rho_of_E (bins x wc x ns x ns, rho(i, j, l, bin)
+  // with i fastest) and radial_mc_steps
+  const WlRadial* radial;
+  int32_t* radial_record;
+  double* rho_of_E;
+  int32_t* radial_steps;
+  int32_t rad_n_offsets, rad_n_class;  // the plan's sizes (shared memory)
 };
 
 // Walkers first..first+count-1 share a window and are averaged together.
@@ -33,8 +53,9 @@ struct WlGroup {
 };
 
 // Shared memory of a walker's sweep; lazy_cap 0 gives the bytes without the
-// deferred-energy log.
-uint32_t wl_smem_bytes(const Geom& g, int nb, int lazy_cap);
+// deferred-energy log; rad_bins > 0 adds the radial-sample scratch.
+uint32_t wl_smem_bytes(const Geom& g, int nb, int lazy_cap, int rad_bins = 0, int rad_n_offsets = 0,
+                       int rad_n_class = 0);
 // max_z: the largest neighbour count of the walkers; all_D: every walker's
 // difference table D is staged (walker_layout's use_D).
 void launch_wl_sweeps(WlWalker* d_walkers, int n, uint32_t smem, int max_z, bool all_D,

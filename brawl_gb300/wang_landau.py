@@ -7,7 +7,8 @@ create_overlap :934-955), the main loop (:198-300) -- sweeps() of every
 walker, replica exchange between adjacent windows, per-walker flatness with
 the converged flag held until every walker is flat, then ln f halved, the
 histograms reset, dos_average and dos_combine -- until ln f falls below the
-tolerance.  Replaced: the burn-in into the windows (enter_energy_window
+tolerance -- and, when asked, the radial-density samples of sweeps() with
+save_rho_E's bookkeeping (:359-396).  Replaced: the burn-in into the windows (enter_energy_window
 :643-741, a biased walk with MPI messages) is a temperature search with the
 device Metropolis kernel that stops each walker inside the central 80% of
 its window, the same acceptance region; pre-sampling, window optimisation
@@ -24,7 +25,7 @@ import numpy as np
 
 from . import K_B_IN_RY, RY_TO_EV, Batch, Setup, WangLandauWalkers
 
-__all__ = ["create_energy_bins", "divide_range", "create_overlap", "wang_landau"]
+__all__ = ["create_energy_bins", "divide_range", "create_overlap", "save_rho_E", "wang_landau"]
 
 
 def create_energy_bins(n_atoms: int, energy_min: float, energy_max: float, bins: int) -> np.ndarray:
@@ -99,12 +100,41 @@ def _burn_in(setup: Setup, V, seeds, conc, targets, n_atoms, max_rounds=400):
     return cfgs, rng_states
 
 
+def save_rho_E(W: WangLandauWalkers, radial_samples: int, state: dict) -> None:
+    """save_rho_E (src/wang-landau.F90:359-396): the walkers' radial_record
+    summed (walker order for the reference's MPI_REDUCE), radial_record_bool
+    set where the sum reaches radial_samples, and once every bin is set the
+    walkers' rho_of_E summed and divided by the bin's count (rho_saved)."""
+    if state["rho_saved"]:
+        return
+    recs, rhos = [], []
+    for w in range(W.n):
+        r, rho, _ = W.radial(w)
+        recs.append(r)
+        rhos.append(rho)
+    total = recs[0].astype(np.int64)
+    for r in recs[1:]:
+        total = total + r
+    done = total >= radial_samples
+    W.radial_set_done(done)
+    state["radial_min"] = float(np.float32(np.count_nonzero(done)) / np.float32(done.size))
+    if done.all():
+        state["rho_saved"] = True
+        s = rhos[0].copy()
+        for rho in rhos[1:]:
+            s = s + rho
+        counts = total.astype(np.float32).astype(np.float64)
+        state["rho_of_E"] = s / counts[:, None, None, None]
+
+
 def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: int = 110179,
-                exchange: bool = True, max_calls: int = 1_000_000, log=None) -> dict:
+                exchange: bool = True, max_calls: int = 1_000_000, log=None, radial=None) -> dict:
     """Runs the main loop to wl.tolerance.  wl: the wl_input fields
     (mc_sweeps, bins, num_windows, bin_overlap, tolerance, flatness, wl_f,
-    energy_min, energy_max).  Returns the combined ln g, the bin edges, the
-    windows and the iteration record."""
+    energy_min, energy_max).  radial (optional): dict(wc_range, shells,
+    radial_samples) turns on the radial-density samples.  Returns the
+    combined ln g, the bin edges, the windows, the iteration record and,
+    with radial samples, rho_of_E once every bin has its samples."""
     n_atoms = setup.n_atoms
     edges = create_energy_bins(n_atoms, wl.energy_min, wl.energy_max, wl.bins)
     windows = create_overlap(divide_range(wl.bins, wl.num_windows), wl.bin_overlap)
@@ -120,6 +150,10 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
     walkers = [dict(setup=setup, V=V, seed=seeds[r], config=cfgs[r], start_idx=windows[r // walkers_per_window][0],
                     end_idx=windows[r // walkers_per_window][1], window=r // walkers_per_window) for r in range(n)]
     W = WangLandauWalkers(walkers, edges)
+    rad_state = {"rho_saved": True, "rho_of_E": None, "radial_min": 0.0}
+    if radial is not None:
+        W.radial_enable(radial["wc_range"], radial["shells"], radial["radial_samples"], walkers_per_window)
+        rad_state["rho_saved"] = False
     f = float(wl.wl_f)
     trials = wl.mc_sweeps * n_atoms
     period = int(0.02 * float(np.float32(n_atoms)))
@@ -140,8 +174,13 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
             f *= 0.5
             W.average()
             lng = W.dos_combine()
+            if radial is not None:
+                save_rho_E(W, radial["radial_samples"], rad_state)
             record.append({"calls": calls, "wl_f": f})
             if log:
                 log(f"ln f -> {f:.3e} after {calls} sweeps() calls")
+    if radial is not None:
+        save_rho_E(W, radial["radial_samples"], rad_state)
     W.close()
-    return {"lng": lng, "bin_edges": edges, "windows": windows, "record": record, "calls": calls}
+    return {"lng": lng, "bin_edges": edges, "windows": windows, "record": record, "calls": calls,
+            "rho_of_E": rad_state["rho_of_E"], "radial_min": rad_state["radial_min"]}

@@ -293,6 +293,21 @@ int brawl_wl_swap_configs(brawl_wl *wl, int a, int b);
 /* n genrand() draws from a walker's stream (exchange shuffles and tests). */
 int brawl_wl_genrand(brawl_wl *wl, int walker, int64_t n, double *out);
 int brawl_wl_counters(brawl_wl *wl, int walker, int64_t *counters);
+/* Radial-density samples inside sweeps() (src/wang-landau.F90:566-586):
+ * while a bin's radial_record is under MAX(radial_samples / num_walkers, 1)
+ * and its radial_record_bool is unset, every n_atoms-th trial that proposes
+ * that bin adds radial_densities(wc_range, shells) of the trial
+ * configuration to the walker's rho_of_E(:, :, :, bin).  All walkers must
+ * share the lattice.  Enabling zeroes radial_record, rho_of_E,
+ * radial_mc_steps and radial_record_bool. */
+int brawl_wl_radial_enable(brawl_wl *wl, int wc_range, const double *shells, int radial_samples,
+                           int num_walkers);
+/* radial_record_bool (bins bytes, 0/1), as save_rho_E sets it; when every
+ * bin is set, sampling stops (rho_saved). */
+int brawl_wl_radial_set_done(brawl_wl *wl, const uint8_t *done);
+/* One walker's radial_record (bins), rho_of_E (bins * wc * ns * ns, i
+ * fastest; may be NULL) and radial_mc_steps (may be NULL). */
+int brawl_wl_radial_get(brawl_wl *wl, int walker, int32_t *record, double *rho_of_E, int32_t *steps);
 
 /* ====================================================================== */
 /* Serving: a request loop that admits anneal, Wang-Landau and nested-    */

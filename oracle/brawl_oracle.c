@@ -774,6 +774,17 @@ int64_t bo_wl_sweep(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
                     bo_rng *r, const double *bin_edges, double *lng,
                     double *hist, double *energy, bo_counters *c)
 {
+    return bo_wl_sweep_radial(m, p, cfg, r, bin_edges, lng, hist, energy, c, NULL);
+}
+
+int64_t bo_wl_sweep_radial(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
+                           bo_rng *r, const double *bin_edges, double *lng,
+                           double *hist, double *energy, bo_counters *c,
+                           const bo_wl_radial *rad)
+{
+    const int n_atoms = bo_n_atoms(m);
+    const int per_bin = rad ? m->ns * m->ns * rad->wc_range : 0;
+    double rho_buf[15 * 15 * 64];
     int64_t accepted = 0;
     double e_unswapped = *energy;
     for (int64_t i = 1; i <= p->n_trials; i++) {
@@ -796,6 +807,17 @@ int64_t bo_wl_sweep(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
         int ibin = bo_wl_bin_index(e_unswapped, bin_edges, p->bins);
         int jbin = bo_wl_bin_index(e_swapped, bin_edges, p->bins);
         int hist_tick = (p->hist_period > 0) && (i % p->hist_period == 0);
+        if (rad && rad->wc_range > 0 && jbin < p->bins + 1 && jbin > 0 &&
+            rad->record[jbin - 1] < rad->cap && !rad->done[jbin - 1]) {
+            *rad->steps += 1;
+            if (*rad->steps >= n_atoms) {
+                *rad->steps = 0;
+                rad->record[jbin - 1] += 1;
+                bo_radial_densities(m, cfg, rad->wc_range, rad->shells, rho_buf, NULL);
+                double *dst = rad->rho_of_E + (size_t)(jbin - 1) * per_bin;
+                for (int k = 0; k < per_bin; k++) dst[k] = dst[k] + rho_buf[k];
+            }
+        }
         if (jbin > p->start_idx - 1 && jbin < p->end_idx + 1) {
             if (c) { c->draws++; c->exp_tests++; }
             if (log(bo_rng_uniform(r)) < (lng[ibin - 1] - lng[jbin - 1])) {

@@ -160,6 +160,24 @@ typedef struct {
  * hist: window-local (end-start+1).  energy in/out is the walker's running
  * e_unswapped (the reference recomputes it with full_energy at entry; the
  * caller passes that value).  Returns accepted moves. */
+/* The radial-density samples sweeps() takes per bin (src/wang-landau.F90:
+ * 566-586): while the bin's radial_record is under cap and radial_record_bool
+ * is unset, every n_atoms-th such trial adds radial_densities of the trial
+ * configuration (the swap applied, before the decision) to rho_of_E. */
+typedef struct {
+    int wc_range;               /* 0: no sampling (rho_saved) */
+    const double *shells;       /* wc_range distances */
+    int cap;                    /* MAX(radial_samples / num_walkers, 1) */
+    const unsigned char *done;  /* radial_record_bool, bins */
+    int32_t *record;            /* radial_record, bins (this walker) */
+    double *rho_of_E;           /* rho_of_E(i, j, l, bin), i fastest */
+    int32_t *steps;             /* radial_mc_steps, carried between calls */
+} bo_wl_radial;
+
+int64_t bo_wl_sweep_radial(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
+                           bo_rng *r, const double *bin_edges, double *lng,
+                           double *hist, double *energy, bo_counters *c,
+                           const bo_wl_radial *rad);
 int64_t bo_wl_sweep(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
                     bo_rng *r, const double *bin_edges, double *lng,
                     double *hist, double *energy, bo_counters *c);

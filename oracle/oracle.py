@@ -67,6 +67,11 @@ class NsParams(C.Structure):
     _fields_ = [("n_walkers", C.c_int), ("n_steps", C.c_int), ("n_iter", C.c_int)]
 
 
+class WlRadial(C.Structure):
+    _fields_ = [("wc_range", C.c_int), ("shells", C.c_void_p), ("cap", C.c_int), ("done", C.c_void_p),
+                ("record", C.c_void_p), ("rho_of_E", C.c_void_p), ("steps", C.c_void_p)]
+
+
 class WlParams(C.Structure):
     _fields_ = [("bins", C.c_int), ("start_idx", C.c_int), ("end_idx", C.c_int),
                 ("n_trials", C.c_int64), ("wl_f", C.c_double), ("hist_period", C.c_int),
@@ -122,6 +127,9 @@ def lib():
         L.bo_wl_sweep.argtypes = [C.POINTER(Model), C.POINTER(WlParams), vp, C.POINTER(Rng), vp,
                                   vp, vp, vp, C.POINTER(Counters)]
         L.bo_wl_sweep.restype = i64
+        L.bo_wl_sweep_radial.argtypes = [C.POINTER(Model), C.POINTER(WlParams), vp, C.POINTER(Rng), vp,
+                                         vp, vp, vp, C.POINTER(Counters), C.POINTER(WlRadial)]
+        L.bo_wl_sweep_radial.restype = i64
         L.bo_wl_replica_exchange.argtypes = [C.c_int, C.c_int, vp, vp, vp, C.c_int, vp, vp,
                                              C.POINTER(Rng), vp, C.c_size_t, vp, vp]
         L.bo_wl_dos_combine.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
@@ -293,12 +301,25 @@ class OracleModel:
         return acc, float(e[0]), c
 
     def wl_sweep(self, cfg, rng, bin_edges, lng, hist, energy, bins, start_idx, end_idx, n_trials,
-                 wl_f, hist_period, nbr_swap=False):
+                 wl_f, hist_period, nbr_swap=False, radial=None):
+        """radial (optional): dict(shells, cap, done (uint8, bins), record
+        (int32, bins), rho_of_E (float64, (bins, wc, ns, ns)), steps (int32,
+        1)), updated in place."""
         e = np.array([energy], dtype=np.float64)
         p = WlParams(bins, start_idx, end_idx, n_trials, wl_f, hist_period, int(bool(nbr_swap)))
         c = Counters()
-        acc = lib().bo_wl_sweep(C.byref(self.m), C.byref(p), _ptr(cfg), C.byref(rng.s), _ptr(bin_edges),
-                                _ptr(lng), _ptr(hist), _ptr(e), C.byref(c))
+        rad = None
+        if radial is not None:
+            for k, dt in (("shells", np.float64), ("done", np.uint8), ("record", np.int32),
+                          ("rho_of_E", np.float64), ("steps", np.int32)):
+                a = radial[k]
+                assert a.dtype == dt and a.flags.c_contiguous, k
+            rad = WlRadial(radial["shells"].size, radial["shells"].ctypes.data, int(radial["cap"]),
+                           radial["done"].ctypes.data, radial["record"].ctypes.data,
+                           radial["rho_of_E"].ctypes.data, radial["steps"].ctypes.data)
+        acc = lib().bo_wl_sweep_radial(C.byref(self.m), C.byref(p), _ptr(cfg), C.byref(rng.s),
+                                       _ptr(bin_edges), _ptr(lng), _ptr(hist), _ptr(e), C.byref(c),
+                                       None if rad is None else C.byref(rad))
         return acc, float(e[0]), c
 
 

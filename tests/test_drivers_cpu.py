@@ -85,3 +85,42 @@ def test_decorrelated_samples_host_logic():
     assert all(np.array_equal(a, b) for a, b in zip(out["configs"], cfgs))
     assert np.array_equal(cfg_a, cfg_b)  # the 200 trials after the last sample ran too
     assert np.array_equal(ra.state_words(), rb.state_words())
+
+
+class FakeRadialWalkers:
+    """The radial interface save_rho_E uses, over fixed arrays."""
+
+    def __init__(self, records, rhos):
+        self.records, self.rhos, self.n = records, rhos, len(records)
+        self.done = None
+
+    def radial(self, w):
+        return self.records[w].copy(), self.rhos[w].copy(), 0
+
+    def radial_set_done(self, done):
+        self.done = np.asarray(done, dtype=bool).copy()
+
+
+def test_save_rho_E_bookkeeping():
+    """save_rho_E (src/wang-landau.F90:359-396): bins complete when the
+    walkers' summed radial_record reaches radial_samples; rho_saved (and the
+    averaged rho_of_E) only once every bin is complete."""
+    from brawl_gb300.wang_landau import save_rho_E
+    rng = np.random.default_rng(3)
+    bins, wc, ns = 6, 2, 3
+    recs = [np.array([2, 0, 3, 1, 2, 2], dtype=np.int32), np.array([1, 2, 0, 2, 1, 2], dtype=np.int32)]
+    rhos = [rng.uniform(0, 1, (bins, wc, ns, ns)) for _ in recs]
+    W = FakeRadialWalkers(recs, rhos)
+    st = {"rho_saved": False, "rho_of_E": None, "radial_min": 0.0}
+    save_rho_E(W, 3, st)
+    assert list(W.done) == [True, False, True, True, True, True]
+    assert not st["rho_saved"] and st["rho_of_E"] is None
+    assert st["radial_min"] == float(np.float32(5) / np.float32(6))
+    W.records[0][1] = 1
+    save_rho_E(W, 3, st)
+    assert W.done.all() and st["rho_saved"]
+    total = (W.records[0] + W.records[1]).astype(np.float64)
+    assert np.array_equal(st["rho_of_E"], (rhos[0] + rhos[1]) / total[:, None, None, None])
+    W.done = None
+    save_rho_E(W, 3, st)                 # rho_saved: nothing more happens
+    assert W.done is None

@@ -204,3 +204,79 @@ def test_wang_landau_exchange_needs_equal_windows():
     with pytest.raises(B.BrawlError) as ex:
         wl.replica_exchange()
     assert ex.value.code == 1
+
+
+@pytest.mark.parametrize("nbr", [False, True])
+def test_wang_landau_radial_samples_match_oracle(nbr):
+    """sweeps() with the radial-density samples (src/wang-landau.F90:566-586):
+    radial_record, rho_of_E and radial_mc_steps per walker equal the
+    oracle's, bit for bit, also after radial_record_bool marks some bins and
+    once every bin is marked (rho_saved)."""
+    rng = np.random.default_rng(33)
+    lattice, n, ns, nsh, wc = "bcc", (4, 4, 4), 4, 6, 3
+    V = random_V(rng, ns, nsh)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    mod0 = O.OracleModel(lattice, *n, V)
+    windows = [(1, 30), (19, 48)]
+    walkers, mods, cfgs, rngs = [], [], [], []
+    r0 = O.OracleRng(777)
+    for win, (lo, hi) in enumerate(windows):
+        for rep in range(2):
+            cfg, _ = mod0.initial_setup(r0, conc_vector(ns))
+            seed = 110179 + 11 * len(walkers)
+            walkers.append(dict(setup=setup, V=V, seed=seed, config=cfg.copy(), start_idx=lo,
+                                end_idx=hi, window=win, nbr_swap=nbr))
+            mods.append(O.OracleModel(lattice, *n, V))
+            cfgs.append(cfg.copy())
+            rngs.append(O.OracleRng(seed))
+    E = np.array([mod0.total_energy(c) for c in cfgs])
+    bins = 48
+    half = max(float(np.ptp(E)), 0.02) * 4.0
+    bin_edges = float(E.mean()) - half + (np.arange(bins + 1) * (2 * half / bins))
+    shells = mod0.lattice_shells(cfgs[0], wc)
+    radial_samples, num_walkers = 5, 2
+    cap = max(radial_samples // num_walkers, 1)
+    done = np.zeros(bins, dtype=np.uint8)
+    rads = [{"shells": np.ascontiguousarray(shells), "cap": cap, "done": done,
+             "record": np.zeros(bins, dtype=np.int32), "rho_of_E": np.zeros((bins, wc, ns, ns)),
+             "steps": np.zeros(1, dtype=np.int32)} for _ in walkers]
+    lngs = [np.zeros(bins) for _ in walkers]
+    hists = [np.zeros(w["end_idx"] - w["start_idx"] + 1) for w in walkers]
+    wl = B.WangLandauWalkers(walkers, bin_edges)
+    wl.radial_enable(wc, shells, radial_samples, num_walkers)
+    wl_f = float(np.float32(0.05))
+    period = int(0.02 * float(np.float32(setup.n_atoms)))
+    for call in range(4):
+        if call == 2:
+            done[::3] = 1                    # save_rho_E marked some bins
+            wl.radial_set_done(done)
+        if call == 3:
+            done[:] = 1                      # rho_saved: no more samples
+            wl.radial_set_done(done)
+        acc_o = []
+        for k, w in enumerate(walkers):
+            e = mods[k].total_energy(cfgs[k])
+            a, _, _ = mods[k].wl_sweep(cfgs[k], rngs[k], bin_edges, lngs[k], hists[k], e, bins,
+                                       w["start_idx"], w["end_idx"], 1500, wl_f, period, nbr_swap=nbr,
+                                       radial=None if call == 3 else rads[k])
+            acc_o.append(a)
+        for win in range(len(windows)):
+            idx = [k for k, w in enumerate(walkers) if w["window"] == win]
+            inv = float(np.float32(len(idx)))
+            for arrs in (lngs, hists):
+                s = arrs[idx[0]].copy()
+                for k in idx[1:]:
+                    s = s + arrs[k]
+                s = s / inv
+                for k in idx:
+                    arrs[k][:] = s
+        acc_g = wl.sweeps(1500, wl_f, period)
+        assert list(acc_g) == acc_o
+        for k in range(len(walkers)):
+            rec, rho, steps = wl.radial(k)
+            assert np.array_equal(rec, rads[k]["record"]), (call, k)
+            assert np.array_equal(rho, rads[k]["rho_of_E"]), (call, k)
+            assert steps == int(rads[k]["steps"][0]), (call, k)
+            assert np.array_equal(wl.config(k), cfgs[k])
+            assert np.array_equal(wl.lng(k), lngs[k])
+    assert sum(int(r["record"].sum()) for r in rads) > 8

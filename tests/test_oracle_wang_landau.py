@@ -166,17 +166,23 @@ BCC_NBRS = [(1, 1, 1), (1, 1, -1), (1, -1, 1), (1, -1, -1), (-1, 1, 1), (-1, 1, 
             (-1, -1, -1)]
 
 
-def _py_sweeps_nbr(mod, n, cfg, rng, edges, lng, hist, e, bins, start, end, n_trials, f, period):
+def _py_sweeps_nbr(mod, n, cfg, rng, edges, lng, hist, e, bins, start, end, n_trials, f, period,
+                   nbr=True, radial=None):
     """sweeps (src/wang-landau.F90:539-632) with select_sites_nbr (:1527-1532)
-    written out from the reference, on a bcc lattice n x n x n; the site draw
-    and the pair energies come from the oracle."""
+    or select_sites, and the radial-density samples (:566-586), written out
+    from the reference, on a bcc lattice n x n x n; the site draw, the pair
+    energies and radial_densities come from the oracle."""
     W = 2 * n
+    n_atoms = 2 * n ** 3
     acc = 0
     for i in range(1, n_trials + 1):
         a = mod.random_site(rng)
-        k = int(math.floor(8.0 * rng.uniform()))          # bcc_random_nbr: floor(8 u) + 1
-        d = BCC_NBRS[k]
-        b = tuple((a[c] + d[c]) % W for c in range(3))
+        if nbr:
+            k = int(math.floor(8.0 * rng.uniform()))      # bcc_random_nbr: floor(8 u) + 1
+            d = BCC_NBRS[k]
+            b = tuple((a[c] + d[c]) % W for c in range(3))
+        else:
+            b = mod.random_site(rng)
         s1, s2 = cfg[a[2], a[1], a[0]], cfg[b[2], b[1], b[0]]
         p_un = mod.pair_energy(cfg, a, b)
         cfg[a[2], a[1], a[0]], cfg[b[2], b[1], b[0]] = s2, s1
@@ -184,6 +190,14 @@ def _py_sweeps_nbr(mod, n, cfg, rng, edges, lng, hist, e, bins, start, end, n_tr
         if s1 != s2:
             e_sw = e - p_un + mod.pair_energy(cfg, a, b)
         ib, jb = _py_bin(e, edges, bins), _py_bin(e_sw, edges, bins)
+        if radial is not None and 0 < jb < bins + 1:
+            if radial["record"][jb - 1] < radial["cap"] and not radial["done"][jb - 1]:
+                radial["steps"][0] += 1
+                if radial["steps"][0] >= n_atoms:
+                    radial["steps"][0] = 0
+                    radial["record"][jb - 1] += 1
+                    rho, _ = mod.radial_densities(cfg, radial["shells"])
+                    radial["rho_of_E"][jb - 1] = radial["rho_of_E"][jb - 1] + rho
         if start - 1 < jb < end + 1 and math.log(rng.uniform()) < lng[ib - 1] - lng[jb - 1]:
             acc += 1
             e = e_sw
@@ -223,3 +237,47 @@ def test_sweeps_with_neighbour_swaps_match_python_restatement():
     assert np.array_equal(lng_a, lng_b) and np.array_equal(hist_a, hist_b)
     assert np.array_equal(ra.state_words(), rb.state_words())
     assert c.draws == 4 * n_trials + c.exp_tests
+
+
+def _radial_state(bins, wc, ns, cap, done_every=0):
+    done = np.zeros(bins, dtype=np.uint8)
+    if done_every:
+        done[::done_every] = 1
+    return {"shells": None, "cap": cap, "done": done, "record": np.zeros(bins, dtype=np.int32),
+            "rho_of_E": np.zeros((bins, wc, ns, ns)), "steps": np.zeros(1, dtype=np.int32)}
+
+
+@pytest.mark.parametrize("nbr", [False, True])
+def test_sweeps_radial_samples_match_python_restatement(nbr):
+    """rho_of_E, radial_record and radial_mc_steps of sweeps() against the
+    reference's lines written out, with some bins already complete
+    (radial_record_bool) and a per-walker cap of 2 samples."""
+    rng = np.random.default_rng(9)
+    ns, nsh, n, wc = 3, 2, 3, 3
+    V = np.zeros((ns, ns, nsh))
+    for sh in range(nsh):
+        a = rng.uniform(-0.05, 0.05, size=(ns, ns))
+        V[:, :, sh] = (np.triu(a) + np.triu(a, 1).T) / 13.605693122
+    mod = O.OracleModel("bcc", n, n, n, V)
+    cfg, _ = mod.initial_setup(O.OracleRng(5), np.array([0.0, 1 / 3, 1 / 3, 1 / 3]), np.array([18, 18, 18]))
+    shells = mod.lattice_shells(cfg, wc)
+    e0 = mod.total_energy(cfg)
+    bins = 40
+    edges = (e0 - 0.03) + np.arange(bins + 1) * (0.06 / bins)
+    start, end, n_trials, period = 5, 35, 6000, 1
+    ra, rb = _radial_state(bins, wc, ns, 2, 7), _radial_state(bins, wc, ns, 2, 7)
+    ra["shells"] = rb["shells"] = np.ascontiguousarray(shells)
+    ra["steps"][0] = rb["steps"][0] = 17
+    cfg_a, cfg_b = cfg.copy(), cfg.copy()
+    lng_a, lng_b = np.zeros(bins), np.zeros(bins)
+    hist_a, hist_b = np.zeros(end - start + 1), np.zeros(end - start + 1)
+    ga, gb = O.OracleRng(31), O.OracleRng(31)
+    acc_a, e_a, _ = mod.wl_sweep(cfg_a, ga, edges, lng_a, hist_a, e0, bins, start, end, n_trials, 1.0, period,
+                                 nbr_swap=nbr, radial=ra)
+    acc_b, e_b = _py_sweeps_nbr(mod, n, cfg_b, gb, edges, lng_b, hist_b, e0, bins, start, end, n_trials,
+                                1.0, period, nbr=nbr, radial=rb)
+    assert acc_a == acc_b and e_a == e_b and np.array_equal(cfg_a, cfg_b)
+    assert np.array_equal(ra["record"], rb["record"]) and ra["record"].sum() > 3
+    assert np.array_equal(ra["rho_of_E"], rb["rho_of_E"])
+    assert ra["steps"][0] == rb["steps"][0]
+    assert np.all(ra["record"][::7] == 0) and np.all(ra["record"] <= 2)
