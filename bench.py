@@ -444,6 +444,61 @@ def walker_legs(args) -> dict:
     return out
 
 
+def anneal_leg(args) -> dict:
+    """The reference's own serial case: simulated annealing of one fcc 8^3
+    chain (2048 sites, 2 species 1024/1024, 2 shells, V uniform +-0.05 eV),
+    T = 1500 -> 300 K in 13 steps of 1000 sweeps, the energy sampled every
+    sweep, ASRO off, static seed of rank 0.  The GPU runs all of it through
+    the annealing driver (one chain: a latency-bound sequence of trials);
+    the oracle a bounded sample of its first temperatures on one host core."""
+    import torch
+    import brawl_gb300 as B
+    from brawl_gb300 import inputs as I
+    from brawl_gb300 import metropolis as M
+    from brawl_gb300 import serving as SV
+    from oracle import oracle as O
+    rng = np.random.default_rng(20260)
+    V = SV.symmetric_V(rng, 2, 2, 0.05)
+    setup = B.Setup("fcc", 8, 8, 8, 2, 2)
+    N = setup.n_atoms
+    conc = np.array([0.0, 0.5, 0.5])
+    nums = np.array([1024, 1024], dtype=np.int64)
+
+    def params(T_steps):
+        return I.MetropolisParams(mode="simulated_annealing", n_mc_steps=1000 * N, n_sample_steps=N,
+                                  calculate_energies=True, calculate_asro=False, n_sample_steps_asro=N,
+                                  n_sample_steps_trajectory=N, T=1500.0, T_steps=T_steps, delta_T=-100.0)
+    ch = B.Chain(setup, V)
+    ch.f90_init_genrand(0, 0)
+    ch.initial_setup(conc, nums)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = M.simulated_annealing(ch, params(13), 2, record_configs=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    trials = 13 * 1000 * N
+    mod = O.OracleModel("fcc", 8, 8, 8, V)
+    r = O.OracleRng(O.lib().bo_static_seed(0))
+    cfg, _ = mod.initial_setup(r, conc, nums)
+    m2 = params(args.anneal_cpu_temperatures)
+    ap = dict(T=m2.T, delta_T=m2.delta_T, T_steps=m2.T_steps, n_mc_steps=m2.n_mc_steps, n_burn_in_steps=0,
+              n_sample_steps=m2.n_sample_steps, n_sample_steps_asro=m2.n_sample_steps_asro,
+              n_sample_steps_alro=0, n_sample_steps_trajectory=m2.n_sample_steps_trajectory, burn_in=0,
+              burn_in_start=0, calculate_energies=1, calculate_asro=0, nbr_swap=0, wc_range=2)
+    t1 = time.perf_counter()
+    ref = mod.anneal(cfg, r, ap)
+    cdt = time.perf_counter() - t1
+    k = args.anneal_cpu_temperatures
+    same = bool(np.array_equal(ref["energies_of_T"][:k], out["energies_of_T"][:k]))
+    return {"metric": "swap trials/s (one chain)", "value": trials / dt, "unit": "trials/s",
+            "workload": "simulated annealing, fcc 8^3, 2 species, 2 shells, T 1500 -> 300 K in 13 steps "
+                        "of 1000 sweeps, energy every sweep, one chain",
+            "seconds": dt,
+            "cpu_baseline": {"value": k * 1000 * N / cdt, "unit": "trials/s", "cores": 1, "kind": "port",
+                             "sample": f"the first {k} temperatures on the oracle, {cdt:.1f} s"},
+            "energies_match_oracle": same}
+
+
 def max_over_ranks(x: float, world: int, device=None) -> float:
     """The largest x over the ranks (the job's time is its slowest rank's)."""
     if world <= 1:
@@ -516,6 +571,8 @@ def main() -> int:
                     help="run only the walker legs and print their JSON")
     ap.add_argument("--wl-calls", type=int, default=5)
     ap.add_argument("--ns-iterations", type=int, default=50)
+    ap.add_argument("--anneal-leg", type=int, default=1, help="time the one-chain annealing case (0: skip)")
+    ap.add_argument("--anneal-cpu-temperatures", type=int, default=3)
     ap.add_argument("--ns-runs", type=int, default=152,
                     help="independent nested-sampling runs of the replica-parallel measurement")
     ap.add_argument("--speculation", type=int, default=0,
@@ -661,6 +718,7 @@ def main() -> int:
     if rank == 0 and world == 1 and not args.no_serve and args.serve_jobs > 0:
         serving = serving_leg(args)
     walkers = walker_legs(args) if rank == 0 and world == 1 and args.walker_legs else {}
+    anneal = anneal_leg(args) if rank == 0 and world == 1 and args.anneal_leg else None
 
     if rank == 0:
         line = {
@@ -689,6 +747,7 @@ def main() -> int:
             "serving": serving,
             "wang_landau": walkers.get("wang_landau"),
             "nested_sampling": walkers.get("nested_sampling"),
+            "anneal_one_chain": anneal,
             "clocks": clk,
             "gpu_launches": args.steps,
             "counters": {"trials": T_all, "evaluated": T_eval, "draws": draws,
