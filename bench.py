@@ -12,8 +12,10 @@ one launch; 50 steps of 10 sweeps make the 500-sweep run.
 Reported:
   value        trials/s with all state resident in HBM (device-timed)
   e2e          trials/s through the C ABI with host buffers: every step
-               copies all replicas' configurations host->device, runs, and
-               copies them back (plus the accept counts)
+               moves all replicas' configurations host->device, runs, and
+               moves them back (plus the accept counts), one call
+               (brawl_batch_metropolis_host) whose kernels read and write
+               the pinned host buffer in place
   roofline     algorithmic bytes per launch / kernel time, against the
                measured HBM copy bandwidth
   cpu_baseline the CPU oracle (a restatement of the reference's serial
@@ -677,9 +679,10 @@ def main() -> int:
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        batch.set_configs(host_grids)          # h2d: every replica's config
-        acc = batch.metropolis(trials)         # launch + wait + accept counts (d2h)
-        batch.get_configs(host_grids)          # d2h: every replica's config
+        # every replica's config from the pinned host buffer, the run, the
+        # configs back into it and the accept counts: one call, the kernels
+        # reading and writing the page-locked buffer in place (NVLink-C2C)
+        acc = batch.metropolis_host(host_grids, trials)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
     e2e_value = world * trials_per_step * e2e_steps / e2e_s

@@ -148,6 +148,7 @@ def load(rebuild: bool = False):
         "brawl_batch_rng_get": ([vp, i, vp], i),
         "brawl_batch_get_configs": ([vp, vp], i),
         "brawl_batch_set_configs": ([vp, vp], i),
+        "brawl_batch_metropolis_host": ([vp, vp, vp, vp, vp], i),
         "brawl_batch_counters": ([vp, vp], i),
         "brawl_batch_radial_densities": ([vp, i, i, vp, vp], i),
     }
@@ -442,6 +443,19 @@ class Batch:
     def set_configs(self, grids: np.ndarray) -> None:
         assert grids.dtype == np.int8 and grids.size == self.grid_bytes and grids.flags.c_contiguous
         _check(load().brawl_batch_set_configs(self._h, _ptr(grids)))
+
+    def metropolis_host(self, grids_in: np.ndarray, n_trials, grids_out: np.ndarray | None = None) -> np.ndarray:
+        """set_configs + metropolis + get_configs in one call from host
+        buffers (page-locked ones are used in place by the kernels);
+        grids_out defaults to grids_in.  Returns the accepted moves."""
+        if grids_out is None:
+            grids_out = grids_in
+        for g in (grids_in, grids_out):
+            assert g.dtype == np.int8 and g.size == self.grid_bytes and g.flags.c_contiguous
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(n_trials, dtype=np.int64), (self.n,)))
+        acc = np.zeros(self.n, dtype=np.int64)
+        _check(load().brawl_batch_metropolis_host(self._h, _ptr(grids_in), _ptr(t), _ptr(grids_out), _ptr(acc)))
+        return acc
 
     def counters(self) -> np.ndarray:
         out = np.zeros((self.n, NUM_COUNTERS), dtype=np.int64)

@@ -857,6 +857,49 @@ int brawl_batch_set_configs(brawl_batch* b, const int8_t* configs) {
   return BRAWL_OK;
 }
 
+// The device address of a page-locked, 16-byte aligned host buffer (the
+// batch conversions read and write it 4 bytes at a time), or null.
+static const void* host_alias(const void* p) {
+  if (reinterpret_cast<uintptr_t>(p) & 15u) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+int brawl_batch_metropolis_host(brawl_batch* b, const int8_t* configs_in, const int64_t* n_trials,
+                                int8_t* configs_out, int64_t* accepted) {
+  if (!b || !configs_in || !n_trials || !configs_out) return fail(BRAWL_EINVAL, "null argument");
+  TRY(ensure_grids(b));
+  const int n = (int)b->jobs.size();
+  cudaStream_t s = b->stream;
+  const int8_t* src = static_cast<const int8_t*>(host_alias(configs_in));
+  if (!src) {
+    CUDA_TRY(cudaMemcpyAsync(b->d_grids, configs_in, (size_t)b->total_cells, cudaMemcpyHostToDevice, s));
+    src = b->d_grids;
+  }
+  // a chain whose grid holds a bad species is flagged here and runs no trial
+  launch_pack_batch(b->d_gjobs, n, b->total_cells, src, s);
+  CUDA_TRY(cudaGetLastError());
+  TRY(run_metropolis(b, n_trials, nullptr, false, s, false));
+  int8_t* dst = static_cast<int8_t*>(const_cast<void*>(host_alias(configs_out)));
+  launch_unpack_batch(b->d_gjobs, n, b->total_cells, dst ? dst : b->d_grids, s);
+  CUDA_TRY(cudaGetLastError());
+  if (!dst)
+    CUDA_TRY(cudaMemcpyAsync(configs_out, b->d_grids, (size_t)b->total_cells, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  std::vector<unsigned long long> cnt;
+  TRY(read_counters(b, cnt));
+  if (accepted)
+    for (int c = 0; c < n; ++c)
+      accepted[c] = (int64_t)(cnt[c * kNumCounters + kCntAccepted] -
+                              b->last_counters[c * kNumCounters + kCntAccepted]);
+  b->last_counters = cnt;
+  return check_status(b);
+}
+
 int brawl_batch_rng_get(brawl_batch* b, int c, uint32_t state[625]) {
   if (!b || !state || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad argument");
   CUDA_TRY(cudaMemcpyAsync(state, b->jobs[c].rng, (kMTN + 1) * 4, cudaMemcpyDeviceToHost, b->stream));

@@ -169,60 +169,87 @@ void launch_unpack(const Geom& g, const int8_t* d_lat, int8_t* d_grid, cudaStrea
   unpack_kernel<<<blocks, 256, 0, stream>>>(g, d_lat, d_grid);
 }
 
-__device__ __forceinline__ int find_grid_job(const GridJob* jobs, int n, int64_t t) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].grid_offset <= t) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
-__global__ void pack_batch_kernel(const GridJob* __restrict__ jobs, int n_jobs, int64_t total,
-                                  const int8_t* __restrict__ grids) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const GridJob& J = jobs[find_grid_job(jobs, n_jobs, t)];
-    const int64_t c = t - J.grid_offset;
-    const int W1 = 2 * J.g.n1, W2 = 2 * J.g.n2;
-    const int x = (int)(c % W1), y = (int)((c / W1) % W2), z = (int)(c / ((int64_t)W1 * W2));
-    const int8_t s = grids[t];
-    if (occupied(J.g, x, y, z)) {
-      J.lat[compact_index(J.g, x, y, z)] = s;
-      if (s < 1 || s > J.g.ns) *J.status = kStatusBadSpecies;
-    } else if (s != 0) {
-      *J.status = kStatusBadSpecies;
+// Batch layout conversions: one row of blocks per chain (blockIdx.y), each
+// thread four consecutive cells of the chain's grid (grids are multiples of
+// 8 cells, 8-byte aligned), so the grids -- possibly page-locked host
+// memory read or written in place -- stream through in 4-byte accesses.
+__global__ void pack_batch_kernel(const GridJob* __restrict__ jobs, const int8_t* __restrict__ grids) {
+  const GridJob& J = jobs[blockIdx.y];
+  const int W1 = 2 * J.g.n1, W2 = 2 * J.g.n2;
+  const int64_t quads = (int64_t)2 * J.g.n1 * J.g.n2 * J.g.n3;  // cells / 4
+  const bool small = quads < ((int64_t)1 << 29);                  // 4 q fits in 32 bits
+  const char4* src = reinterpret_cast<const char4*>(grids + J.grid_offset);
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < quads;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const char4 v = src[q];
+    const int8_t s4[4] = {v.x, v.y, v.z, v.w};
+    const int row = small ? (int)(4 * q) / W1 : (int)((4 * q) / W1);  // < W2 * W3
+    int x = (int)(4 * q - (int64_t)row * W1), y = row % W2, z = row / W2;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int8_t s = s4[k];
+      if (occupied(J.g, x, y, z)) {
+        J.lat[compact_index(J.g, x, y, z)] = s;
+        if (s < 1 || s > J.g.ns) *J.status = kStatusBadSpecies;
+      } else if (s != 0) {
+        *J.status = kStatusBadSpecies;
+      }
+      if (++x == W1) {  // the quad runs on into the next row
+        x = 0;
+        if (++y == W2) {
+          y = 0;
+          ++z;
+        }
+      }
     }
   }
 }
 
-__global__ void unpack_batch_kernel(const GridJob* __restrict__ jobs, int n_jobs, int64_t total,
-                                    int8_t* __restrict__ grids) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const GridJob& J = jobs[find_grid_job(jobs, n_jobs, t)];
-    const int64_t c = t - J.grid_offset;
-    const int W1 = 2 * J.g.n1, W2 = 2 * J.g.n2;
-    const int x = (int)(c % W1), y = (int)((c / W1) % W2), z = (int)(c / ((int64_t)W1 * W2));
-    grids[t] = occupied(J.g, x, y, z) ? J.lat[compact_index(J.g, x, y, z)] : (int8_t)0;
+__global__ void unpack_batch_kernel(const GridJob* __restrict__ jobs, int8_t* __restrict__ grids) {
+  const GridJob& J = jobs[blockIdx.y];
+  const int W1 = 2 * J.g.n1, W2 = 2 * J.g.n2;
+  const int64_t quads = (int64_t)2 * J.g.n1 * J.g.n2 * J.g.n3;
+  const bool small = quads < ((int64_t)1 << 29);
+  char4* dst = reinterpret_cast<char4*>(grids + J.grid_offset);
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < quads;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    int8_t s4[4];
+    const int row = small ? (int)(4 * q) / W1 : (int)((4 * q) / W1);
+    int x = (int)(4 * q - (int64_t)row * W1), y = row % W2, z = row / W2;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      s4[k] = occupied(J.g, x, y, z) ? J.lat[compact_index(J.g, x, y, z)] : (int8_t)0;
+      if (++x == W1) {
+        x = 0;
+        if (++y == W2) {
+          y = 0;
+          ++z;
+        }
+      }
+    }
+    dst[q] = make_char4(s4[0], s4[1], s4[2], s4[3]);
   }
+}
+
+// blocks per chain: enough threads for the largest grid's quads, at most 32
+static dim3 batch_grid(int n_jobs, int64_t total_cells) {
+  const int64_t per = total_cells / 4 / (n_jobs > 0 ? n_jobs : 1);
+  int64_t bx = (per + 255) / 256;
+  if (bx < 1) bx = 1;
+  if (bx > 32) bx = 32;
+  return dim3((unsigned)bx, (unsigned)n_jobs);
 }
 
 void launch_pack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells,
                        const int8_t* d_grids, cudaStream_t stream) {
-  int64_t blocks = (total_cells + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
   BRAWL_CARVEOUT(pack_batch_kernel);
-  if (n_jobs > 0) pack_batch_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_cells, d_grids);
+  if (n_jobs > 0) pack_batch_kernel<<<batch_grid(n_jobs, total_cells), 256, 0, stream>>>(d_jobs, d_grids);
 }
 
 void launch_unpack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells, int8_t* d_grids,
                          cudaStream_t stream) {
-  int64_t blocks = (total_cells + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
   BRAWL_CARVEOUT(unpack_batch_kernel);
-  if (n_jobs > 0) unpack_batch_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_cells, d_grids);
+  if (n_jobs > 0) unpack_batch_kernel<<<batch_grid(n_jobs, total_cells), 256, 0, stream>>>(d_jobs, d_grids);
 }
 
 }  // namespace brawl

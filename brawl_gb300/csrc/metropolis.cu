@@ -39,6 +39,7 @@ template <int NJ, bool kSmemLat, bool kUseD>
 __global__ void __launch_bounds__(32) metropolis_kernel(const ChainJob* __restrict__ jobs) {
   extern __shared__ __align__(16) unsigned char smem[];
   const ChainJob J = jobs[blockIdx.x];
+  if (J.status && *J.status != 0) return;  // the chain's input was flagged: no trial runs
   const Geom g = J.g;
   const int lane = threadIdx.x;
   __shared__ unsigned long long s_t_start;  // kept out of registers

@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   extern __shared__ uint32_t s_u32[];
   extern __shared__ int8_t s_i8[];
   const ChainJob* Jg = jobs + blockIdx.x;
+  if (Jg->status && *Jg->status != 0) return;  // the chain's input was flagged: no trial runs
   const Geom g = Jg->g;
   const HaloGeom H = Jg->hg;
   const int lane = threadIdx.x;

@@ -113,6 +113,7 @@ __global__ void __launch_bounds__(32 * (NC * (NC + 1) / 2))
   __shared__ SpecSlot slots[W];
   __shared__ unsigned long long s_t_start;
   const ChainJob* Jg = jobs + blockIdx.x;
+  if (Jg->status && *Jg->status != 0) return;  // the chain's input was flagged: no trial runs
   const Geom g = Jg->g;
   const HaloGeom H = Jg->hg;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;

@@ -187,6 +187,14 @@ int brawl_batch_set_config(brawl_batch *batch, int chain, const int8_t *config);
  * concatenated in chain order (the host side of the ensemble). */
 int brawl_batch_get_configs(brawl_batch *batch, int8_t *configs);
 int brawl_batch_set_configs(brawl_batch *batch, const int8_t *configs);
+/* set_configs, metropolis_run and get_configs as one call from host
+ * buffers (every chain's grid, as set_configs takes them; configs_out may be
+ * configs_in): page-locked buffers are read and written in place by the
+ * kernels (no staging copy), others go through a device copy.  One wait at
+ * the end.  A bad species in configs_in fails the call (BRAWL_ESTATE)
+ * before any trial runs. */
+int brawl_batch_metropolis_host(brawl_batch *batch, const int8_t *configs_in, const int64_t *n_trials,
+                                int8_t *configs_out, int64_t *accepted);
 int brawl_batch_rng_get(brawl_batch *batch, int chain, uint32_t state[625]);
 int brawl_batch_counters(brawl_batch *batch, int64_t *counters /* n_chains * 8 */);
 int brawl_batch_radial_densities(brawl_batch *batch, int chain, int wc_range,

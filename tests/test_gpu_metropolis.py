@@ -275,6 +275,43 @@ def test_batched_replica_shape_matches_oracle():
         assert row["evaluated"] == c.evaluated and row["exp_tests"] == c.exp_tests
 
 
+def test_metropolis_from_host_buffers():
+    """brawl_batch_metropolis_host (pinned buffers used in place, pageable
+    ones through a copy) gives what set_configs + metropolis + get_configs
+    give; a bad species flags its chain, which runs no trial, and the call
+    fails."""
+    import torch
+    rng = np.random.default_rng(12)
+    V = random_V(rng, 3, 4)
+    Ls = [3, 5, 4, 6]
+    def make():
+        return B.Batch([dict(setup=B.Setup("bcc", L, L, L, 3, 4), V=V, seed=7 + r,
+                             beta=1.0 / (600.0 * B.K_B_IN_RY), species_concentrations=conc_vector(3))
+                        for r, L in enumerate(Ls)])
+    a, b, c = make(), make(), make()
+    trials = np.array([10 * 2 * L ** 3 for L in Ls], dtype=np.int64)
+    grids = a.get_configs()
+    pinned = torch.empty(a.grid_bytes, dtype=torch.int8, pin_memory=True).numpy()
+    pinned[:] = grids
+    pageable = grids.copy()
+    for _ in range(3):
+        acc_a = a.metropolis_host(pinned, trials)
+        acc_c = c.metropolis_host(pageable, trials)
+        b.set_configs(b.get_configs())
+        acc_b = b.metropolis(trials)
+        ref = b.get_configs()
+        assert list(acc_a) == list(acc_b) == list(acc_c)
+        assert np.array_equal(pinned, ref) and np.array_equal(pageable, ref)
+    bad = pinned.copy()
+    occupied = np.nonzero(bad)[0]
+    bad[occupied[0]] = 9                       # species 9 of 3, in chain 0's grid
+    with pytest.raises(B.BrawlError):
+        a.metropolis_host(bad, trials)
+    cnt = a.counters()
+    assert cnt[0][0] == 3 * trials[0]          # chain 0 ran no trial in the failed call
+    assert cnt[1][0] == 4 * trials[1]          # the others did
+
+
 def test_initial_setup_modes_match_oracle():
     rng = np.random.default_rng(11)
     for lat, n, ns in (("fcc", (4, 3, 2), 5), ("bcc", (5, 5, 5), 3), ("simple_cubic", (2, 2, 3), 4)):
