@@ -95,6 +95,9 @@ def load(rebuild: bool = False):
         "brawl_lattice_shells": ([vp, i, vp], i),
         "brawl_radial_densities": ([vp, i, vp, vp], i),
         "brawl_counters": ([vp, vp], i),
+        "brawl_alro_add": ([vp], i),
+        "brawl_alro_get": ([vp, vp], i),
+        "brawl_alro_reset": ([vp], i),
         "brawl_total_energy_noalloc": ([vp, vp, vp, vp, vp], i),
         "brawl_ns_create": ([vp, i, vp], i),
         "brawl_ns_destroy": ([vp], i),
@@ -150,6 +153,9 @@ def load(rebuild: bool = False):
         "brawl_batch_set_configs": ([vp, vp], i),
         "brawl_batch_metropolis_host": ([vp, vp, vp, vp, vp], i),
         "brawl_batch_counters": ([vp, vp], i),
+        "brawl_batch_alro_add": ([vp], i),
+        "brawl_batch_alro_get": ([vp, i, vp], i),
+        "brawl_batch_alro_reset": ([vp], i),
         "brawl_batch_radial_densities": ([vp, i, i, vp, vp], i),
     }
     for name, (args, res) in sig.items():
@@ -302,6 +308,20 @@ class Chain:
         c = np.zeros(NUM_COUNTERS, dtype=np.int64)
         _check(load().brawl_counters(self._h, _ptr(c)))
         return dict(zip(COUNTER_NAMES, (int(v) for v in c)))
+
+    # -- ALRO (store_state, src/analytics.f90:43-64) ----------------------------
+    def alro_add(self) -> None:
+        _check(load().brawl_alro_add(self._h))
+
+    def alro_reset(self) -> None:
+        _check(load().brawl_alro_reset(self._h))
+
+    def alro(self) -> np.ndarray:
+        """order(species, basis, x, y, z) as its C view, shaped
+        (2n3, 2n2, 2n1, 1, n_species)."""
+        out = np.zeros(self.setup.grid_shape + (1, self.setup.n_species), dtype=np.float64)
+        _check(load().brawl_alro_get(self._h, _ptr(out)))
+        return out
 
     # -- analytics ------------------------------------------------------------
     def lattice_shells(self, wc_range: int) -> np.ndarray:

@@ -360,6 +360,9 @@ struct brawl_batch {
   int device = 0;
   int max_optin = 0;
   int spec_nc = kDefaultSpeculation;  // trials per speculative round (1: none)
+  double* d_alro = nullptr;              // ALRO counts: per chain ns x n_sites
+  int64_t* d_alro_off = nullptr;
+  std::vector<int64_t> alro_off;
 };
 
 struct brawl_ctx {
@@ -703,7 +706,8 @@ int brawl_batch_destroy(brawl_batch* b) {
   if (!b) return BRAWL_OK;
   if (b->stream) {
     for (const void* p : {(const void*)b->arena, (const void*)b->d_site_e, (const void*)b->d_grid,
-                          (const void*)b->d_grids, (const void*)b->d_gjobs, (const void*)b->d_scratch})
+                          (const void*)b->d_grids, (const void*)b->d_gjobs, (const void*)b->d_scratch,
+                          (const void*)b->d_alro, (const void*)b->d_alro_off})
       dfree(p, b->stream);
     cudaStreamSynchronize(b->stream);
     cudaStreamDestroy(b->stream);
@@ -898,6 +902,60 @@ int brawl_batch_metropolis_host(brawl_batch* b, const int8_t* configs_in, const 
                               b->last_counters[c * kNumCounters + kCntAccepted]);
   b->last_counters = cnt;
   return check_status(b);
+}
+
+static int ensure_alro(brawl_batch* b) {
+  if (b->d_alro) return BRAWL_OK;
+  TRY(ensure_grids(b));
+  const int n = (int)b->jobs.size();
+  b->alro_off.assign(n + 1, 0);
+  for (int c = 0; c < n; ++c)
+    b->alro_off[c + 1] = b->alro_off[c] + (int64_t)b->models[c].g.ns * b->models[c].g.n_sites;
+  CUDA_TRY(dalloc(&b->d_alro, (size_t)b->alro_off[n] * 8, b->stream));
+  CUDA_TRY(dalloc(&b->d_alro_off, (size_t)n * 8, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(b->d_alro_off, b->alro_off.data(), (size_t)n * 8, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaMemsetAsync(b->d_alro, 0, (size_t)b->alro_off[n] * 8, b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_alro_add(brawl_batch* b) {
+  if (!b) return fail(BRAWL_EINVAL, "null argument");
+  TRY(ensure_alro(b));
+  launch_alro_add(b->d_gjobs, (int)b->jobs.size(), b->d_alro, b->d_alro_off, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  return BRAWL_OK;
+}
+
+int brawl_batch_alro_reset(brawl_batch* b) {
+  if (!b) return fail(BRAWL_EINVAL, "null argument");
+  TRY(ensure_alro(b));
+  CUDA_TRY(cudaMemsetAsync(b->d_alro, 0, (size_t)b->alro_off.back() * 8, b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_alro_get(brawl_batch* b, int c, double* order) {
+  if (!b || !order || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad argument");
+  TRY(ensure_alro(b));
+  const Geom& g = b->models[c].g;
+  std::vector<double> cnt((size_t)g.ns * g.n_sites);
+  CUDA_TRY(cudaMemcpyAsync(cnt.data(), b->d_alro + b->alro_off[c], cnt.size() * 8, cudaMemcpyDeviceToHost,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  // order(species, basis, x, y, z), species fastest; empty cells stay 0
+  const int W1 = 2 * g.n1, W2 = 2 * g.n2, W3 = 2 * g.n3, ns = g.ns;
+  std::fill(order, order + (size_t)ns * W1 * W2 * W3, 0.0);
+  for (int z = 0; z < W3; ++z)
+    for (int y = 0; y < W2; ++y)
+      for (int x = 0; x < W1; ++x) {
+        const bool occ = g.lattice == kBcc   ? (((x & 1) == (z & 1)) && ((y & 1) == (z & 1)))
+                         : g.lattice == kFcc ? (((x + y + z) & 1) == 0)
+                                             : true;
+        if (!occ) continue;
+        const int i = z * g.sz + (y >> g.ys) * g.sy + (x >> g.xs);
+        double* cell = order + ((size_t)(z * W2 + y) * W1 + x) * ns;
+        for (int s = 0; s < ns; ++s) cell[s] = cnt[(size_t)s * g.n_sites + i];
+      }
+  return BRAWL_OK;
 }
 
 int brawl_batch_rng_get(brawl_batch* b, int c, uint32_t state[625]) {
@@ -1187,6 +1245,21 @@ int brawl_radial_densities(brawl_ctx* ctx, int wc_range, const double* shells, d
 int brawl_counters(brawl_ctx* ctx, int64_t* counters) {
   if (!ctx) return fail(BRAWL_EINVAL, "null argument");
   return brawl_batch_counters(ctx->b, counters);
+}
+
+int brawl_alro_add(brawl_ctx* ctx) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_alro_add(ctx->b);
+}
+
+int brawl_alro_reset(brawl_ctx* ctx) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_alro_reset(ctx->b);
+}
+
+int brawl_alro_get(brawl_ctx* ctx, double* order) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  return brawl_batch_alro_get(ctx->b, 0, order);
 }
 
 }  // extern "C"

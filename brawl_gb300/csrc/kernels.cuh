@@ -225,5 +225,8 @@ void launch_pack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells,
                        const int8_t* d_grids, cudaStream_t stream);
 void launch_unpack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells, int8_t* d_grids,
                          cudaStream_t stream);
+// counts[offsets[c] + (s - 1) * n_sites + i] += 1 for chain c's site i of species s
+void launch_alro_add(const GridJob* d_jobs, int n_jobs, double* d_counts, const int64_t* d_offsets,
+                     cudaStream_t stream);
 
 }  // namespace brawl

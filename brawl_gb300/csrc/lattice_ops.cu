@@ -231,6 +231,26 @@ __global__ void unpack_batch_kernel(const GridJob* __restrict__ jobs, int8_t* __
   }
 }
 
+// store_state (src/analytics.f90:43-64): every occupied site adds 1.0 to its
+// species' count, one block row per chain (+1.0 sums of a few thousand
+// samples are exact, so the order of the adds does not matter).
+__global__ void alro_add_kernel(const GridJob* __restrict__ jobs, double* __restrict__ counts,
+                                const int64_t* __restrict__ offsets) {
+  const GridJob& J = jobs[blockIdx.y];
+  double* c = counts + offsets[blockIdx.y];
+  const int n = J.g.n_sites;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = J.lat[i];
+    if (s >= 1 && s <= J.g.ns) c[(size_t)(s - 1) * n + i] += 1.0;
+  }
+}
+
+void launch_alro_add(const GridJob* d_jobs, int n_jobs, double* d_counts, const int64_t* d_offsets,
+                     cudaStream_t stream) {
+  BRAWL_CARVEOUT(alro_add_kernel);
+  if (n_jobs > 0) alro_add_kernel<<<dim3(8, n_jobs), 256, 0, stream>>>(d_jobs, d_counts, d_offsets);
+}
+
 // blocks per chain: enough threads for the largest grid's quads, at most 32
 static dim3 batch_grid(int n_jobs, int64_t total_cells) {
   const int64_t per = total_cells / 4 / (n_jobs > 0 ? n_jobs : 1);

@@ -4,7 +4,8 @@ simulated_annealing mirrors metropolis_simulated_annealing
 (src/metropolis.F90:84-558): per
 temperature, the optional burn-in, the sample at step 0, n_sweeps blocks of
 n_sweep_steps swap trials on the device, and after each block the energy
-(total_energy), the ASRO sample (radial_densities) and the trajectory rows.
+(total_energy), the ASRO sample (radial_densities), the ALRO sample
+(store_state, on the device) and the trajectory rows.
 The per-temperature averages use the reference's arithmetic: E and E^2
 accumulated in FP64 sample by sample, n_save_* = floor(real/real) in single
 precision, C clamped at zero.  decorrelated_samples mirrors
@@ -32,6 +33,7 @@ def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs:
     shells = chain.lattice_shells(wc_range)
     n_save_energy = _f32_floor_div(m.n_mc_steps, m.n_sample_steps)
     n_save_asro = _f32_floor_div(m.n_mc_steps, m.n_sample_steps_asro)
+    n_save_alro = _f32_floor_div(m.n_mc_steps, m.n_sample_steps_alro) if m.calculate_alro else 1
     Ts = m.T_steps
     out = {
         "shells": shells,
@@ -39,6 +41,7 @@ def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs:
         "acceptance_of_T": np.zeros(Ts), "rho_of_T": np.zeros((Ts, wc_range, ns, ns)),
         "traj_step": [], "traj_energy": [], "traj_asro": [],
         "initial_configs": [], "final_configs": [],
+        "order_of_T": (np.zeros((Ts,) + chain.setup.grid_shape + (1, ns)) if m.calculate_alro else None),
     }
     asro = np.zeros((wc_range, ns, ns))
     for j in range(Ts):
@@ -49,6 +52,8 @@ def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs:
         sim_temp = temp * K_B_IN_RY
         beta = 1.0 / sim_temp if sim_temp != 0.0 else float("inf")
         out["temperature"][j] = temp
+        if m.calculate_alro:
+            chain.alro_reset()
         burn = m.burn_in_start if j == 0 else m.burn_in
         if burn and m.n_burn_in_steps > 0:
             chain.metropolis(beta, m.n_burn_in_steps, m.nbr_swap)
@@ -75,6 +80,8 @@ def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs:
             if m.calculate_asro and step_n % m.n_sample_steps_asro == 0:
                 asro = chain.radial_densities(shells)
                 r_dens = r_dens + asro
+            if m.calculate_alro and step_n % m.n_sample_steps_alro == 0:
+                chain.alro_add()
             if step_n % m.n_sample_steps_trajectory == 0:
                 out["traj_step"].append(step_n)
                 out["traj_energy"].append(current_energy)
@@ -93,6 +100,9 @@ def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs:
             out["C_of_T"][j] = C
         if m.calculate_asro:
             out["rho_of_T"][j] = r_dens / float(n_save_asro)
+        if m.calculate_alro:
+            # order / real(n_save_alro): the count in single precision, exact
+            out["order_of_T"][j] = chain.alro() / float(np.float32(n_save_alro))
         if record_configs:
             out["final_configs"].append(chain.config())
     out["traj_step"] = np.array(out["traj_step"], dtype=np.int64)

@@ -121,6 +121,13 @@ int brawl_metropolis_run(brawl_ctx *ctx, double beta, int64_t n_trials, int nbr_
 int brawl_lattice_shells(brawl_ctx *ctx, int wc_range, double *shells);
 /* radial_densities (src/analytics.f90:293-404), bit-identical. */
 int brawl_radial_densities(brawl_ctx *ctx, int wc_range, const double *shells, double *rho);
+/* ALRO (store_state, src/analytics.f90:43-64): add the configuration's
+ * occupancies to a device accumulator; read it as
+ * order(species, basis, 2n1, 2n2, 2n3) (species fastest, empty cells 0);
+ * zero it (the reference zeroes it at every temperature). */
+int brawl_alro_add(brawl_ctx *ctx);
+int brawl_alro_get(brawl_ctx *ctx, double *order);
+int brawl_alro_reset(brawl_ctx *ctx);
 
 /* Cumulative counters of this chain (BRAWL_NUM_COUNTERS values). */
 int brawl_counters(brawl_ctx *ctx, int64_t *counters);
@@ -197,6 +204,9 @@ int brawl_batch_metropolis_host(brawl_batch *batch, const int8_t *configs_in, co
                                 int8_t *configs_out, int64_t *accepted);
 int brawl_batch_rng_get(brawl_batch *batch, int chain, uint32_t state[625]);
 int brawl_batch_counters(brawl_batch *batch, int64_t *counters /* n_chains * 8 */);
+int brawl_batch_alro_add(brawl_batch *batch);                       /* every chain */
+int brawl_batch_alro_get(brawl_batch *batch, int chain, double *order);
+int brawl_batch_alro_reset(brawl_batch *batch);
 int brawl_batch_radial_densities(brawl_batch *batch, int chain, int wc_range,
                                  const double *shells, double *rho);
 

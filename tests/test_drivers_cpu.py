@@ -15,8 +15,9 @@ from oracle import oracle as O
 class OracleChain:
     """The chain interface the drivers use, over the oracle."""
 
-    def __init__(self, mod, cfg, rng):
+    def __init__(self, mod, cfg, rng, setup=None):
         self.mod, self.cfg, self.rng = mod, cfg, rng
+        self.setup = setup
 
     def metropolis(self, beta, n_trials, nbr_swap=False):
         acc, _ = self.mod.mc_run(self.cfg, self.rng, beta, n_trials, nbr_swap)
@@ -27,6 +28,23 @@ class OracleChain:
 
     def config(self):
         return self.cfg.copy()
+
+    def lattice_shells(self, wc_range):
+        return self.mod.lattice_shells(self.cfg, wc_range)
+
+    def radial_densities(self, shells):
+        return self.mod.radial_densities(self.cfg, shells)[0]
+
+    # ALRO on the host: store_state's +1.0 per occupied site and species
+    def alro_reset(self):
+        self._order = np.zeros(self.cfg.shape + (1, self.mod.ns))
+
+    def alro_add(self):
+        for s in range(1, self.mod.ns + 1):
+            self._order[..., 0, s - 1] += (self.cfg == s)
+
+    def alro(self):
+        return self._order.copy()
 
 
 def small_system(seed):
@@ -124,3 +142,42 @@ def test_save_rho_E_bookkeeping():
     W.done = None
     save_rho_E(W, 3, st)                 # rho_saved: nothing more happens
     assert W.done is None
+
+
+def reference_alro(mod, cfg, rng, m):
+    """metropolis_simulated_annealing's ALRO (src/metropolis.F90:192-197,
+    394-399, 444-447) on the oracle: per temperature the order array is
+    zeroed, every n_sample_steps_alro trials store_state adds the
+    occupancies, and order_of_T = order / real(n_save_alro)."""
+    n_sweeps = m.n_mc_steps // m.n_sample_steps
+    n_sweep_steps = m.n_mc_steps // n_sweeps
+    n_save = int(np.floor(np.float32(m.n_mc_steps) / np.float32(m.n_sample_steps_alro)))
+    out = []
+    for j in range(m.T_steps):
+        temp = m.T + float(j) * m.delta_T
+        beta = 1.0 / (temp * B.K_B_IN_RY)
+        order = np.zeros(cfg.shape + (1, mod.ns))
+        for i in range(1, n_sweeps + 1):
+            mod.mc_run(cfg, rng, beta, n_sweep_steps, m.nbr_swap)
+            if (i * n_sweep_steps) % m.n_sample_steps_alro == 0:
+                for s in range(1, mod.ns + 1):
+                    order[..., 0, s - 1] += (cfg == s)
+        out.append(order / float(np.float32(n_save)))
+    return np.array(out)
+
+
+def test_annealing_alro_host_logic():
+    m = I.MetropolisParams(mode="simulated_annealing", n_mc_steps=540, n_sample_steps=54,
+                           calculate_energies=True, calculate_asro=False, n_sample_steps_asro=54,
+                           calculate_alro=True, n_sample_steps_alro=108, n_sample_steps_trajectory=54,
+                           T=900.0, T_steps=3, delta_T=-300.0)
+    mod, cfg, r, _ = small_system(21)
+    ra, rb = O.OracleRng(1), O.OracleRng(1)
+    ra.set_state_words(r.state_words())
+    rb.set_state_words(r.state_words())
+    ref = reference_alro(mod, cfg.copy(), ra, m)
+    setup = B.Setup("bcc", 3, 3, 3, 3, 2)
+    out = M.simulated_annealing(OracleChain(mod, cfg.copy(), rb, setup), m, 2, record_configs=False)
+    assert out["order_of_T"].shape == ref.shape
+    assert np.array_equal(out["order_of_T"], ref)
+    assert np.allclose(out["order_of_T"].sum(axis=-1)[:, cfg > 0], 1.0)  # occupied sites: one species each

@@ -421,3 +421,20 @@ def test_decorrelated_samples_match_oracle(nbr_swap):
     g = O.OracleRng(1)
     g.set_state_words(ch.rng_state())
     assert [g.uniform() for _ in range(700)] == [r.uniform() for _ in range(700)]
+
+
+def test_annealing_alro_matches_oracle():
+    """The annealing driver's ALRO (store_state accumulated on the device)
+    against the reference's loop on the oracle, bit for bit."""
+    from tests.test_drivers_cpu import reference_alro, small_system
+    m = I.MetropolisParams(mode="simulated_annealing", n_mc_steps=2700, n_sample_steps=54,
+                           calculate_energies=True, calculate_asro=False, n_sample_steps_asro=54,
+                           calculate_alro=True, n_sample_steps_alro=162, n_sample_steps_trajectory=54,
+                           T=1200.0, T_steps=4, delta_T=-250.0)
+    mod, cfg, r, V = small_system(23)
+    ch = B.Chain(B.Setup("bcc", 3, 3, 3, 3, 2), V)
+    ch.set_config(cfg)
+    ch.set_rng_state(r.state_words())
+    ref = reference_alro(mod, cfg.copy(), r, m)
+    out = anneal.simulated_annealing(ch, m, 2, record_configs=False)
+    assert np.array_equal(out["order_of_T"], ref)
