@@ -13,6 +13,10 @@ of the classic format (CDF-1) for the files the sampling path produces.
                       Range.
 * 1-D data         -- ncdf_writer_1d (:731-806): "grid data" over x (the
                       Wang-Landau density of states).
+* ALRO             -- ncdf_order_writer (:362-480): "grid data" holding
+                      order(species, basis, x, y, z, T) under the dimension
+                      names the reference gives it (b, x, y, z, s, t, in
+                      that order), and "temperature data" over temp.
 
 The layout is the one the netCDF library gives a file created with
 NF90_CLOBBER and closed after one enddef: header, then each variable's data
@@ -28,7 +32,7 @@ import struct
 import numpy as np
 
 __all__ = ["write_config", "read_config", "write_radial_density", "read_radial_density",
-           "write_grid_1d", "read_file"]
+           "write_grid_1d", "write_order", "read_file"]
 
 _MAGIC = b"CDF\x01"
 _ABSENT = b"\x00" * 8
@@ -262,3 +266,23 @@ def write_grid_1d(path: str, data) -> None:
     a = np.asarray(data, dtype=">f8").ravel()
     with open(path, "wb") as f:
         f.write(_encode([("x", a.size)], [], [("grid data", ["x"], a)]))
+
+
+def write_order(path: str, order_of_T, temperature, p) -> None:
+    """ncdf_order_writer.  order_of_T: C-ordered (T, 2n3, 2n2, 2n1, n_basis,
+    n_species) -- the Fortran order(species, basis, x, y, z, T) -- as the
+    annealing driver returns it.  The reference labels the six dimensions
+    b, x, y, z, s, t in Fortran order whatever they hold (so "b" has
+    n_species entries), and writes N_Basis (capital B) among the run's
+    attributes."""
+    o = np.asarray(order_of_T, dtype=">f8")
+    nT, n3, n2, n1, nb, ns = o.shape
+    T = np.asarray(temperature, dtype=">f8").ravel()
+    attrs = [("N_Basis", np.int32(p.n_basis))] + _run_attrs(p, False) + [
+        ("Interaction file", p.interaction_file.strip()),
+        ("Concentrations", np.asarray(p.species_concentrations, dtype=np.float64)),
+        ("Warren-Cowley Range", np.int32(p.wc_range))]
+    dims = [("b", ns), ("x", nb), ("y", n1), ("z", n2), ("s", n3), ("t", nT), ("temp", T.size)]
+    variables = [("grid data", ["t", "s", "z", "y", "x", "b"], o), ("temperature data", ["temp"], T)]
+    with open(path, "wb") as f:
+        f.write(_encode(dims, attrs, variables))

@@ -104,3 +104,21 @@ def test_oracle_run_written_byte_for_byte(tmp_path):
     out = tmp_path / "init.nc"
     N.write_config(str(out), cfg, p)
     assert out.read_bytes() == _raw("02_proc_0002_initial_config_at_0300.0.nc")
+
+
+def test_order_writer_reads_back_with_scipy(tmp_path):
+    """ncdf_order_writer's layout, checked with scipy's independent reader."""
+    from scipy.io import netcdf_file
+    p = _params("02")
+    rng = np.random.default_rng(4)
+    order = rng.uniform(0, 1, (3, 8, 8, 8, 1, p.n_species))
+    T = np.array([300.0, 250.0, 200.0])
+    out = tmp_path / "alro.nc"
+    N.write_order(str(out), order, T, p)
+    f = netcdf_file(str(out), "r", mmap=False)
+    assert f.dimensions == {"b": p.n_species, "x": 1, "y": 8, "z": 8, "s": 8, "t": 3, "temp": 3}
+    assert f.variables["grid data"].dimensions == ("t", "s", "z", "y", "x", "b")
+    assert np.array_equal(np.array(f.variables["grid data"].data), order)
+    assert np.array_equal(np.array(f.variables["temperature data"].data), T)
+    assert int(f.N_Basis) == 1 and f._attributes["Lattice Type"] == b"bcc"
+    f.close()
