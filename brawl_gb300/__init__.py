@@ -154,6 +154,7 @@ def load(rebuild: bool = False):
         "brawl_batch_metropolis_host": ([vp, vp, vp, vp, vp], i),
         "brawl_batch_counters": ([vp, vp], i),
         "brawl_batch_alro_add": ([vp], i),
+        "brawl_batch_lattice_shells": ([vp, i, i, vp], i),
         "brawl_batch_alro_get": ([vp, i, vp], i),
         "brawl_batch_alro_reset": ([vp], i),
         "brawl_batch_radial_densities": ([vp, i, i, vp, vp], i),
@@ -351,9 +352,11 @@ class Batch:
         descs = (_ChainDesc * n)()
         self._keep = []
         self.setups = []
+        self.nbr_swap = []
         for k, ch in enumerate(chains):
             s = ch["setup"]
             self.setups.append(s)
+            self.nbr_swap.append(bool(ch.get("nbr_swap", False)))
             V = _v_array(s, ch["V"])
             self._keep.append(V)
             d = descs[k]
@@ -488,6 +491,24 @@ class Batch:
         ns = self.setups[c].n_species
         out = np.zeros((wc, ns, ns), dtype=np.float64)
         _check(load().brawl_batch_radial_densities(self._h, c, wc, _ptr(shells), _ptr(out)))
+        return out
+
+    def lattice_shells(self, c: int, wc_range: int) -> np.ndarray:
+        out = np.zeros(wc_range, dtype=np.float64)
+        _check(load().brawl_batch_lattice_shells(self._h, c, wc_range, _ptr(out)))
+        return out
+
+    # -- ALRO (store_state) of every chain --------------------------------------
+    def alro_add(self) -> None:
+        _check(load().brawl_batch_alro_add(self._h))
+
+    def alro_reset(self) -> None:
+        _check(load().brawl_batch_alro_reset(self._h))
+
+    def alro(self, c: int) -> np.ndarray:
+        s = self.setups[c]
+        out = np.zeros(s.grid_shape + (1, s.n_species), dtype=np.float64)
+        _check(load().brawl_batch_alro_get(self._h, c, _ptr(out)))
         return out
 
 

@@ -1237,6 +1237,13 @@ int brawl_lattice_shells(brawl_ctx* ctx, int wc_range, double* shells) {
   return BRAWL_OK;
 }
 
+int brawl_batch_lattice_shells(brawl_batch* b, int c, int wc_range, double* shells) {
+  if (!b || !shells || wc_range < 1 || c < 0 || c >= (int)b->jobs.size())
+    return fail(BRAWL_EINVAL, "bad argument");
+  lattice_shells_host(b->models[c].g, wc_range, shells);
+  return BRAWL_OK;
+}
+
 int brawl_radial_densities(brawl_ctx* ctx, int wc_range, const double* shells, double* rho) {
   if (!ctx) return fail(BRAWL_EINVAL, "null argument");
   return brawl_batch_radial_densities(ctx->b, 0, wc_range, shells, rho);

@@ -9,13 +9,15 @@ n_sweep_steps swap trials on the device, and after each block the energy
 The per-temperature averages use the reference's arithmetic: E and E^2
 accumulated in FP64 sample by sample, n_save_* = floor(real/real) in single
 precision, C clamped at zero.  decorrelated_samples mirrors
-metropolis_decorrelated_samples (:560-738).
+metropolis_decorrelated_samples (:560-738).  simulated_annealing_ensemble
+runs the MPI ranks' annealings as the chains of one batch and averages them
+as comms_reduce_metropolis_results does (src/comms.F90:122-160).
 """
 from __future__ import annotations
 
 import numpy as np
 
-from . import K_B_IN_RY, Chain
+from . import K_B_IN_RY, Batch, Chain
 
 
 def _f32_floor_div(a: int, b: int) -> int:
@@ -150,3 +152,107 @@ def decorrelated_samples(chain: Chain, metropolis, record_configs: bool = True):
     out["sample_energy"] = np.array(out["sample_energy"])
     out["sample_accepted"] = np.array(out["sample_accepted"], dtype=np.int64)
     return out
+
+
+def simulated_annealing_ensemble(batch: Batch, metropolis, wc_range: int, record_configs: bool = True):
+    """metropolis_simulated_annealing on every chain of a batch at once (the
+    reference's ranks, each with its own stream and configuration), every
+    sweep block one launch for all chains.  Each chain's outputs are what
+    simulated_annealing gives for it alone; "average" holds the ensemble
+    averages of comms_reduce_metropolis_results: the rank sum in rank order
+    divided by real(p)."""
+    m = metropolis
+    n = batch.n
+    if any(b != bool(m.nbr_swap) for b in batch.nbr_swap):
+        raise ValueError("the batch's chains must be created with nbr_swap = metropolis.nbr_swap")
+    ns = batch.setups[0].n_species
+    n_atoms = np.array([s.n_atoms for s in batch.setups], dtype=np.float64)
+    shells = [batch.lattice_shells(c, wc_range) for c in range(n)]
+    n_save_energy = _f32_floor_div(m.n_mc_steps, m.n_sample_steps)
+    n_save_asro = _f32_floor_div(m.n_mc_steps, m.n_sample_steps_asro)
+    n_save_alro = _f32_floor_div(m.n_mc_steps, m.n_sample_steps_alro) if m.calculate_alro else 1
+    Ts = m.T_steps
+    outs = [{
+        "shells": shells[c],
+        "temperature": np.zeros(Ts), "energies_of_T": np.zeros(Ts), "C_of_T": np.zeros(Ts),
+        "acceptance_of_T": np.zeros(Ts), "rho_of_T": np.zeros((Ts, wc_range, ns, ns)),
+        "traj_step": [], "traj_energy": [], "traj_asro": [],
+        "initial_configs": [], "final_configs": [],
+        "order_of_T": (np.zeros((Ts,) + batch.setups[c].grid_shape + (1, ns)) if m.calculate_alro else None),
+    } for c in range(n)]
+    asro = [np.zeros((wc_range, ns, ns)) for _ in range(n)]
+    for j in range(Ts):
+        r_dens = [np.zeros((wc_range, ns, ns)) for _ in range(n)]
+        step_E = np.zeros(n)
+        step_Esq = np.zeros(n)
+        temp = m.T + float(j) * m.delta_T
+        sim_temp = temp * K_B_IN_RY
+        beta = 1.0 / sim_temp if sim_temp != 0.0 else float("inf")
+        batch.set_beta(np.full(n, beta))
+        if m.calculate_alro:
+            batch.alro_reset()
+        burn = m.burn_in_start if j == 0 else m.burn_in
+        if burn and m.n_burn_in_steps > 0:
+            batch.metropolis(m.n_burn_in_steps)
+        energy = batch.total_energy() if m.calculate_energies else np.zeros(n)
+        if m.calculate_asro:
+            asro = [batch.radial_densities(c, shells[c]) for c in range(n)]
+        for c in range(n):
+            o = outs[c]
+            o["temperature"][j] = temp
+            o["traj_step"].append(0)
+            o["traj_energy"].append(energy[c])
+            o["traj_asro"].append(asro[c].copy())
+            if record_configs:
+                o["initial_configs"].append(batch.config(c))
+        n_sweeps = m.n_mc_steps // m.n_sample_steps
+        n_sweep_steps = m.n_mc_steps // n_sweeps
+        accepted = np.zeros(n, dtype=np.int64)
+        for i in range(1, n_sweeps + 1):
+            accepted += batch.metropolis(n_sweep_steps)
+            step_n = i * n_sweep_steps
+            if m.calculate_energies:
+                energy = batch.total_energy()
+                step_E = step_E + energy
+                step_Esq = step_Esq + energy * energy
+            if m.calculate_asro and step_n % m.n_sample_steps_asro == 0:
+                asro = [batch.radial_densities(c, shells[c]) for c in range(n)]
+                r_dens = [r + a for r, a in zip(r_dens, asro)]
+            if m.calculate_alro and step_n % m.n_sample_steps_alro == 0:
+                batch.alro_add()
+            if step_n % m.n_sample_steps_trajectory == 0:
+                for c in range(n):
+                    outs[c]["traj_step"].append(step_n)
+                    outs[c]["traj_energy"].append(energy[c])
+                    outs[c]["traj_asro"].append(asro[c].copy())
+        for c in range(n):
+            o = outs[c]
+            o["acceptance_of_T"][j] = float(accepted[c]) / float(np.float32(m.n_mc_steps))
+            if m.calculate_energies:
+                ne = float(n_save_energy)
+                o["energies_of_T"][j] = step_E[c] / ne / n_atoms[c]
+                mean = step_E[c] / ne
+                C = (step_Esq[c] / ne - mean * mean) / (sim_temp * temp) / n_atoms[c]
+                if C < 0.0 or temp <= 0.0:
+                    C = 0.0
+                o["C_of_T"][j] = C
+            if m.calculate_asro:
+                o["rho_of_T"][j] = r_dens[c] / float(n_save_asro)
+            if m.calculate_alro:
+                o["order_of_T"][j] = batch.alro(c) / float(np.float32(n_save_alro))
+            if record_configs:
+                o["final_configs"].append(batch.config(c))
+    for o in outs:
+        o["traj_step"] = np.array(o["traj_step"], dtype=np.int64)
+        o["traj_energy"] = np.array(o["traj_energy"])
+        o["traj_asro"] = np.array(o["traj_asro"])
+    p = float(np.float32(n))
+    av = {}
+    keys = ["acceptance_of_T"] + (["energies_of_T", "C_of_T"] if m.calculate_energies else []) + \
+        (["rho_of_T"] if m.calculate_asro else [])
+    for k in keys:
+        s = outs[0][k]
+        for o in outs[1:]:
+            s = s + o[k]
+        av[k] = s / p
+    return {"ranks": outs, "average": av}

@@ -204,6 +204,7 @@ int brawl_batch_metropolis_host(brawl_batch *batch, const int8_t *configs_in, co
                                 int8_t *configs_out, int64_t *accepted);
 int brawl_batch_rng_get(brawl_batch *batch, int chain, uint32_t state[625]);
 int brawl_batch_counters(brawl_batch *batch, int64_t *counters /* n_chains * 8 */);
+int brawl_batch_lattice_shells(brawl_batch *batch, int chain, int wc_range, double *shells);
 int brawl_batch_alro_add(brawl_batch *batch);                       /* every chain */
 int brawl_batch_alro_get(brawl_batch *batch, int chain, double *order);
 int brawl_batch_alro_reset(brawl_batch *batch);

@@ -82,6 +82,40 @@ def test_golden_anneal_on_gpu(test, rank, tmp_path):
             assert path.read_bytes() == f.read()
 
 
+def test_golden_ensemble_in_one_batch():
+    """The four MPI ranks of golden test 02 as the chains of one batch
+    (simulated_annealing_ensemble): every rank's outputs are its golden
+    files, and the ensemble average (comms_reduce_metropolis_results) is
+    av_energy_diagnostics.dat and av_radial_density.nc."""
+    test = "02_parallel_metropolis"
+    p, V = G.load_inputs(test)
+    m = I.read_metropolis_file(G.path(test, "metropolis.inp"))
+    setup = B.Setup.from_run_params(p)
+    chains = [dict(setup=setup, V=V, seed=110179 + 11 * r, beta=0.0, nbr_swap=m.nbr_swap,
+                   species_concentrations=p.species_concentrations, species_numbers=p.numbers_or_none())
+              for r in range(4)]
+    res = anneal.simulated_annealing_ensemble(B.Batch(chains), m, p.wc_range)
+    for r, out in enumerate(res["ranks"]):
+        tag = "proc_%04d" % r
+        assert np.array_equal(out["initial_configs"][0], G.config_zyx(test, tag + "_initial_config_at_0300.0.npz"))
+        assert np.array_equal(out["final_configs"][0], G.config_zyx(test, tag + "_final_config_at_0300.0.npz"))
+        lines = [OUT.energy_trajectory_header()] + [
+            OUT.energy_trajectory_line(s, e) for s, e in zip(out["traj_step"], out["traj_energy"])]
+        assert lines == G.text(test, tag + "_energy_trajectory_at_T_0300.0.dat")
+        rho = G.npz(test, tag + "_rho_of_T.npz")
+        assert np.array_equal(rho["rho_data"], out["rho_of_T"])
+        diag = OUT.diagnostics_lines(out["temperature"], out["energies_of_T"], out["C_of_T"],
+                                     out["acceptance_of_T"])
+        assert diag == G.text(test, tag + "_energy_diagnostics.dat")
+    av = res["average"]
+    diag = OUT.diagnostics_lines(res["ranks"][0]["temperature"], av["energies_of_T"], av["C_of_T"],
+                                 av["acceptance_of_T"])
+    assert diag == G.text(test, "av_energy_diagnostics.dat")
+    ref = G.npz(test, "av_radial_density.npz")
+    assert np.array_equal(ref["rho_data"], av["rho_of_T"])
+    assert np.array_equal(ref["U_data"], av["energies_of_T"])
+
+
 # ---------------------------------------------------------------------------
 # trial-level parity with the oracle
 # ---------------------------------------------------------------------------
