@@ -120,6 +120,7 @@ def load(rebuild: bool = False):
         "brawl_wl_genrand": ([vp, i, i64, vp], i),
         "brawl_wl_counters": ([vp, i, vp], i),
         "brawl_wl_radial_enable": ([vp, i, vp, i, i], i),
+        "brawl_wl_enter_windows": ([vp, C.c_double, C.c_double, vp, vp, i, C.c_int64, vp], i),
         "brawl_wl_radial_set_done": ([vp, vp], i),
         "brawl_wl_radial_get": ([vp, i, vp, vp, vp], i),
         "brawl_wl_replica_exchange": ([vp, vp, vp, vp], i),
@@ -698,6 +699,19 @@ class WangLandauWalkers:
         c = np.zeros(NUM_COUNTERS, dtype=np.int64)
         _check(load().brawl_wl_counters(self._h, w, _ptr(c)))
         return dict(zip(COUNTER_NAMES, (int(v) for v in c)))
+
+    # -- enter_energy_window (src/wang-landau.F90:643-741) -----------------------
+    def enter_windows(self, energy_min: float, energy_max: float, species_concentrations,
+                      species_numbers=None, initial: bool = True, max_steps: int = 10 ** 8) -> np.ndarray:
+        """The biased walk of every walker into its window (energy range in
+        meV/atom as wl_input gives it); returns the iterations each took."""
+        conc = np.ascontiguousarray(species_concentrations, dtype=np.float64)
+        nums = None if species_numbers is None else np.ascontiguousarray(species_numbers, dtype=np.int64)
+        steps = np.zeros(self.n, dtype=np.int64)
+        _check(load().brawl_wl_enter_windows(self._h, float(energy_min), float(energy_max), _ptr(conc),
+                                             None if nums is None else _ptr(nums), int(bool(initial)),
+                                             int(max_steps), _ptr(steps)))
+        return steps
 
     # -- radial-density samples inside sweeps() (src/wang-landau.F90:566-586) --
     def radial_enable(self, wc_range: int, shells, radial_samples: int, num_walkers: int) -> None:

@@ -1523,6 +1523,7 @@ struct brawl_wl {
   brawl_batch* b = nullptr;
   int bins = 0;
   double e1 = 0.0, range = 0.0;
+  std::vector<double> edges;             // bin_edges (bins + 1)
   std::vector<WlWalker> w;
   std::vector<WlGroup> groups;
   WlWalker* d_w = nullptr;
@@ -1627,6 +1628,7 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
   if (rc != BRAWL_OK) return cleanup(rc);
   wl->bins = bins;
   wl->e1 = bin_edges[0];
+  wl->edges.assign(bin_edges, bin_edges + bins + 1);
   wl->range = bin_edges[bins] - bin_edges[0];
   size_t hist_total = 0;
   for (int c = 0; c < n; ++c) hist_total += walkers[c].end_idx - walkers[c].start_idx + 1;
@@ -1783,6 +1785,81 @@ extern "C" int brawl_wl_reset_hist(brawl_wl* wl) {
   for (const WlWalker& W : wl->w) total += W.end - W.start + 1;
   CUDA_TRY(cudaMemsetAsync(wl->d_hist, 0, total * 8, wl->b->stream));
   CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_enter_windows(brawl_wl* wl, double energy_min, double energy_max,
+                                      const double* conc, const int64_t* numbers, int initial,
+                                      int64_t max_steps, int64_t* steps) {
+  if (!wl || !conc || max_steps < 1) return fail(BRAWL_EINVAL, "bad argument");
+  brawl_batch* b = wl->b;
+  const int n = (int)wl->w.size();
+  cudaStream_t s = b->stream;
+  int max_optin = 0;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  std::vector<WlEnterJob> jobs(n);
+  uint32_t smem = 0;
+  int64_t scratch = 0;
+  std::vector<int64_t> off(n);
+  for (int c = 0; c < n; ++c) {
+    off[c] = scratch;
+    scratch += b->models[c].g.n_sites;
+  }
+  double* d_site_e = nullptr;
+  WlEnterJob* d_jobs = nullptr;
+  if (dalloc(&d_site_e, (size_t)scratch * 8, s) != cudaSuccess ||
+      dalloc(&d_jobs, (size_t)n * sizeof(WlEnterJob), s) != cudaSuccess) {
+    dfree(d_site_e, s);
+    return fail(BRAWL_ENOMEM, "burn-in scratch");
+  }
+  auto cleanup = [&](int rc) {
+    dfree(d_site_e, s);
+    dfree(d_jobs, s);
+    return rc;
+  };
+  for (int c = 0; c < n; ++c) {
+    const Model& m = b->models[c];
+    WlEnterJob& E = jobs[c];
+    std::memset(&E, 0, sizeof(E));
+    E.job = b->jobs[c];
+    std::vector<double> cc(conc, conc + m.g.ns + 1);
+    int rc = make_init_job(m, cc.data(), numbers, E.init);
+    if (rc != BRAWL_OK) return cleanup(fail(rc, "walker " + std::to_string(c) + ": " + g_err));
+    E.init.lat = E.job.lat;
+    E.init.rng = E.job.rng;
+    E.init.counters = E.job.counters;
+    E.init.status = E.job.status;
+    const WlWalker& W = wl->w[c];
+    E.min_e = wl->edges[W.start - 1];
+    E.max_e = wl->edges[W.end];
+    // (2.0 * (0.0025 * ABS(energy_max - energy_min) * n_atoms / (Ry_to_eV * 1000))**2):
+    // energy_min/max and 0.0025 are default (single precision) reals, so the
+    // product up to n_atoms is single precision; the division by the double
+    // Ry_to_eV * 1000 and the rest are double
+    const float d4 = std::fabs((float)energy_max - (float)energy_min);
+    const float x4 = (0.0025f * d4) * (float)m.g.n_sites;
+    const double x = (double)x4 / (13.605693122 * 1000.0);
+    E.sig2x2 = 2.0 * (x * x);
+    E.max_steps = max_steps;
+    E.site_e = d_site_e + off[c];
+    E.initial = initial ? 1 : 0;
+    smem = std::max(smem, wl_enter_smem_bytes(m.g));
+  }
+  if (smem > (uint32_t)max_optin) return cleanup(fail(BRAWL_EINVAL, "lattice too large for the burn-in kernel"));
+  CUDA_TRY(cudaMemcpyAsync(d_jobs, jobs.data(), (size_t)n * sizeof(WlEnterJob), cudaMemcpyHostToDevice, s));
+  launch_wl_enter(d_jobs, n, smem, s);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(jobs.data(), d_jobs, (size_t)n * sizeof(WlEnterJob), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  cleanup(BRAWL_OK);
+  int rc = check_status(b);
+  if (rc != BRAWL_OK) return rc;
+  bool all = true;
+  for (int c = 0; c < n; ++c) {
+    if (steps) steps[c] = jobs[c].steps;
+    all = all && jobs[c].steps > 0;
+  }
+  if (!all) return fail(BRAWL_ESTATE, "a walker did not enter its window within max_steps");
   return BRAWL_OK;
 }
 

@@ -141,6 +141,30 @@ void launch_metropolis(const ChainJob* d_jobs, int n_jobs, bool lattice_in_smem,
 // initial_setup (src/initialise.F90:434-617) on the device, one warp per
 // chain.  Per chain: counts[ns] species quotas, lo_w/hi_w[ns] the interval
 // bounds in units of 2^-32 (w >= lo_w and w <= hi_w <=> lo <= u <= hi).
+// ---------------------------------------------------------------------------
+// Site energies in the reference's order: each shell sum starts from 0.0
+// and adds V_ex(species, neighbour, shell) in list order; the shell sums are
+// added left to right (src/bw_hamiltonian.f90:898-1262, 1712-1910,
+// 2059-2106).
+// ---------------------------------------------------------------------------
+__device__ inline double site_energy_ref(const Geom& g, const int8_t* lat, const double* V,
+                                  const uint32_t* ents, const int16_t* sstart, int x, int y,
+                                  int z) {
+  const int cs = lat[compact_index(g, x, y, z)];
+  double total = 0.0;
+  for (int sh = 0; sh < g.nsh; ++sh) {
+    double e = 0.0;
+    for (int k = sstart[sh]; k < sstart[sh + 1]; ++k) {
+      int dx, dy, dz, shk;
+      unpack_entry(ents[k], dx, dy, dz, shk);
+      const int s = lat[neighbour_index(g, x, y, z, dx, dy, dz)];
+      e = __dadd_rn(e, V[(cs - 1) + g.ns * ((s - 1) + g.ns * sh)]);
+    }
+    total = sh == 0 ? e : __dadd_rn(total, e);
+  }
+  return total;
+}
+
 struct InitJob {
   int8_t* lat;
   uint32_t* rng;

@@ -41,30 +41,6 @@ void launch_initial_setup(const InitJob* d_jobs, int n_jobs, cudaStream_t stream
   if (n_jobs > 0) initial_setup_kernel<<<n_jobs, 32, 0, stream>>>(d_jobs);
 }
 
-// ---------------------------------------------------------------------------
-// Site energies in the reference's order: each shell sum starts from 0.0
-// and adds V_ex(species, neighbour, shell) in list order; the shell sums are
-// added left to right (src/bw_hamiltonian.f90:898-1262, 1712-1910,
-// 2059-2106).  Grid-stride over (chain, site) pairs.
-// ---------------------------------------------------------------------------
-__device__ double site_energy_ref(const Geom& g, const int8_t* lat, const double* V,
-                                  const uint32_t* ents, const int16_t* sstart, int x, int y,
-                                  int z) {
-  const int cs = lat[compact_index(g, x, y, z)];
-  double total = 0.0;
-  for (int sh = 0; sh < g.nsh; ++sh) {
-    double e = 0.0;
-    for (int k = sstart[sh]; k < sstart[sh + 1]; ++k) {
-      int dx, dy, dz, shk;
-      unpack_entry(ents[k], dx, dy, dz, shk);
-      const int s = lat[neighbour_index(g, x, y, z, dx, dy, dz)];
-      e = __dadd_rn(e, V[(cs - 1) + g.ns * ((s - 1) + g.ns * sh)]);
-    }
-    total = sh == 0 ? e : __dadd_rn(total, e);
-  }
-  return total;
-}
-
 __global__ void site_energies_kernel(const EnergyJob* __restrict__ jobs, int n_jobs,
                                      int64_t total_sites) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total_sites;

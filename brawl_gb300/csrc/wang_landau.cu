@@ -367,6 +367,139 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   }
 }
 
+// full_energy (src/bw_hamiltonian.f90:58-81) of the staged lattice: the
+// site energies in the reference's order, one lane per site, then their sum
+// in site order on one lane and the half.  Returned in every lane.
+__device__ double full_energy_warp(const Geom& g, const int8_t* lat, const double* V,
+                                   const uint32_t* ents, const int16_t* sstart, double* site_e,
+                                   int lane) {
+  for (int i = lane; i < g.n_sites; i += 32) {
+    int x, y, z;
+    decode_site(g, i, x, y, z);
+    site_e[i] = site_energy_ref(g, lat, V, ents, sstart, x, y, z);
+  }
+  __syncwarp();
+  double e = 0.0;
+  if (lane == 0) {
+    for (int i = 0; i < g.n_sites; ++i) e = __dadd_rn(e, site_e[i]);
+    e = __dmul_rn(0.5, e);
+  }
+  e = __shfl_sync(kFull, e, 0);
+  __syncwarp();
+  return e;
+}
+
+// enter_energy_window (src/wang-landau.F90:643-741), one warp per walker:
+// the walk biased towards the middle of the window, log(u) < -delta_e with
+// delta_e = ((e_sw - target)^2 - (e_un - target)^2) / sig2x2 decided from
+// the reference-order pair energies, until full_energy lies inside the
+// window's inner 80%; every n_atoms*250 steps initial_setup draws the
+// configuration again (the running energy left as it is, as the reference
+// leaves it).  Bounded by max_steps.
+__global__ void __launch_bounds__(32, 1) wl_enter_kernel(WlEnterJob* __restrict__ jobs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int64_t check[kMaxSpecies];
+  WlEnterJob& E = jobs[blockIdx.x];
+  const ChainJob& J = E.job;
+  const Geom g = J.g;
+  const int lane = threadIdx.x;
+  const int nV = g.ns * g.ns * g.nsh;
+  uint32_t* mt = reinterpret_cast<uint32_t*>(smem);
+  double* V = reinterpret_cast<double*>(smem + align_up(kMTN * 4, 16));
+  uint32_t* ents = reinterpret_cast<uint32_t*>(V + nV);
+  int16_t* sstart = reinterpret_cast<int16_t*>(ents + g.z);
+  int8_t* lat = reinterpret_cast<int8_t*>(
+      smem + align_up((uint32_t)(reinterpret_cast<unsigned char*>(sstart + g.nsh + 1) - smem), 16));
+  double* vbuf = reinterpret_cast<double*>(
+      smem + align_up((uint32_t)(reinterpret_cast<unsigned char*>(lat + g.n_sites) - smem), 16));
+  for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
+  for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
+  for (int i = lane; i < g.z; i += 32) ents[i] = J.entries[i];
+  for (int i = lane; i <= g.nsh; i += 32) sstart[i] = J.shell_start[i];
+  for (int i = lane; i < g.n_sites; i += 32) lat[i] = J.lat[i];
+  int pos = (int)J.rng[kMTN];
+  __syncwarp();
+  unsigned long long draws = 0;
+  int status = kStatusOk;
+  if (E.initial && !initial_setup_warp(E.init, lat, mt, pos, check, draws, lane)) status = kStatusBadSpecies;
+  const double lo = E.min_e, hi = E.max_e;
+  const double target = __ddiv_rn(__dadd_rn(lo, hi), 2.0);
+  const double cond = __dmul_rn(fabs(__dsub_rn(hi, lo)), 0.1);
+  const double in_hi = __dsub_rn(hi, cond), in_lo = __dadd_rn(lo, cond);
+  const int64_t reinit = (int64_t)g.n_sites * 250;
+  double e_un = status == kStatusOk ? full_energy_warp(g, lat, V, ents, sstart, E.site_e, lane) : 0.0;
+  int64_t steps = -1, i_steps = 0;
+  DecideStats st = {0u, 0u};
+  for (int64_t it = 1; it <= E.max_steps && status == kStatusOk; ++it) {
+    if (++i_steps % reinit == 0) {
+      i_steps = 0;
+      if (!initial_setup_warp(E.init, lat, mt, pos, check, draws, lane)) {
+        status = kStatusBadSpecies;
+        break;
+      }
+    }
+    if (e_un < in_hi && e_un > in_lo) {
+      e_un = full_energy_warp(g, lat, V, ents, sstart, E.site_e, lane);
+      if (e_un < in_hi && e_un > in_lo) {
+        steps = it;
+        break;
+      }
+      continue;
+    }
+    const uint32_t w = mt_peek(mt, pos, 6, lane);
+    SitePair p;
+    draw_site(g, __shfl_sync(kFull, w, 0), __shfl_sync(kFull, w, 1), __shfl_sync(kFull, w, 2), p.ax,
+              p.ay, p.az);
+    draw_site(g, __shfl_sync(kFull, w, 3), __shfl_sync(kFull, w, 4), __shfl_sync(kFull, w, 5), p.bx,
+              p.by, p.bz);
+    pos += 6;
+    p.ai = compact_index(g, p.ax, p.ay, p.az);
+    p.bi = compact_index(g, p.bx, p.by, p.bz);
+    p.sa = lat[p.ai];
+    p.sb = lat[p.bi];
+    if (p.sa != p.sb) {
+      double p_un, p_sw;
+      exact_pair_energies_staged(g, CompactLat{lat}, V, ents, sstart, p, lane, p_un, p_sw, vbuf);
+      const double e_sw = __dadd_rn(__dsub_rn(e_un, p_un), p_sw);
+      const double a = __dsub_rn(e_sw, target), b = __dsub_rn(e_un, target);
+      const double d = __ddiv_rn(__dsub_rn(__dmul_rn(a, a), __dmul_rn(b, b)), E.sig2x2);
+      const uint32_t wu = __shfl_sync(kFull, mt_peek(mt, pos, 1, lane), 0);
+      pos += 1;
+      if (log_u_lt(wu, -d, st)) {
+        e_un = e_sw;
+        if (lane == 0) {
+          lat[p.ai] = (int8_t)p.sb;
+          lat[p.bi] = (int8_t)p.sa;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  __syncwarp();
+  for (int i = lane; i < g.n_sites; i += 32) J.lat[i] = lat[i];
+  for (int i = lane; i < kMTN; i += 32) J.rng[i] = mt[i];
+  if (lane == 0) {
+    J.rng[kMTN] = (uint32_t)(pos < 0 ? 0 : pos);
+    E.steps = steps;
+    E.energy = e_un;
+    if (status != kStatusOk) *J.status = status;
+  }
+}
+
+uint32_t wl_enter_smem_bytes(const Geom& g) {
+  uint32_t b = align_up(kMTN * 4, 16) + (uint32_t)(g.ns * g.ns * g.nsh) * 8 + (uint32_t)g.z * 4 +
+               (uint32_t)(g.nsh + 1) * 2;
+  b = align_up(b, 16) + (uint32_t)g.n_sites;
+  b = align_up(b, 16) + 4u * (uint32_t)g.z * 8;
+  return align_up(b, 16);
+}
+
+void launch_wl_enter(WlEnterJob* d_jobs, int n, uint32_t smem, cudaStream_t stream) {
+  cudaFuncSetAttribute(wl_enter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  BRAWL_CARVEOUT(wl_enter_kernel);
+  if (n > 0) wl_enter_kernel<<<n, 32, smem, stream>>>(d_jobs);
+}
+
 // The window average: for every bin, the walkers' values summed in walker
 // order and divided by their count (MPI_Allreduce SUM then /num_walkers,
 // src/wang-landau.F90:628-631; dos_average, :1127-1133, averages ln g

@@ -47,6 +47,23 @@ struct WlWalker {
   int32_t rad_n_offsets, rad_n_class;  // the plan's sizes (shared memory)
 };
 
+// enter_energy_window (src/wang-landau.F90:643-741) for one walker.
+struct WlEnterJob {
+  ChainJob job;          // lattice (compact), stream, V, entries, shell starts
+  InitJob init;          // initial_setup of the redraws (and of the start)
+  double min_e, max_e;   // the window's outer bin edges
+  double sig2x2;         // 2 (0.0025 |E_max - E_min| n_atoms / (Ry_to_eV 1000))^2
+  int64_t max_steps;
+  double* site_e;        // n_sites scratch for full_energy
+  int64_t steps;         // out: loop iterations, -1 when max_steps ran out
+  double energy;         // out: the final full_energy
+  int32_t initial;       // draw the starting configuration with initial_setup first
+  int32_t pad;
+};
+
+uint32_t wl_enter_smem_bytes(const Geom& g);
+void launch_wl_enter(WlEnterJob* d_jobs, int n, uint32_t smem, cudaStream_t stream);
+
 // Walkers first..first+count-1 share a window and are averaged together.
 struct WlGroup {
   int32_t first, count;

@@ -8,14 +8,19 @@ walker, replica exchange between adjacent windows, per-walker flatness with
 the converged flag held until every walker is flat, then ln f halved, the
 histograms reset, dos_average and dos_combine -- until ln f falls below the
 tolerance -- and, when asked, the radial-density samples of sweeps() with
-save_rho_E's bookkeeping (:359-396).  Replaced: the burn-in into the windows (enter_energy_window
-:643-741, a biased walk with MPI messages) is a temperature search with the
-device Metropolis kernel that stops each walker inside the central 80% of
-its window, the same acceptance region; pre-sampling, window optimisation
-and the per-bin configuration reloads (which draw from gfortran's
-random_number) are left out.  The density of states is therefore the
-reference's only statistically (its own test compares against the stored
-result with a 1% NRMSE criterion), which is the comparison made here.
+save_rho_E's bookkeeping (:359-396).  The burn-in into the windows is the
+reference's enter_energy_window (:643-741) on the device (burn_in =
+"reference"): the biased walk of every walker from initial_setup on its own
+stream; of the walkers of a window, the one that got in first (fewest
+iterations, then the lowest index, where the reference's MPI race decides)
+hands its configuration to the others.  Alternatively (burn_in =
+"temperature") a temperature search with the device Metropolis kernel that
+stops each walker inside the same central 80% of its window.  Left out:
+pre-sampling, window optimisation (driven by wall times) and the per-bin
+configuration reloads (which draw from gfortran's random_number).  The
+density of states is therefore the reference's only statistically (its own
+test compares against the stored result with a 1% NRMSE criterion), which
+is the comparison made here.
 """
 from __future__ import annotations
 
@@ -128,7 +133,8 @@ def save_rho_E(W: WangLandauWalkers, radial_samples: int, state: dict) -> None:
 
 
 def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: int = 110179,
-                exchange: bool = True, max_calls: int = 1_000_000, log=None, radial=None) -> dict:
+                exchange: bool = True, max_calls: int = 1_000_000, log=None, radial=None,
+                burn_in: str = "temperature", numbers=None) -> dict:
     """Runs the main loop to wl.tolerance.  wl: the wl_input fields
     (mc_sweeps, bins, num_windows, bin_overlap, tolerance, flatness, wl_f,
     energy_min, energy_max).  radial (optional): dict(wc_range, shells,
@@ -146,10 +152,29 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
         lo_e, hi_e = edges[s - 1], edges[e]
         cond = abs(hi_e - lo_e) * 0.1
         targets.append((lo_e + cond, hi_e - cond))
-    cfgs, _ = _burn_in(setup, V, seeds, conc, targets, n_atoms)
+    if burn_in == "temperature":
+        cfgs, _ = _burn_in(setup, V, seeds, conc, targets, n_atoms)
+    elif burn_in == "reference":
+        # placeholders: enter_windows draws every walker's start with initial_setup
+        tmp = Batch([dict(setup=setup, V=V, seed=seeds[0], beta=0.0, species_concentrations=conc,
+                          species_numbers=numbers)])
+        cfgs = [tmp.config(0)] * n
+        tmp.close()
+    else:
+        raise ValueError(f"unknown burn_in {burn_in!r}")
     walkers = [dict(setup=setup, V=V, seed=seeds[r], config=cfgs[r], start_idx=windows[r // walkers_per_window][0],
-                    end_idx=windows[r // walkers_per_window][1], window=r // walkers_per_window) for r in range(n)]
+                    end_idx=windows[r // walkers_per_window][1], window=r // walkers_per_window,
+                    nbr_swap=bool(getattr(wl, "nbr_swap", False))) for r in range(n)]
     W = WangLandauWalkers(walkers, edges)
+    burn_steps = None
+    if burn_in == "reference":
+        burn_steps = W.enter_windows(wl.energy_min, wl.energy_max, conc, numbers, initial=True)
+        for win in range(wl.num_windows):
+            ks = list(range(win * walkers_per_window, (win + 1) * walkers_per_window))
+            first = min(ks, key=lambda k: (burn_steps[k], k))
+            for k in ks:
+                if k != first:
+                    W.set_config(k, W.config(first))
     rad_state = {"rho_saved": True, "rho_of_E": None, "radial_min": 0.0}
     if radial is not None:
         W.radial_enable(radial["wc_range"], radial["shells"], radial["radial_samples"], walkers_per_window)
@@ -183,4 +208,5 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
         save_rho_E(W, radial["radial_samples"], rad_state)
     W.close()
     return {"lng": lng, "bin_edges": edges, "windows": windows, "record": record, "calls": calls,
-            "rho_of_E": rad_state["rho_of_E"], "radial_min": rad_state["radial_min"]}
+            "rho_of_E": rad_state["rho_of_E"], "radial_min": rad_state["radial_min"],
+            "burn_in_steps": burn_steps}

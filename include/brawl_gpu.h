@@ -312,6 +312,18 @@ int brawl_wl_swap_configs(brawl_wl *wl, int a, int b);
 /* n genrand() draws from a walker's stream (exchange shuffles and tests). */
 int brawl_wl_genrand(brawl_wl *wl, int walker, int64_t n, double *out);
 int brawl_wl_counters(brawl_wl *wl, int walker, int64_t *counters);
+/* enter_energy_window (src/wang-landau.F90:643-741) for every walker: the
+ * biased walk into the inner 80% of the walker's window (energy_min /
+ * energy_max the wl_input range in meV/atom, single-precision values as the
+ * reference reads them, which set the bias width), on
+ * the walker's own stream; with initial != 0 the walk starts from
+ * initial_setup(conc, numbers) (numbers may be NULL), which also draws the
+ * redraws every n_atoms*250 steps.  steps (n, may be NULL) gets each
+ * walker's loop iterations.  The MPI hand-over (the first walker of a window
+ * in sends its configuration to the others) is left to the caller.
+ * BRAWL_ESTATE when a walker has not entered after max_steps. */
+int brawl_wl_enter_windows(brawl_wl *wl, double energy_min, double energy_max, const double *conc,
+                           const int64_t *numbers, int initial, int64_t max_steps, int64_t *steps);
 /* Radial-density samples inside sweeps() (src/wang-landau.F90:566-586):
  * while a bin's radial_record is under MAX(radial_samples / num_walkers, 1)
  * and its radial_record_bool is unset, every n_atoms-th trial that proposes

@@ -971,3 +971,49 @@ double bo_wl_flatness(const double *hist, int n)
     }
     return mn / (s / (double)n);
 }
+
+/* enter_energy_window (src/wang-landau.F90:643-741), one walker. */
+int64_t bo_wl_enter_window(const bo_model *m, int8_t *cfg, bo_rng *r, const double *conc,
+                           const int64_t *numbers, double min_e, double max_e, double sig2x2,
+                           int64_t max_steps, double *energy_out)
+{
+    const double target = (min_e + max_e) / 2.0;
+    const double condition = fabs(max_e - min_e) * 0.1;
+    const int64_t reinit = (int64_t)bo_n_atoms(m) * 50 * 5;
+    double conc_buf[16];
+    double e_un = bo_total_energy(m, cfg);
+    int64_t i_steps = 0;
+    for (int64_t it = 1; it <= max_steps; it++) {
+        i_steps++;
+        if (i_steps % reinit == 0) {
+            i_steps = 0;
+            for (int k = 0; k <= m->ns; k++) conc_buf[k] = conc[k];
+            if (bo_initial_setup(m, conc_buf, numbers, r, cfg) != 0) return -1;
+        }
+        if (e_un < max_e - condition && e_un > min_e + condition) {
+            e_un = bo_total_energy(m, cfg);
+            if (e_un < max_e - condition && e_un > min_e + condition) {
+                *energy_out = e_un;
+                return it;
+            }
+            continue;
+        }
+        int a[3], b[3];
+        bo_random_site(m, r, a);
+        bo_random_site(m, r, b);
+        const int8_t s1 = cfg[cfg_index(m, a[0], a[1], a[2])];
+        const int8_t s2 = cfg[cfg_index(m, b[0], b[1], b[2])];
+        if (s1 != s2) {
+            const double p_un = bo_pair_energy(m, cfg, a, b);
+            pair_swap(m, cfg, a, b);
+            const double p_sw = bo_pair_energy(m, cfg, a, b);
+            const double e_sw = e_un - p_un + p_sw;
+            const double delta_e = ((e_sw - target) * (e_sw - target) -
+                                    (e_un - target) * (e_un - target)) / sig2x2;
+            if (log(bo_rng_uniform(r)) < -delta_e) e_un = e_sw;
+            else pair_swap(m, cfg, a, b);
+        }
+    }
+    *energy_out = e_un;
+    return -1;
+}

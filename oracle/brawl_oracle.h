@@ -178,6 +178,18 @@ int64_t bo_wl_sweep_radial(const bo_model *m, const bo_wl_params *p, int8_t *cfg
                            bo_rng *r, const double *bin_edges, double *lng,
                            double *hist, double *energy, bo_counters *c,
                            const bo_wl_radial *rad);
+/* enter_energy_window (src/wang-landau.F90:643-741) for one walker,
+ * without the MPI hand-over between walkers of a window: the biased walk
+ * towards the middle of [min_e, max_e] until the energy is inside the inner
+ * 80% (checked with full_energy).  sig2x2 = 2 (0.0025 |E_max - E_min| n_atoms
+ * / (Ry_to_eV 1000))^2.  Every n_atoms*50*5 steps the configuration is drawn
+ * again with initial_setup (conc / numbers as initial_setup takes them); the
+ * running energy is not recomputed then, as in the reference.  Returns the
+ * loop iterations taken, or -1 after max_steps; energy_out gets the final
+ * full_energy. */
+int64_t bo_wl_enter_window(const bo_model *m, int8_t *cfg, bo_rng *r, const double *conc,
+                           const int64_t *numbers, double min_e, double max_e, double sig2x2,
+                           int64_t max_steps, double *energy_out);
 int64_t bo_wl_sweep(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
                     bo_rng *r, const double *bin_edges, double *lng,
                     double *hist, double *energy, bo_counters *c);

@@ -130,6 +130,8 @@ def lib():
         L.bo_wl_sweep_radial.argtypes = [C.POINTER(Model), C.POINTER(WlParams), vp, C.POINTER(Rng), vp,
                                          vp, vp, vp, C.POINTER(Counters), C.POINTER(WlRadial)]
         L.bo_wl_sweep_radial.restype = i64
+        L.bo_wl_enter_window.argtypes = [C.POINTER(Model), vp, C.POINTER(Rng), vp, vp, dp, dp, dp, i64, vp]
+        L.bo_wl_enter_window.restype = i64
         L.bo_wl_replica_exchange.argtypes = [C.c_int, C.c_int, vp, vp, vp, C.c_int, vp, vp,
                                              C.POINTER(Rng), vp, C.c_size_t, vp, vp]
         L.bo_wl_dos_combine.argtypes = [C.c_int, vp, vp, C.c_int, vp, vp]
@@ -299,6 +301,16 @@ class OracleModel:
         acc = lib().bo_ns_walk(C.byref(self.m), _ptr(cfg), C.byref(rng.s), _ptr(e), ener_limit, n_steps,
                                C.byref(c))
         return acc, float(e[0]), c
+
+    def wl_enter_window(self, cfg, rng, conc, numbers, min_e, max_e, sig2x2, max_steps):
+        """enter_energy_window for one walker: (iterations or -1, energy)."""
+        conc = np.ascontiguousarray(np.asarray(conc, dtype=np.float64))
+        nums = None if numbers is None else np.ascontiguousarray(np.asarray(numbers, dtype=np.int64))
+        e = np.zeros(1)
+        it = lib().bo_wl_enter_window(C.byref(self.m), _ptr(cfg), C.byref(rng.s), _ptr(conc),
+                                      None if nums is None else _ptr(nums), float(min_e), float(max_e),
+                                      float(sig2x2), int(max_steps), _ptr(e))
+        return int(it), float(e[0])
 
     def wl_sweep(self, cfg, rng, bin_edges, lng, hist, energy, bins, start_idx, end_idx, n_trials,
                  wl_f, hist_period, nbr_swap=False, radial=None):

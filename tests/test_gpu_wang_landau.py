@@ -280,3 +280,43 @@ def test_wang_landau_radial_samples_match_oracle(nbr):
             assert np.array_equal(wl.config(k), cfgs[k])
             assert np.array_equal(wl.lng(k), lngs[k])
     assert sum(int(r["record"].sum()) for r in rads) > 8
+
+
+def test_enter_windows_match_oracle():
+    """enter_energy_window on the device (brawl_wl_enter_windows, starting
+    from initial_setup on each walker's stream) against the oracle's walk:
+    iterations, configuration, energy and stream of every walker."""
+    rng = np.random.default_rng(44)
+    lattice, n, ns, nsh = "bcc", (4, 4, 4), 3, 4
+    V = random_V(rng, ns, nsh)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    mod = O.OracleModel(lattice, *n, V)
+    conc = conc_vector(ns)
+    nums = None
+    c0, _ = mod.initial_setup(O.OracleRng(1), conc, nums)
+    E = np.array([mod.total_energy(mod.initial_setup(O.OracleRng(s), conc, nums)[0]) for s in range(20)])
+    bins = 40
+    half = max(float(np.ptp(E)), 0.02) * 1.5
+    edges = float(E.mean()) - half + np.arange(bins + 1) * (2 * half / bins)
+    windows = [(1, 22), (19, 40)]
+    walkers = []
+    for win, (lo, hi) in enumerate(windows):
+        for rep in range(2):
+            walkers.append(dict(setup=setup, V=V, seed=110179 + 11 * len(walkers), config=c0, start_idx=lo,
+                                end_idx=hi, window=win))
+    e_min_mev, e_max_mev = -30.0, 20.0
+    W = B.WangLandauWalkers(walkers, edges)
+    steps = W.enter_windows(e_min_mev, e_max_mev, conc, nums, initial=True, max_steps=2_000_000)
+    f32 = np.float32
+    x4 = (f32(0.0025) * abs(f32(e_max_mev) - f32(e_min_mev))) * f32(setup.n_atoms)
+    x = float(x4) / (13.605693122 * 1000.0)
+    sig2x2 = 2.0 * (x * x)
+    for k, w in enumerate(walkers):
+        r = O.OracleRng(w["seed"])
+        cfg, _ = mod.initial_setup(r, conc, nums)
+        it, e = mod.wl_enter_window(cfg, r, conc, nums, edges[w["start_idx"] - 1], edges[w["end_idx"]],
+                                    sig2x2, 2_000_000)
+        assert it > 0 and steps[k] == it, k
+        assert np.array_equal(W.config(k), cfg), k
+        assert W.energies()[k] == e
+        assert np.array_equal(W.genrand(k, 10), np.array([r.uniform() for _ in range(10)])), k

@@ -18,15 +18,25 @@ pytestmark = pytest.mark.gpu
 G = os.path.join(os.path.dirname(__file__), "golden", "04_parallel_wang-landau")
 
 
-def test_wang_landau_reproduces_the_reference_dos():
+@pytest.mark.parametrize("burn_in", ["temperature", "reference"])
+def test_wang_landau_reproduces_the_reference_dos(burn_in):
+    """burn_in "reference" enters the windows with enter_energy_window on
+    the device; "temperature" with the temperature search."""
     p = I.read_control_file(os.path.join(G, "brawl.inp"))
     wl = I.read_wl_file(os.path.join(G, "wl_input.inp"))
     V = I.read_exchange(os.path.join(G, "bcc_epi.vij"), p.n_species, p.interaction_range)
     setup = B.Setup.from_run_params(p)
     conc = np.asarray(p.species_concentrations, dtype=np.float64)
-    out = WLD.wang_landau(setup, V, conc, wl)
+    radial = None
+    if burn_in == "reference":
+        # the run's radial-density samples too (wl_input radial_samples, wc_range)
+        radial = dict(wc_range=p.wc_range, shells=B.Chain(setup, V).lattice_shells(p.wc_range),
+                      radial_samples=wl.radial_samples)
+    out = WLD.wang_landau(setup, V, conc, wl, burn_in=burn_in, numbers=p.numbers_or_none(), radial=radial)
     ver = np.load(os.path.join(G, "wl_dos.npz"))["grid_data"]
     run = out["lng"]
     assert out["windows"] == [[1, 128], [97, 256], [217, 384], [343, 512]]
     nrmse = np.sqrt(np.mean((ver - run) ** 2)) / np.mean(ver)
     assert nrmse < 0.01, nrmse
+    if radial is not None:
+        assert out["radial_min"] > 0.0

@@ -281,3 +281,85 @@ def test_sweeps_radial_samples_match_python_restatement(nbr):
     assert np.array_equal(ra["rho_of_E"], rb["rho_of_E"])
     assert ra["steps"][0] == rb["steps"][0]
     assert np.all(ra["record"][::7] == 0) and np.all(ra["record"] <= 2)
+
+
+def _py_enter_window(mod, cfg, rng, conc, nums, min_e, max_e, sig2x2, max_steps):
+    """enter_energy_window (src/wang-landau.F90:643-741) written out from the
+    reference, one walker, the oracle giving sites, energies and
+    initial_setup."""
+    target = (min_e + max_e) / 2.0
+    cond = abs(max_e - min_e) * 0.1
+    reinit = mod.n_atoms * 50 * 5
+    e_un = mod.total_energy(cfg)
+    i_steps = 0
+    for it in range(1, max_steps + 1):
+        i_steps += 1
+        if i_steps % reinit == 0:
+            i_steps = 0
+            new, _ = mod.initial_setup(rng, conc, nums)
+            cfg[...] = new
+        if max_e - cond > e_un > min_e + cond:
+            e_un = mod.total_energy(cfg)
+            if max_e - cond > e_un > min_e + cond:
+                return it, e_un
+            continue
+        a, b = mod.random_site(rng), mod.random_site(rng)
+        s1, s2 = cfg[a[2], a[1], a[0]], cfg[b[2], b[1], b[0]]
+        if s1 != s2:
+            p_un = mod.pair_energy(cfg, a, b)
+            cfg[a[2], a[1], a[0]], cfg[b[2], b[1], b[0]] = s2, s1
+            e_sw = e_un - p_un + mod.pair_energy(cfg, a, b)
+            d = ((e_sw - target) * (e_sw - target) - (e_un - target) * (e_un - target)) / sig2x2
+            if math.log(rng.uniform()) < -d:
+                e_un = e_sw
+            else:
+                cfg[a[2], a[1], a[0]], cfg[b[2], b[1], b[0]] = s1, s2
+    return -1, e_un
+
+
+def test_enter_window_matches_python_restatement():
+    rng = np.random.default_rng(13)
+    ns, nsh, n = 3, 2, 3
+    V = np.zeros((ns, ns, nsh))
+    for sh in range(nsh):
+        a = rng.uniform(-0.05, 0.05, size=(ns, ns))
+        V[:, :, sh] = (np.triu(a) + np.triu(a, 1).T) / 13.605693122
+    mod = O.OracleModel("bcc", n, n, n, V)
+    conc = np.array([0.0, 1 / 3, 1 / 3, 1 / 3])
+    nums = np.array([18, 18, 18])
+    cfg, _ = mod.initial_setup(O.OracleRng(5), conc, nums)
+    e0 = mod.total_energy(cfg)
+    # a window below the start: the walk has to go down
+    lo, hi = e0 - 0.04, e0 - 0.02
+    sig2x2 = 2.0 * (float(np.float32(0.0025)) * 40.0 * 54 / (13.605693122 * 1000)) ** 2
+    ca, cb = cfg.copy(), cfg.copy()
+    ra, rb = O.OracleRng(91), O.OracleRng(91)
+    it_a, e_a = mod.wl_enter_window(ca, ra, conc, nums, lo, hi, sig2x2, 200000)
+    it_b, e_b = _py_enter_window(mod, cb, rb, conc, nums, lo, hi, sig2x2, 200000)
+    assert it_a == it_b > 0 and e_a == e_b
+    assert np.array_equal(ca, cb)
+    assert np.array_equal(ra.state_words(), rb.state_words())
+    assert lo + 0.1 * (hi - lo) < e_a < hi - 0.1 * (hi - lo)
+
+
+def test_enter_window_redraws_like_the_reference():
+    """An unreachable window: the walk redraws the configuration every
+    n_atoms * 250 steps (the running energy kept stale, as the reference
+    keeps it) and stops at max_steps."""
+    rng = np.random.default_rng(14)
+    ns, nsh, n = 3, 2, 3
+    V = np.zeros((ns, ns, nsh))
+    for sh in range(nsh):
+        a = rng.uniform(-0.05, 0.05, size=(ns, ns))
+        V[:, :, sh] = (np.triu(a) + np.triu(a, 1).T) / 13.605693122
+    mod = O.OracleModel("bcc", n, n, n, V)
+    conc = np.array([0.0, 1 / 3, 1 / 3, 1 / 3])
+    cfg, _ = mod.initial_setup(O.OracleRng(6), conc, np.array([18, 18, 18]))
+    lo, hi = -100.0, -99.0
+    sig2x2 = 0.5
+    ca, cb = cfg.copy(), cfg.copy()
+    ra, rb = O.OracleRng(92), O.OracleRng(92)
+    it_a, e_a = mod.wl_enter_window(ca, ra, conc, np.array([18, 18, 18]), lo, hi, sig2x2, 30000)
+    it_b, e_b = _py_enter_window(mod, cb, rb, conc, np.array([18, 18, 18]), lo, hi, sig2x2, 30000)
+    assert it_a == it_b == -1 and e_a == e_b
+    assert np.array_equal(ca, cb) and np.array_equal(ra.state_words(), rb.state_words())
