@@ -30,14 +30,25 @@ import numpy as np
 
 from . import K_B_IN_RY, RY_TO_EV, Batch, Setup, WangLandauWalkers
 
-__all__ = ["create_energy_bins", "divide_range", "create_overlap", "save_rho_E", "wang_landau"]
+__all__ = ["create_energy_bins", "divide_range", "create_overlap", "save_rho_E", "compute_mean_energy",
+           "wang_landau"]
+
+
+def bin_width_ry(n_atoms: int, energy_min: float, energy_max: float, bins: int) -> float:
+    """bin_width (src/wang-landau.F90:976-980): energy_min/max are default
+    (single precision) reals, so (energy_max - energy_min)/real(bins) is
+    single precision; the conversion to Ry, n_atoms/(Ry_to_eV*1000), double."""
+    f32 = np.float32
+    w = f32(f32(f32(energy_max) - f32(energy_min)) / f32(bins))
+    return float(w) * (n_atoms / (RY_TO_EV * 1000.0))
 
 
 def create_energy_bins(n_atoms: int, energy_min: float, energy_max: float, bins: int) -> np.ndarray:
     """bin_edges(1:bins+1) in Ry from meV/atom (src/wang-landau.F90:969-992)."""
     energy_to_ry = n_atoms / (RY_TO_EV * 1000.0)
-    bin_width = (energy_max - energy_min) / float(np.float32(bins)) * energy_to_ry
-    return np.array([energy_min * energy_to_ry + i * bin_width for i in range(bins + 1)])
+    bin_width = bin_width_ry(n_atoms, energy_min, energy_max, bins)
+    e0 = float(np.float32(energy_min)) * energy_to_ry
+    return np.array([e0 + i * bin_width for i in range(bins + 1)])
 
 
 def divide_range(bins: int, num_windows: int) -> list[list[int]]:
@@ -103,6 +114,30 @@ def _burn_in(setup: Setup, V, seeds, conc, targets, n_atoms, max_rounds=400):
     rng_states = [b.rng_state(k) for k in range(n)]
     b.close()
     return cfgs, rng_states
+
+
+def _seq_sum(a: np.ndarray) -> float:
+    """SUM as a left-to-right loop."""
+    return float(np.cumsum(a)[-1]) if a.size else 0.0
+
+
+def compute_mean_energy(lng, bin_edges, bins: int, bin_width: float) -> np.ndarray:
+    """compute_mean_energy (src/wang-landau.F90:457-477): for T = 10, 20,
+    ..., 3000 K, the canonical mean energy from ln g over the bin centres.
+    Returns mean_energy(itemp, 1:2) as (300, 2): the mean energy and beta.
+    The exponentials use numpy's exp, which may differ from the C library's
+    in the last bit, so the values are the reference's to rounding."""
+    buf = np.asarray(lng, dtype=np.float64) - np.max(lng)
+    centres = np.asarray(bin_edges[:bins], dtype=np.float64) + 0.5 * bin_width
+    out = np.zeros((300, 2))
+    for itemp in range(1, 301):
+        beta = 1.0 / (K_B_IN_RY * itemp * 10.0)
+        prob = buf - beta * centres
+        prob = np.exp(prob - np.max(prob))
+        prob = prob / _seq_sum(prob)
+        out[itemp - 1, 0] = _seq_sum(centres * prob)
+        out[itemp - 1, 1] = beta
+    return out
 
 
 def save_rho_E(W: WangLandauWalkers, radial_samples: int, state: dict) -> None:
@@ -207,6 +242,8 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
     if radial is not None:
         save_rho_E(W, radial["radial_samples"], rad_state)
     W.close()
+    mean_energy = compute_mean_energy(lng, edges, wl.bins,
+                                      bin_width_ry(n_atoms, wl.energy_min, wl.energy_max, wl.bins))
     return {"lng": lng, "bin_edges": edges, "windows": windows, "record": record, "calls": calls,
             "rho_of_E": rad_state["rho_of_E"], "radial_min": rad_state["radial_min"],
-            "burn_in_steps": burn_steps}
+            "burn_in_steps": burn_steps, "mean_energy": mean_energy}

@@ -181,3 +181,18 @@ def test_annealing_alro_host_logic():
     assert out["order_of_T"].shape == ref.shape
     assert np.array_equal(out["order_of_T"], ref)
     assert np.allclose(out["order_of_T"].sum(axis=-1)[:, cfg > 0], 1.0)  # occupied sites: one species each
+
+
+def test_compute_mean_energy():
+    """compute_mean_energy (src/wang-landau.F90:457-477): beta per row, the
+    canonical mean over the bin centres, low T at the low-energy end."""
+    from brawl_gb300.wang_landau import compute_mean_energy
+    bins = 50
+    edges = -1.0 + np.arange(bins + 1) * 0.02
+    lng = 40.0 * np.sin(np.linspace(0, np.pi, bins))      # a smooth ln g, largest mid-range
+    me = compute_mean_energy(lng, edges, bins, 0.02)
+    assert me.shape == (300, 2)
+    assert np.allclose(me[:, 1], 1.0 / (B.K_B_IN_RY * np.arange(1, 301) * 10.0), rtol=0, atol=0)
+    centres = edges[:bins] + 0.01
+    assert np.all(me[:, 0] >= centres[0] - 1e-12) and np.all(me[:, 0] <= centres[-1] + 1e-12)
+    assert me[0, 0] < me[-1, 0]                              # colder: lower mean energy
