@@ -15,8 +15,9 @@ stream; of the walkers of a window, the one that got in first (fewest
 iterations, then the lowest index, where the reference's MPI race decides)
 hands its configuration to the others.  Alternatively (burn_in =
 "temperature") a temperature search with the device Metropolis kernel that
-stops each walker inside the same central 80% of its window.  Left out:
-pre-sampling, window optimisation (driven by wall times) and the per-bin
+stops each walker inside the same central 80% of its window.  Pre-sampling
+(:757-808) is optional (pre_sample=True).  Left out: window optimisation
+and the configuration reloads it needs, and the per-bin
 configuration reloads (which draw from gfortran's random_number).  The
 density of states is therefore the reference's only statistically (its own
 test compares against the stored result with a 1% NRMSE criterion), which
@@ -140,6 +141,44 @@ def compute_mean_energy(lng, bin_edges, bins: int, bin_width: float) -> np.ndarr
     return out
 
 
+def pre_sampling(W: WangLandauWalkers, wl, walkers_per_window: int, n_atoms: int, f: float,
+                 exchange: bool = True, max_calls: int = 1_000_000) -> int:
+    """pre_sampling (src/wang-landau.F90:757-808) up to its dos_average and
+    dos_combine: sweeps() of every walker at the initial wl_f, replica
+    exchange after the 10th call and every 9th after it, until every
+    window is pre-sampled -- a window is as soon as one of its walkers has
+    min(hist) > 1000/num_walkers and is flatter than wl_flatness (the
+    reference's MPI_MAX over ranks); a walker of a pre-sampled window has its
+    histogram set to n_atoms + 1 once.  Returns the sweeps() calls made."""
+    trials = wl.mc_sweeps * n_atoms
+    period = int(0.02 * float(np.float32(n_atoms)))
+    nwin = wl.num_windows
+    done = np.zeros(nwin, dtype=bool)
+    state = np.zeros(W.n, dtype=bool)
+    i_sweeps = 0
+    calls = 0
+    while not done.all() and calls < max_calls:
+        W.sweeps(trials, f, period)
+        calls += 1
+        i_sweeps += 1
+        if i_sweeps % 10 == 0:
+            i_sweeps = 1
+            if exchange and nwin > 1:
+                W.replica_exchange()
+        flat = W.flatness()
+        for k in range(W.n):
+            if not state[k] and flat[k] > wl.flatness and W.hist(k).min() > 1000.0 / float(walkers_per_window):
+                done[k // walkers_per_window] = True
+        for k in range(W.n):
+            if done[k // walkers_per_window] and not state[k]:
+                state[k] = True
+                h = W.hist(k)
+                W.set_hist(k, np.full(h.size, float(np.float32(n_atoms)) + 1.0))
+    W.average()
+    W.dos_combine()
+    return calls
+
+
 def save_rho_E(W: WangLandauWalkers, radial_samples: int, state: dict) -> None:
     """save_rho_E (src/wang-landau.F90:359-396): the walkers' radial_record
     summed (walker order for the reference's MPI_REDUCE), radial_record_bool
@@ -169,7 +208,7 @@ def save_rho_E(W: WangLandauWalkers, radial_samples: int, state: dict) -> None:
 
 def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: int = 110179,
                 exchange: bool = True, max_calls: int = 1_000_000, log=None, radial=None,
-                burn_in: str = "temperature", numbers=None) -> dict:
+                burn_in: str = "temperature", numbers=None, pre_sample: bool = False) -> dict:
     """Runs the main loop to wl.tolerance.  wl: the wl_input fields
     (mc_sweeps, bins, num_windows, bin_overlap, tolerance, flatness, wl_f,
     energy_min, energy_max).  radial (optional): dict(wc_range, shells,
@@ -217,6 +256,10 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
     f = float(wl.wl_f)
     trials = wl.mc_sweeps * n_atoms
     period = int(0.02 * float(np.float32(n_atoms)))
+    pre_calls = 0
+    if pre_sample:
+        pre_calls = pre_sampling(W, wl, walkers_per_window, n_atoms, f, exchange, max_calls)
+        W.reset_hist()                   # mpi_wl_hist = 0 before the main loop
     converged = np.zeros(n, dtype=bool)
     record = []
     calls = 0
@@ -246,4 +289,4 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
                                       bin_width_ry(n_atoms, wl.energy_min, wl.energy_max, wl.bins))
     return {"lng": lng, "bin_edges": edges, "windows": windows, "record": record, "calls": calls,
             "rho_of_E": rad_state["rho_of_E"], "radial_min": rad_state["radial_min"],
-            "burn_in_steps": burn_steps, "mean_energy": mean_energy}
+            "burn_in_steps": burn_steps, "mean_energy": mean_energy, "pre_sampling_calls": pre_calls}

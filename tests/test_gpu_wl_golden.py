@@ -21,7 +21,8 @@ G = os.path.join(os.path.dirname(__file__), "golden", "04_parallel_wang-landau")
 @pytest.mark.parametrize("burn_in", ["temperature", "reference"])
 def test_wang_landau_reproduces_the_reference_dos(burn_in):
     """burn_in "reference" enters the windows with enter_energy_window on
-    the device; "temperature" with the temperature search."""
+    the device and pre-samples, with the radial-density samples on;
+    "temperature" enters with the temperature search."""
     p = I.read_control_file(os.path.join(G, "brawl.inp"))
     wl = I.read_wl_file(os.path.join(G, "wl_input.inp"))
     V = I.read_exchange(os.path.join(G, "bcc_epi.vij"), p.n_species, p.interaction_range)
@@ -32,7 +33,8 @@ def test_wang_landau_reproduces_the_reference_dos(burn_in):
         # the run's radial-density samples too (wl_input radial_samples, wc_range)
         radial = dict(wc_range=p.wc_range, shells=B.Chain(setup, V).lattice_shells(p.wc_range),
                       radial_samples=wl.radial_samples)
-    out = WLD.wang_landau(setup, V, conc, wl, burn_in=burn_in, numbers=p.numbers_or_none(), radial=radial)
+    out = WLD.wang_landau(setup, V, conc, wl, burn_in=burn_in, numbers=p.numbers_or_none(), radial=radial,
+                          pre_sample=burn_in == "reference")
     ver = np.load(os.path.join(G, "wl_dos.npz"))["grid_data"]
     run = out["lng"]
     assert out["windows"] == [[1, 128], [97, 256], [217, 384], [343, 512]]
