@@ -123,6 +123,12 @@ def load(rebuild: bool = False):
         "brawl_wl_enter_windows": ([vp, C.c_double, C.c_double, vp, vp, i, C.c_int64, vp], i),
         "brawl_wl_radial_set_done": ([vp, vp], i),
         "brawl_wl_radial_get": ([vp, i, vp, vp, vp], i),
+        "brawl_wl_store_enable": ([vp], i),
+        "brawl_wl_store_flags": ([vp, vp], i),
+        "brawl_wl_store_merge": ([vp, vp], i),
+        "brawl_wl_store_load": ([vp, i, i], i),
+        "brawl_wl_store_get": ([vp, i, i, vp], i),
+        "brawl_wl_set_windows": ([vp, vp, vp], i),
         "brawl_wl_replica_exchange": ([vp, vp, vp, vp], i),
         "brawl_wl_flatness": ([vp, vp], i),
         "brawl_wl_dos_combine": ([vp, vp], i),
@@ -589,7 +595,7 @@ class WangLandauWalkers:
         n = len(walkers)
         descs = (_WlDesc * n)()
         keep = []
-        self.walkers = walkers
+        self.walkers = [dict(w) for w in walkers]  # windows may change (set_windows)
         for k, w in enumerate(walkers):
             s = w["setup"]
             V = _v_array(s, w["V"])
@@ -736,3 +742,46 @@ class WangLandauWalkers:
         st = np.zeros(1, dtype=np.int32)
         _check(load().brawl_wl_radial_get(self._h, w, _ptr(rec), _ptr(rho), _ptr(st)))
         return rec, rho, int(st[0])
+
+    # -- the configuration store (config_per_bin, src/wang-landau.F90:605-622) --
+    def store_enable(self) -> None:
+        """Every walker's per-bin configuration slots, all open."""
+        _check(load().brawl_wl_store_enable(self._h))
+
+    def store_flags(self) -> np.ndarray:
+        """config_store of every walker: (n, bins) bool, True = open."""
+        out = np.zeros((self.n, self.bins), dtype=np.uint8)
+        _check(load().brawl_wl_store_flags(self._h, _ptr(out)))
+        return out.astype(bool)
+
+    def store_merge(self, pick) -> None:
+        """merge_configs' copies: pick[bin - 1] is the walker whose slot
+        every walker takes, or -1 (the bin reopens)."""
+        p = np.ascontiguousarray(pick, dtype=np.int32)
+        if p.size != self.bins:
+            raise ValueError("pick needs one entry per bin")
+        _check(load().brawl_wl_store_merge(self._h, _ptr(p)))
+
+    def store_load(self, w: int, bin_1based: int) -> None:
+        """load_window_config: walker w takes its stored configuration of the bin."""
+        _check(load().brawl_wl_store_load(self._h, int(w), int(bin_1based)))
+
+    def store_config(self, w: int, bin_1based: int) -> np.ndarray:
+        """Walker w's stored configuration of the bin, (2n3, 2n2, 2n1) as config()."""
+        out = np.zeros(self.walkers[w]["setup"].grid_shape, dtype=np.int8)
+        _check(load().brawl_wl_store_get(self._h, int(w), int(bin_1based), _ptr(out)))
+        return out
+
+    def set_windows(self, start_idx, end_idx) -> None:
+        """Per window, the new 1-based [start, end] (overlap included); the
+        histograms restart from 0, ln g is kept."""
+        a = np.ascontiguousarray(start_idx, dtype=np.int32)
+        b = np.ascontiguousarray(end_idx, dtype=np.int32)
+        _check(load().brawl_wl_set_windows(self._h, _ptr(a), _ptr(b)))
+        win = [d["window"] for d in self.walkers]
+        first = {}
+        for k, wi in enumerate(win):
+            first.setdefault(wi, len(first))
+        for k, d in enumerate(self.walkers):
+            j = first[d["window"]]
+            d["start_idx"], d["end_idx"] = int(a[j]), int(b[j])

@@ -1551,6 +1551,11 @@ struct brawl_wl {
   int* d_nacc = nullptr;
   double* d_flat = nullptr;
   double* d_combined = nullptr;
+  // configuration store (brawl_wl_store_enable): every walker's bins slots,
+  // their open flags (walker-major) and merge_configs' picks
+  int8_t* d_store = nullptr;
+  uint8_t* d_store_open = nullptr;
+  int* d_pick = nullptr;
 };
 
 namespace {
@@ -1590,7 +1595,8 @@ extern "C" int brawl_wl_destroy(brawl_wl* wl) {
                           (const void*)wl->d_flat, (const void*)wl->d_combined, (const void*)wl->d_rad,
                           (const void*)wl->d_rad_offsets, (const void*)wl->d_rad_masks,
                           (const void*)wl->d_rad_done, (const void*)wl->d_rad_record,
-                          (const void*)wl->d_rad_rho, (const void*)wl->d_rad_steps})
+                          (const void*)wl->d_rad_rho, (const void*)wl->d_rad_steps,
+                          (const void*)wl->d_store, (const void*)wl->d_store_open, (const void*)wl->d_pick})
       dfree(p, wl->b->stream);
     brawl_batch_destroy(wl->b);
   }
@@ -1951,6 +1957,166 @@ extern "C" int brawl_wl_radial_get(brawl_wl* wl, int c, int32_t* record, double*
     CUDA_TRY(cudaMemcpy(rho_of_E, wl->d_rad_rho + (size_t)c * wl->bins * per, (size_t)wl->bins * per * 8,
                         cudaMemcpyDeviceToHost));
   if (steps) CUDA_TRY(cudaMemcpy(steps, wl->d_rad_steps + c, 4, cudaMemcpyDeviceToHost));
+  return BRAWL_OK;
+}
+
+namespace {
+bool same_lattice(const Geom& a, const Geom& b) {
+  return a.lattice == b.lattice && a.n1 == b.n1 && a.n2 == b.n2 && a.n3 == b.n3;
+}
+}  // namespace
+
+extern "C" int brawl_wl_store_enable(brawl_wl* wl) {
+  if (!wl) return fail(BRAWL_EINVAL, "null argument");
+  if (wl->d_store) return fail(BRAWL_EINVAL, "configuration store already enabled");
+  brawl_batch* b = wl->b;
+  const int n = (int)wl->w.size();
+  std::vector<size_t> off(n);
+  size_t total = 0;
+  for (int c = 0; c < n; ++c) {
+    off[c] = total;
+    total += (size_t)wl->bins * (size_t)b->models[c].g.n_sites;
+  }
+  cudaStream_t s = b->stream;
+  if (dalloc(&wl->d_store, total, s) != cudaSuccess ||
+      dalloc(&wl->d_store_open, (size_t)n * wl->bins, s) != cudaSuccess ||
+      dalloc(&wl->d_pick, (size_t)wl->bins * sizeof(int), s) != cudaSuccess) {
+    for (const void* p : {(const void*)wl->d_store, (const void*)wl->d_store_open, (const void*)wl->d_pick})
+      dfree(p, s);
+    wl->d_store = nullptr;
+    wl->d_store_open = nullptr;
+    wl->d_pick = nullptr;
+    return fail(BRAWL_ENOMEM, "configuration store (bins x sites per walker)");
+  }
+  CUDA_TRY(cudaMemsetAsync(wl->d_store, 0, total, s));             // config_per_bin = 0
+  CUDA_TRY(cudaMemsetAsync(wl->d_store_open, 1, (size_t)n * wl->bins, s));  // config_store = .True.
+  CUDA_TRY(cudaStreamSynchronize(s));
+  for (int c = 0; c < n; ++c) {
+    wl->w[c].store = wl->d_store + off[c];
+    wl->w[c].store_open = wl->d_store_open + (size_t)c * wl->bins;
+  }
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_store_flags(brawl_wl* wl, uint8_t* open) {
+  if (!wl || !open) return fail(BRAWL_EINVAL, "null argument");
+  if (!wl->d_store) return fail(BRAWL_EINVAL, "configuration store not enabled");
+  CUDA_TRY(cudaMemcpy(open, wl->d_store_open, wl->w.size() * (size_t)wl->bins, cudaMemcpyDeviceToHost));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_store_merge(brawl_wl* wl, const int* pick) {
+  if (!wl || !pick) return fail(BRAWL_EINVAL, "null argument");
+  if (!wl->d_store) return fail(BRAWL_EINVAL, "configuration store not enabled");
+  brawl_batch* b = wl->b;
+  const int n = (int)wl->w.size();
+  for (int c = 1; c < n; ++c)
+    if (!same_lattice(b->models[c].g, b->models[0].g)) return fail(BRAWL_EINVAL, "walkers have different lattices");
+  std::vector<uint8_t> open((size_t)n * wl->bins);
+  CUDA_TRY(cudaMemcpy(open.data(), wl->d_store_open, open.size(), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < wl->bins; ++k) {
+    if (pick[k] < -1 || pick[k] >= n) return fail(BRAWL_EINVAL, "pick outside -1 .. n_walkers-1");
+    if (pick[k] >= 0 && open[(size_t)pick[k] * wl->bins + k])
+      return fail(BRAWL_EINVAL, "bin " + std::to_string(k + 1) + ": the picked walker holds no configuration");
+  }
+  cudaStream_t s = b->stream;
+  CUDA_TRY(cudaMemcpyAsync(wl->d_pick, pick, (size_t)wl->bins * sizeof(int), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), n * sizeof(WlWalker), cudaMemcpyHostToDevice, s));
+  launch_wl_store_merge(wl->d_w, n, wl->bins, wl->d_pick, s);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return BRAWL_OK;
+}
+
+namespace {
+int store_slot(brawl_wl* wl, int c, int bin, const int8_t** slot) {
+  if (!wl || c < 0 || c >= (int)wl->w.size() || bin < 1 || bin > wl->bins) return fail(BRAWL_EINVAL, "bad argument");
+  if (!wl->d_store) return fail(BRAWL_EINVAL, "configuration store not enabled");
+  uint8_t open = 1;
+  CUDA_TRY(cudaMemcpy(&open, wl->w[c].store_open + (bin - 1), 1, cudaMemcpyDeviceToHost));
+  if (open) return fail(BRAWL_ESTATE, "walker " + std::to_string(c) + ": bin " + std::to_string(bin) +
+                                          " holds no stored configuration");
+  *slot = wl->w[c].store + (size_t)(bin - 1) * (size_t)wl->b->models[c].g.n_sites;
+  return BRAWL_OK;
+}
+}  // namespace
+
+extern "C" int brawl_wl_store_load(brawl_wl* wl, int c, int bin) {
+  const int8_t* slot = nullptr;
+  TRY(store_slot(wl, c, bin, &slot));
+  brawl_batch* b = wl->b;
+  CUDA_TRY(cudaMemcpyAsync(b->jobs[c].lat, slot, (size_t)b->models[c].g.n_sites, cudaMemcpyDeviceToDevice,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_store_get(brawl_wl* wl, int c, int bin, int8_t* config) {
+  if (!config) return fail(BRAWL_EINVAL, "null argument");
+  const int8_t* slot = nullptr;
+  TRY(store_slot(wl, c, bin, &slot));
+  brawl_batch* b = wl->b;
+  const Geom& g = b->models[c].g;
+  const size_t grid = (size_t)8 * g.n1 * g.n2 * g.n3;
+  TRY(ensure_grid(b, grid));
+  launch_unpack(g, slot, b->d_grid, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(config, b->d_grid, grid, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+extern "C" int brawl_wl_set_windows(brawl_wl* wl, const int* start_idx, const int* end_idx) {
+  if (!wl || !start_idx || !end_idx) return fail(BRAWL_EINVAL, "null argument");
+  const int nwin = (int)wl->groups.size();
+  for (int k = 0; k < nwin; ++k)
+    if (start_idx[k] < 1 || end_idx[k] > wl->bins || start_idx[k] > end_idx[k])
+      return fail(BRAWL_EINVAL, "window " + std::to_string(k + 1) + " outside 1..bins");
+  brawl_batch* b = wl->b;
+  int max_optin = 0;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  const int rad_bins = wl->d_rad ? wl->bins : 0;
+  // the layout of every walker first: nothing changes if one does not fit
+  std::vector<int> cap(wl->w.size());
+  uint32_t smem = 0;
+  bool all_D = true;
+  size_t hist_total = 0;
+  for (int k = 0; k < nwin; ++k) {
+    const WlGroup& G = wl->groups[k];
+    const int nb = end_idx[k] - start_idx[k] + 1;
+    for (int c = G.first; c < G.first + G.count; ++c) {
+      const Geom& g = wl->w[c].job.g;
+      const uint32_t base = wl_smem_bytes(g, nb, 0, rad_bins, wl->rad_n_off, wl->rad_n_class);
+      cap[c] = lazy_cap_for(g, base, (uint32_t)max_optin);
+      if (cap[c] == 0) return fail(BRAWL_EINVAL, "window " + std::to_string(k + 1) + " too large for shared memory");
+      smem = std::max(smem, wl_smem_bytes(g, nb, cap[c], rad_bins, wl->rad_n_off, wl->rad_n_class));
+      all_D = all_D && walker_layout(g, nb, cap[c]).use_D;
+      hist_total += (size_t)nb;
+    }
+  }
+  if (smem > (uint32_t)max_optin) return fail(BRAWL_EINVAL, "windows too large for shared memory");
+  // mpi_arrays (src/wang-landau.F90:1351-1379): the histograms start from 0
+  cudaStream_t s = b->stream;
+  double* d_hist = nullptr;
+  if (dalloc(&d_hist, hist_total * 8, s) != cudaSuccess) return fail(BRAWL_ENOMEM, "window histograms");
+  CUDA_TRY(cudaMemsetAsync(d_hist, 0, hist_total * 8, s));
+  dfree(wl->d_hist, s);
+  wl->d_hist = d_hist;
+  size_t hoff = 0;
+  for (int k = 0; k < nwin; ++k) {
+    const WlGroup& G = wl->groups[k];
+    for (int c = G.first; c < G.first + G.count; ++c) {
+      WlWalker& W = wl->w[c];
+      W.start = start_idx[k];
+      W.end = end_idx[k];
+      W.hist = d_hist + hoff;
+      W.lazy_cap = cap[c];
+      hoff += (size_t)(W.end - W.start + 1);
+    }
+  }
+  wl->smem = smem;
+  wl->all_D = all_D;
+  CUDA_TRY(cudaStreamSynchronize(s));
   return BRAWL_OK;
 }
 

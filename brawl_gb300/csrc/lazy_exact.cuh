@@ -73,7 +73,7 @@ __device__ inline LazyLog lazy_layout(const Geom& g, unsigned char* base, int ca
 // the histogram (Wang-Landau), the neighbour entries and shell starts, the
 // compact lattice, the staged exact-sum terms (4 z doubles) and the log.
 struct WalkerLayout {
-  uint32_t mt, tbuf, V, I, slices, ents, sstart, lat, vbuf, lazy;
+  uint32_t mt, tbuf, V, I, slices, sopen, ents, sstart, lat, vbuf, lazy;
   uint32_t rad, rad_offsets, rad_masks, rad_hist, total;  // radial-sample scratch
   uint32_t tab_len[3];
   int32_t F_off, D_off, use_D, nI;
@@ -102,7 +102,9 @@ __host__ __device__ inline WalkerLayout walker_layout(const Geom& g, int nb, int
   L.D_off = (int32_t)(ntab + nF);
   L.nI = (int32_t)(ntab + nF + (L.use_D ? nD : 0));
   L.slices = align_up(L.I + (uint32_t)L.nI * 4, 16);
-  L.ents = L.slices + 2u * (uint32_t)nb * 8;
+  // the window's ln g and histogram slices, then its open store flags
+  L.sopen = L.slices + 2u * (uint32_t)nb * 8;
+  L.ents = align_up(L.sopen + (uint32_t)nb, 4);
   L.sstart = L.ents + (uint32_t)g.z * 4;
   L.lat = align_up(L.sstart + (uint32_t)(g.nsh + 1) * 2, 16);
   L.vbuf = align_up(L.lat + (uint32_t)g.n_sites, 16);

@@ -100,6 +100,20 @@ __device__ __noinline__ void wl_radial_sample(const Geom& g, const int8_t* lat, 
   __syncwarp();
 }
 
+// config_per_bin(jbin, ...) = config: the warp copies the compact lattice
+// to the bin's store slot, in words when the size and the slot allow.  Out
+// of line: a bin is stored once.
+__device__ __noinline__ void wl_store_config(const Geom& g, const int8_t* lat, int8_t* dst, int lane) {
+  const int n = g.n_sites;
+  if ((n & 3) == 0 && (reinterpret_cast<uintptr_t>(dst) & 3) == 0) {
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(lat);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    for (int i = lane; i < (n >> 2); i += 32) d[i] = s[i];
+  } else {
+    for (int i = lane; i < n; i += 32) dst[i] = lat[i];
+  }
+}
+
 template <int NJ, bool kUseD>
 __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ walkers) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -120,6 +134,7 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   int32_t* F = I + WLy.F_off;
   double* lng = reinterpret_cast<double*>(smem + WLy.slices);
   double* hist = lng + nb;
+  uint8_t* sopen = smem + WLy.sopen;  // the window's open store flags
   uint32_t* ents = reinterpret_cast<uint32_t*>(smem + WLy.ents);
   int16_t* sstart = reinterpret_cast<int16_t*>(smem + WLy.sstart);
   int8_t* lat = reinterpret_cast<int8_t*>(smem + WLy.lat);
@@ -131,6 +146,7 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   for (int i = lane; i < nb; i += 32) {
     lng[i] = W.lng[W.start - 1 + i];
     hist[i] = W.hist[i];
+    sopen[i] = W.store ? W.store_open[W.start - 1 + i] : (uint8_t)0;
   }
   for (int i = lane; i < g.z; i += 32) ents[i] = J.entries[i];
   for (int i = lane; i <= g.nsh; i += 32) sstart[i] = J.shell_start[i];
@@ -331,6 +347,14 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
     }
     if (--until == 0) {
       if (lane == 0) hist[jbin - start] = __dadd_rn(hist[jbin - start], 1.0);
+      // config_per_bin(jbin) = config the first time the bin is sampled
+      // (src/wang-landau.F90:605-610); the flag reads alike in every lane
+      if (sopen[jbin - start]) {
+        __syncwarp();
+        wl_store_config(g, lat, W.store + (size_t)(jbin - 1) * (size_t)g.n_sites, lane);
+        __syncwarp();
+        if (lane == 0) sopen[jbin - start] = 0;
+      }
       until = period;
     }
     if (lane == 0) lng[jbin - start] = __dadd_rn(lng[jbin - start], f);
@@ -345,6 +369,7 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   for (int i = lane; i < nb; i += 32) {
     W.lng[W.start - 1 + i] = lng[i];
     W.hist[i] = hist[i];
+    if (W.store) W.store_open[W.start - 1 + i] = sopen[i];
   }
   for (int i = lane; i < g.n_sites; i += 32) J.lat[i] = lat[i];
   ring_writeback(mt, tbuf, ring, J.rng, lane);
@@ -870,6 +895,31 @@ void launch_wl_combine(WlWalker* d_walkers, int n, const WlGroup* d_groups, int 
   dim3 grid((bins + 255) / 256, n);
   BRAWL_CARVEOUT(wl_broadcast_kernel);
   wl_broadcast_kernel<<<grid, 256, 0, stream>>>(d_walkers, d_out);
+}
+
+// merge_configs (src/wang-landau.F90:1556-1615) after the host's draw: bin b
+// of every walker's store takes walker pick[b]'s slot (walker 0's when no
+// walker holds the bin, as rank 0's array is broadcast), and its flag is
+// closed when a walker held it, open otherwise.  One block per (bin,
+// walker stripe); the source slot is never written.
+__global__ void wl_store_merge_kernel(const WlWalker* __restrict__ W, int n, const int* __restrict__ pick) {
+  const int b = blockIdx.x;
+  const int src = pick[b] >= 0 ? pick[b] : 0;
+  const size_t n_sites = (size_t)W[src].job.g.n_sites;
+  const int8_t* from = W[src].store + (size_t)b * n_sites;
+  for (int w = blockIdx.y; w < n; w += gridDim.y) {
+    if (w != src) {
+      int8_t* to = W[w].store + (size_t)b * n_sites;
+      for (size_t i = threadIdx.x; i < n_sites; i += blockDim.x) to[i] = from[i];
+    }
+    if (threadIdx.x == 0) W[w].store_open[b] = pick[b] >= 0 ? 0 : 1;
+  }
+}
+
+void launch_wl_store_merge(const WlWalker* d_walkers, int n, int bins, const int* d_pick, cudaStream_t stream) {
+  if (n <= 0 || bins <= 0) return;
+  const dim3 grid((unsigned)bins, (unsigned)std::min(n, 64));
+  wl_store_merge_kernel<<<grid, 256, 0, stream>>>(d_walkers, n, d_pick);
 }
 
 }  // namespace brawl

@@ -45,6 +45,11 @@ struct WlWalker {
   double* rho_of_E;
   int32_t* radial_steps;
   int32_t rad_n_offsets, rad_n_class;  // the plan's sizes (shared memory)
+  // configuration store (config_per_bin / config_store, null when off):
+  // bins slots of n_sites bytes in the compact device layout, and one flag
+  // per bin, set while the bin's slot is still open
+  int8_t* store;
+  uint8_t* store_open;
 };
 
 // enter_energy_window (src/wang-landau.F90:643-741) for one walker.
@@ -86,5 +91,8 @@ void launch_wl_exchange(WlWalker* d_walkers, const double* d_energy, const WlGro
 void launch_wl_flatness(const WlWalker* d_walkers, int n, double* d_out, cudaStream_t stream);
 void launch_wl_combine(WlWalker* d_walkers, int n, const WlGroup* d_groups, int n_groups, int bins,
                        double* d_out, int* d_status, cudaStream_t stream);
+// merge_configs' copies: pick[bins] (device) names the walker whose slot each
+// bin takes, or -1
+void launch_wl_store_merge(const WlWalker* d_walkers, int n, int bins, const int* d_pick, cudaStream_t stream);
 
 }  // namespace brawl

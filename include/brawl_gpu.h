@@ -339,6 +339,36 @@ int brawl_wl_radial_set_done(brawl_wl *wl, const uint8_t *done);
 /* One walker's radial_record (bins), rho_of_E (bins * wc * ns * ns, i
  * fastest; may be NULL) and radial_mc_steps (may be NULL). */
 int brawl_wl_radial_get(brawl_wl *wl, int walker, int32_t *record, double *rho_of_E, int32_t *steps);
+/* The configuration store of sweeps() (config_per_bin / config_store,
+ * src/wang-landau.F90:60-61, 605-622, 1042-1043, 1109-1110): every walker
+ * gets bins slots (bins * n_sites bytes, zeroed) and their flags, all open;
+ * from then on, at every histogram tick the walker's configuration goes to
+ * the slot of the tick's bin if that bin is still open, which closes it.
+ * BRAWL_ENOMEM when the slots do not fit. */
+int brawl_wl_store_enable(brawl_wl *wl);
+/* The flags (n_walkers * bins bytes, walker-major; 1 = open, i.e. the
+ * reference's config_store(bin) = .True.). */
+int brawl_wl_store_flags(brawl_wl *wl, uint8_t *open);
+/* merge_configs (src/wang-landau.F90:1556-1615) after the caller's draw:
+ * pick[bin-1] is the walker whose slot every walker takes for that bin (the
+ * rank drawn among those holding it) or -1 when none holds it; the bin's
+ * flag becomes closed, or open for -1, in every walker.  The draw is the
+ * caller's (the reference uses gfortran's random_number).  All walkers must
+ * share the lattice. */
+int brawl_wl_store_merge(brawl_wl *wl, const int *pick);
+/* load_window_config (src/wang-landau.F90:1541-1554) after the caller's
+ * draw of the 1-based bin: the walker's configuration becomes its slot for
+ * that bin.  BRAWL_ESTATE when the slot is still open. */
+int brawl_wl_store_load(brawl_wl *wl, int walker, int bin);
+/* One stored configuration in the config(1, 2n1, 2n2, 2n3) layout. */
+int brawl_wl_store_get(brawl_wl *wl, int walker, int bin, int8_t *config);
+/* New windows after mpi_window_optimise (src/wang-landau.F90:1211-1328):
+ * start_idx / end_idx per window (1-based bins, overlap included as
+ * create_overlap gives it), applied to every walker of the window; the
+ * histograms restart from 0 as mpi_arrays reallocates them (:1351-1379).
+ * ln g is kept.  A walker whose energy then lies outside its window needs
+ * a configuration from it (brawl_wl_store_load) before the next sweeps. */
+int brawl_wl_set_windows(brawl_wl *wl, const int *start_idx, const int *end_idx);
 
 /* ====================================================================== */
 /* Serving: a request loop that admits anneal, Wang-Landau and nested-    */

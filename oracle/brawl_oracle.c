@@ -782,6 +782,14 @@ int64_t bo_wl_sweep_radial(const bo_model *m, const bo_wl_params *p, int8_t *cfg
                            double *hist, double *energy, bo_counters *c,
                            const bo_wl_radial *rad)
 {
+    return bo_wl_sweep_store(m, p, cfg, r, bin_edges, lng, hist, energy, c, rad, NULL);
+}
+
+int64_t bo_wl_sweep_store(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
+                          bo_rng *r, const double *bin_edges, double *lng,
+                          double *hist, double *energy, bo_counters *c,
+                          const bo_wl_radial *rad, const bo_wl_store *store)
+{
     const int n_atoms = bo_n_atoms(m);
     const int per_bin = rad ? m->ns * m->ns * rad->wc_range : 0;
     double rho_buf[15 * 15 * 64];
@@ -831,7 +839,13 @@ int64_t bo_wl_sweep_radial(const bo_model *m, const bo_wl_params *p, int8_t *cfg
             jbin = ibin;
             pair_swap(m, cfg, a, b);
         }
-        if (hist_tick) hist[jbin - p->start_idx] = hist[jbin - p->start_idx] + 1.0;
+        if (hist_tick) {
+            hist[jbin - p->start_idx] = hist[jbin - p->start_idx] + 1.0;
+            if (store && store->open[jbin - 1]) {
+                store->open[jbin - 1] = 0;
+                memcpy(store->slots + (size_t)(jbin - 1) * store->cfg_bytes, cfg, store->cfg_bytes);
+            }
+        }
         lng[jbin - 1] = lng[jbin - 1] + p->wl_f;
     }
     if (c) c->accepted += accepted;

@@ -178,6 +178,18 @@ int64_t bo_wl_sweep_radial(const bo_model *m, const bo_wl_params *p, int8_t *cfg
                            bo_rng *r, const double *bin_edges, double *lng,
                            double *hist, double *energy, bo_counters *c,
                            const bo_wl_radial *rad);
+/* The configuration store of sweeps() (config_per_bin / config_store,
+ * src/wang-landau.F90:605-622): at a histogram tick whose bin is still
+ * open, the configuration goes to that bin's slot and the bin closes. */
+typedef struct {
+    int8_t *slots;          /* bins x cfg_bytes, bin 1 first */
+    unsigned char *open;    /* bins; 1 = open (config_store = .True.) */
+    size_t cfg_bytes;
+} bo_wl_store;
+int64_t bo_wl_sweep_store(const bo_model *m, const bo_wl_params *p, int8_t *cfg,
+                          bo_rng *r, const double *bin_edges, double *lng,
+                          double *hist, double *energy, bo_counters *c,
+                          const bo_wl_radial *rad, const bo_wl_store *store);
 /* enter_energy_window (src/wang-landau.F90:643-741) for one walker,
  * without the MPI hand-over between walkers of a window: the biased walk
  * towards the middle of [min_e, max_e] until the energy is inside the inner

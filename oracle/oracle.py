@@ -72,6 +72,10 @@ class WlRadial(C.Structure):
                 ("record", C.c_void_p), ("rho_of_E", C.c_void_p), ("steps", C.c_void_p)]
 
 
+class WlStore(C.Structure):
+    _fields_ = [("slots", C.c_void_p), ("open", C.c_void_p), ("cfg_bytes", C.c_size_t)]
+
+
 class WlParams(C.Structure):
     _fields_ = [("bins", C.c_int), ("start_idx", C.c_int), ("end_idx", C.c_int),
                 ("n_trials", C.c_int64), ("wl_f", C.c_double), ("hist_period", C.c_int),
@@ -130,6 +134,10 @@ def lib():
         L.bo_wl_sweep_radial.argtypes = [C.POINTER(Model), C.POINTER(WlParams), vp, C.POINTER(Rng), vp,
                                          vp, vp, vp, C.POINTER(Counters), C.POINTER(WlRadial)]
         L.bo_wl_sweep_radial.restype = i64
+        L.bo_wl_sweep_store.argtypes = [C.POINTER(Model), C.POINTER(WlParams), vp, C.POINTER(Rng), vp,
+                                        vp, vp, vp, C.POINTER(Counters), C.POINTER(WlRadial),
+                                        C.POINTER(WlStore)]
+        L.bo_wl_sweep_store.restype = i64
         L.bo_wl_enter_window.argtypes = [C.POINTER(Model), vp, C.POINTER(Rng), vp, vp, dp, dp, dp, i64, vp]
         L.bo_wl_enter_window.restype = i64
         L.bo_wl_replica_exchange.argtypes = [C.c_int, C.c_int, vp, vp, vp, C.c_int, vp, vp,
@@ -313,10 +321,12 @@ class OracleModel:
         return int(it), float(e[0])
 
     def wl_sweep(self, cfg, rng, bin_edges, lng, hist, energy, bins, start_idx, end_idx, n_trials,
-                 wl_f, hist_period, nbr_swap=False, radial=None):
+                 wl_f, hist_period, nbr_swap=False, radial=None, store=None):
         """radial (optional): dict(shells, cap, done (uint8, bins), record
         (int32, bins), rho_of_E (float64, (bins, wc, ns, ns)), steps (int32,
-        1)), updated in place."""
+        1)), updated in place.  store (optional): dict(slots (int8, (bins,)
+        + cfg.shape), open (uint8, bins)), config_per_bin and config_store,
+        updated in place."""
         e = np.array([energy], dtype=np.float64)
         p = WlParams(bins, start_idx, end_idx, n_trials, wl_f, hist_period, int(bool(nbr_swap)))
         c = Counters()
@@ -329,9 +339,16 @@ class OracleModel:
             rad = WlRadial(radial["shells"].size, radial["shells"].ctypes.data, int(radial["cap"]),
                            radial["done"].ctypes.data, radial["record"].ctypes.data,
                            radial["rho_of_E"].ctypes.data, radial["steps"].ctypes.data)
-        acc = lib().bo_wl_sweep_radial(C.byref(self.m), C.byref(p), _ptr(cfg), C.byref(rng.s),
-                                       _ptr(bin_edges), _ptr(lng), _ptr(hist), _ptr(e), C.byref(c),
-                                       None if rad is None else C.byref(rad))
+        st = None
+        if store is not None:
+            sl, op = store["slots"], store["open"]
+            assert sl.dtype == np.int8 and sl.flags.c_contiguous and sl.shape[0] == bins
+            assert op.dtype == np.uint8 and op.flags.c_contiguous and op.size == bins
+            st = WlStore(sl.ctypes.data, op.ctypes.data, cfg.size)
+        acc = lib().bo_wl_sweep_store(C.byref(self.m), C.byref(p), _ptr(cfg), C.byref(rng.s),
+                                      _ptr(bin_edges), _ptr(lng), _ptr(hist), _ptr(e), C.byref(c),
+                                      None if rad is None else C.byref(rad),
+                                      None if st is None else C.byref(st))
         return acc, float(e[0]), c
 
 

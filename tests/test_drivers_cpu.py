@@ -196,3 +196,114 @@ def test_compute_mean_energy():
     centres = edges[:bins] + 0.01
     assert np.all(me[:, 0] >= centres[0] - 1e-12) and np.all(me[:, 0] <= centres[-1] + 1e-12)
     assert me[0, 0] < me[-1, 0]                              # colder: lower mean energy
+
+
+# ---------------------------------------------------------------------------
+# Wang-Landau window optimisation and the configuration store's host side
+# (src/wang-landau.F90:1211-1328, 1541-1615, 1686-1703)
+# ---------------------------------------------------------------------------
+from brawl_gb300 import wang_landau as WLD  # noqa: E402
+
+QUARTERS = [[1, 128], [129, 256], [257, 384], [385, 512]]
+
+
+def test_window_optimise_hand_cases():
+    """Each case worked by hand from the reference's formulas: weights
+    1/(steps/ABS(first-last+1)) normalised, mixed with the previous
+    fractions by alpha, floored at 0.02, NINT(bins * frac), rounding settled
+    on the windows by descending size."""
+    # iteration 0: alpha = 1, fractions (1, 1/2, 1, 1/4) / 2.75 -> 186, 93, 186, 47
+    iv, prev = WLD.window_optimise(0, QUARTERS, [1e6, 2e6, 1e6, 4e6], [0.25] * 4, 512)
+    assert iv == [[1, 186], [187, 279], [280, 465], [466, 512]]
+    assert np.allclose(prev, np.array([1.0, 0.5, 1.0, 0.25]) / 2.75, rtol=0, atol=1e-15)
+    # iteration 2: alpha = 0.8 * 0.8 = 0.64 mixed with the previous fractions:
+    # 137.59, 96.44, 174.45, 103.52 -> 138, 96, 174, 104
+    iv, _ = WLD.window_optimise(2, QUARTERS, [1e6, 2e6, 1e6, 4e6], [0.1, 0.2, 0.3, 0.4], 512)
+    assert iv == [[1, 138], [139, 234], [235, 408], [409, 512]]
+    # equal work keeps equal windows
+    iv, _ = WLD.window_optimise(1, QUARTERS, [1e6] * 4, [0.25] * 4, 512)
+    assert iv == QUARTERS
+    # three fast windows are floored at 0.02: the remainder comes off the free
+    # one (0.94 -> 481.28 -> 481), and the missing bin goes to the largest
+    iv, _ = WLD.window_optimise(0, QUARTERS, [1.0, 1e6, 1e6, 1e6], [0.25] * 4, 512)
+    assert iv == [[1, 482], [483, 492], [493, 502], [503, 512]]
+    # ABS(first - last + 1) = 32, 31, 31 bins: 34.04, 32.98, 32.98 -> 34, 33, 33
+    iv, _ = WLD.window_optimise(0, [[1, 34], [35, 67], [68, 100]], [5.0] * 3, [1 / 3] * 3, 100)
+    assert iv == [[1, 34], [35, 67], [68, 100]]
+    # performance outside 0-3, or one window: unchanged
+    for args in ((QUARTERS, 4), ([[1, 512]], 0)):
+        iv, prev = WLD.window_optimise(0, args[0], [1.0] * len(args[0]), [1.0] * len(args[0]), 512, args[1])
+        assert iv == args[0]
+
+
+def test_window_optimise_settles_rounding_by_descending_size():
+    # 100 bins over 3 equal windows of work: 33 each, the extra bin to the first
+    iv, _ = WLD.window_optimise(1, [[1, 34], [35, 68], [69, 100]], [1.0, 1.0, 1.0], [1 / 3] * 3, 100)
+    sizes = [e - s + 1 for s, e in iv]
+    assert sum(sizes) == 100 and iv[0][0] == 1 and iv[-1][1] == 100
+
+
+def test_sort_descending_is_the_reference_exchange_sort():
+    # ties keep the order the exchanges leave (3 before 1), not a stable sort's
+    assert WLD.sort_descending([3, 1, 4, 1, 5]) == [4, 2, 0, 3, 1]
+    assert WLD.sort_descending([33, 33, 33]) == [0, 1, 2]
+
+
+def test_nint_and_powi():
+    assert [WLD._nint(x) for x in (2.5, -2.5, 0.49999999999999994, 3.4999, 481.28)] == [3, -3, 0, 3, 481]
+    for k in range(0, 12):
+        y = 1.0
+        for _ in range(k):
+            y = y * 0.8
+        assert abs(WLD._powi(0.8, k) - y) <= 4e-16
+    assert WLD._powi(0.8, 3) == (0.8 * 0.8) * 0.8
+
+
+class FakeStore:
+    """The walker-store calls of the drivers, recorded."""
+
+    def __init__(self, open_, windows):
+        self.open = open_.copy()
+        self.n, self.bins = open_.shape
+        self.merged = None
+        self.loads = []
+
+    def store_flags(self):
+        return self.open.copy()
+
+    def store_merge(self, pick):
+        self.merged = np.array(pick)
+        for b, p in enumerate(pick):
+            self.open[:, b] = p < 0
+
+    def store_load(self, k, b):
+        assert not self.open[k, b - 1]
+        self.loads.append((k, b))
+
+
+def test_merge_and_load_draw_like_the_reference():
+    """merge_configs draws one holder per bin as ranks_with_config(1 +
+    int(u * size)); load_window_config draws min_bin + int(u * (max - min +
+    1)) over the walker's window; the draws come in bin then walker order."""
+    rng = np.random.default_rng(9)
+    open_ = rng.random((4, 20)) < 0.5
+    open_[:, 7] = True                     # nobody holds bin 8
+    W = FakeStore(open_, None)
+    pick = WLD.merge_configs(W, np.random.default_rng(123))
+    u = np.random.default_rng(123)
+    for b in range(20):
+        holders = np.nonzero(~open_[:, b])[0]
+        if holders.size:
+            assert pick[b] == holders[int(u.random() * holders.size)]
+        else:
+            assert pick[b] == -1
+    assert W.open[:, 7].all()
+    assert all(W.open[:, b].all() == (pick[b] < 0) for b in range(20))
+    W.open[:] = False                      # after a merge every visited bin is held
+    windows = [[1, 12], [9, 20]]
+    bins = WLD.load_window_config(W, windows, 2, np.random.default_rng(77))
+    u = np.random.default_rng(77)
+    for k in range(4):
+        s, e = windows[k // 2]
+        assert bins[k] == s + int(u.random() * (e - s + 1)) and s <= bins[k] <= e
+    assert W.loads == [(k, int(bins[k])) for k in range(4)]

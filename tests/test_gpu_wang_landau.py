@@ -320,3 +320,119 @@ def test_enter_windows_match_oracle():
         assert np.array_equal(W.config(k), cfg), k
         assert W.energies()[k] == e
         assert np.array_equal(W.genrand(k, 10), np.array([r.uniform() for _ in range(10)])), k
+
+
+def test_wang_landau_store_merge_windows_match_oracle():
+    """The configuration store of sweeps() (config_per_bin / config_store),
+    merge_configs' copies, load_window_config and new windows against the
+    oracle: flags, every stored configuration, ln g, histograms,
+    configurations and accepted moves, bit for bit, before and after the
+    windows change."""
+    lattice, n, ns, nsh = "bcc", (4, 4, 4), 4, 6
+    windows = [(1, 30), (19, 48)]
+    rng = np.random.default_rng(33)
+    V = random_V(rng, ns, nsh)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    mod0 = O.OracleModel(lattice, *n, V)
+    walkers, mods, cfgs, rngs = [], [], [], []
+    r0 = O.OracleRng(977)
+    for win, (lo, hi) in enumerate(windows):
+        for rep in range(2):
+            cfg, _ = mod0.initial_setup(r0, conc_vector(ns))
+            seed = 110179 + 11 * len(walkers)
+            walkers.append(dict(setup=setup, V=V, seed=seed, config=cfg.copy(), start_idx=lo,
+                                end_idx=hi, window=win))
+            mods.append(O.OracleModel(lattice, *n, V))
+            cfgs.append(cfg.copy())
+            rngs.append(O.OracleRng(seed))
+    E = np.array([mod0.total_energy(c) for c in cfgs])
+    bins = 48
+    half = max(float(np.ptp(E)), 0.02) * 4.0
+    bin_edges = float(E.mean()) - half + (np.arange(bins + 1) * (2 * half / bins))
+    nw = len(walkers)
+    lngs = [np.zeros(bins) for _ in walkers]
+    hists = [np.zeros(w["end_idx"] - w["start_idx"] + 1) for w in walkers]
+    stores = [dict(slots=np.zeros((bins,) + cfgs[0].shape, dtype=np.int8), open=np.ones(bins, dtype=np.uint8))
+              for _ in walkers]
+    wl = B.WangLandauWalkers(walkers, bin_edges)
+    wl.store_enable()
+    wl_f = float(np.float32(0.05))
+    period = int(0.02 * float(np.float32(setup.n_atoms)))
+
+    def run_calls(calls):
+        for _ in range(calls):
+            acc_o = []
+            for k, w in enumerate(walkers):
+                e = mods[k].total_energy(cfgs[k])
+                a, _, _ = mods[k].wl_sweep(cfgs[k], rngs[k], bin_edges, lngs[k], hists[k], e, bins,
+                                           w["start_idx"], w["end_idx"], 600, wl_f, period, store=stores[k])
+                acc_o.append(a)
+            for win in range(len(windows)):
+                idx = [k for k, w in enumerate(walkers) if w["window"] == win]
+                for arrs in (lngs, hists):
+                    s = arrs[idx[0]].copy()
+                    for k in idx[1:]:
+                        s = s + arrs[k]
+                    s = s / float(np.float32(len(idx)))
+                    for k in idx:
+                        arrs[k][:] = s
+            assert list(wl.sweeps(600, wl_f, period)) == acc_o
+        check_all()
+
+    def check_all():
+        flags = wl.store_flags()
+        for k in range(nw):
+            assert np.array_equal(flags[k], stores[k]["open"].astype(bool)), k
+            for b in np.nonzero(~flags[k])[0]:
+                assert np.array_equal(wl.store_config(k, int(b) + 1), stores[k]["slots"][b]), (k, b)
+            assert np.array_equal(wl.lng(k), lngs[k])
+            assert np.array_equal(wl.hist(k), hists[k])
+            assert np.array_equal(wl.config(k), cfgs[k])
+
+    run_calls(2)
+    closed = [np.nonzero(stores[k]["open"] == 0)[0] for k in range(nw)]
+    assert all(c.size > 0 for c in closed)
+    # an open bin holds nothing to load; a non-holder cannot be picked
+    open_bin = int(np.nonzero(stores[0]["open"])[0][0]) + 1 if stores[0]["open"].any() else None
+    if open_bin is not None:
+        with pytest.raises(B.BrawlError, match="holds no stored configuration"):
+            wl.store_load(0, open_bin)
+        bad = np.full(bins, -1, dtype=np.int32)
+        bad[open_bin - 1] = 0
+        with pytest.raises(B.BrawlError, match="holds no configuration"):
+            wl.store_merge(bad)
+
+    # merge_configs with a drawn holder per bin
+    pick = np.full(bins, -1, dtype=np.int32)
+    draw = np.random.default_rng(5)
+    for b in range(bins):
+        holders = [k for k in range(nw) if stores[k]["open"][b] == 0]
+        if holders:
+            pick[b] = holders[int(draw.random() * len(holders))]
+    wl.store_merge(pick)
+    for b in range(bins):
+        src = pick[b] if pick[b] >= 0 else 0
+        for k in range(nw):
+            if k != src:
+                stores[k]["slots"][b] = stores[src]["slots"][b]
+            stores[k]["open"][b] = 0 if pick[b] >= 0 else 1
+    check_all()
+
+    # new windows (the histograms restart), then a stored configuration of
+    # each walker's new window
+    new = [(1, 26), (20, 48)]
+    with pytest.raises(B.BrawlError, match="outside 1..bins"):
+        wl.set_windows([1, 20], [26, 49])
+    wl.set_windows([s for s, _ in new], [e for _, e in new])
+    for k, w in enumerate(walkers):
+        w["start_idx"], w["end_idx"] = new[w["window"]]
+        hists[k] = np.zeros(w["end_idx"] - w["start_idx"] + 1)
+    for k, w in enumerate(walkers):
+        inside = [b for b in range(w["start_idx"], w["end_idx"] + 1) if stores[k]["open"][b - 1] == 0]
+        assert inside
+        b = inside[int(draw.random() * len(inside))]
+        wl.store_load(k, b)
+        cfgs[k] = stores[k]["slots"][b - 1].copy()
+        assert O.wl_bin_index(mod0.total_energy(cfgs[k]), bin_edges, bins) == b
+    check_all()
+    run_calls(2)

@@ -21,8 +21,11 @@ G = os.path.join(os.path.dirname(__file__), "golden", "04_parallel_wang-landau")
 @pytest.mark.parametrize("burn_in", ["temperature", "reference"])
 def test_wang_landau_reproduces_the_reference_dos(burn_in):
     """burn_in "reference" enters the windows with enter_energy_window on
-    the device and pre-samples, with the radial-density samples on;
-    "temperature" enters with the temperature search."""
+    the device and pre-samples, with the radial-density samples on, the
+    per-bin configuration store, merge_configs, load_window_config at every
+    ln f step and mpi_window_optimise (wl_input leaves performance at 0, so
+    the reference's run resized its windows too); "temperature" enters with
+    the temperature search and keeps the windows."""
     p = I.read_control_file(os.path.join(G, "brawl.inp"))
     wl = I.read_wl_file(os.path.join(G, "wl_input.inp"))
     V = I.read_exchange(os.path.join(G, "bcc_epi.vij"), p.n_species, p.interaction_range)
@@ -37,7 +40,11 @@ def test_wang_landau_reproduces_the_reference_dos(burn_in):
                           pre_sample=burn_in == "reference")
     ver = np.load(os.path.join(G, "wl_dos.npz"))["grid_data"]
     run = out["lng"]
-    assert out["windows"] == [[1, 128], [97, 256], [217, 384], [343, 512]]
+    assert out["window_sets"][0] == [[1, 128], [97, 256], [217, 384], [343, 512]]
+    for ws in out["window_sets"]:        # every set covers the bins with overlaps
+        assert ws[0][0] == 1 and ws[-1][1] == 512
+        assert all(ws[i][0] <= ws[i - 1][1] and ws[i][1] > ws[i - 1][1] for i in range(1, len(ws)))
+    assert len(out["window_sets"]) == (1 if burn_in == "temperature" else len(out["record"]) + 2)
     nrmse = np.sqrt(np.mean((ver - run) ** 2)) / np.mean(ver)
     assert nrmse < 0.01, nrmse
     if radial is not None:

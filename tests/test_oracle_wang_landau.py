@@ -363,3 +363,34 @@ def test_enter_window_redraws_like_the_reference():
     it_b, e_b = _py_enter_window(mod, cb, rb, conc, np.array([18, 18, 18]), lo, hi, sig2x2, 30000)
     assert it_a == it_b == -1 and e_a == e_b
     assert np.array_equal(ca, cb) and np.array_equal(ra.state_words(), rb.state_words())
+
+
+def test_sweeps_store_keeps_the_first_sampled_configuration_per_bin():
+    """config_per_bin (src/wang-landau.F90:605-610): a bin closes at its
+    first histogram tick, so the closed bins are exactly those with ticks,
+    each slot holds a configuration of that bin's energy, and a second call
+    leaves closed slots alone."""
+    rng = np.random.default_rng(3)
+    V = np.zeros((3, 3, 2))
+    for sh in range(2):
+        a = rng.uniform(-0.05, 0.05, (3, 3))
+        V[:, :, sh] = (np.triu(a) + np.triu(a, 1).T) / 13.6
+    mod = O.OracleModel("bcc", 4, 4, 4, V)
+    r = O.OracleRng(5)
+    cfg, _ = mod.initial_setup(r, np.array([0.0, 1 / 3, 1 / 3, 1 / 3]))
+    E = mod.total_energy(cfg)
+    bins = 40
+    edges = E - 0.2 + np.arange(bins + 1) * (0.4 / bins)
+    lng, hist = np.zeros(bins), np.zeros(bins)
+    store = dict(slots=np.zeros((bins,) + cfg.shape, dtype=np.int8), open=np.ones(bins, dtype=np.uint8))
+    _, E, _ = mod.wl_sweep(cfg, r, edges, lng, hist, E, bins, 1, bins, 3000, 1.0, 2, store=store)
+    closed = np.nonzero(store["open"] == 0)[0]
+    assert closed.size > 0 and np.array_equal(closed, np.nonzero(hist > 0)[0])
+    for b in closed:
+        assert O.wl_bin_index(mod.total_energy(store["slots"][b]), edges, bins) == b + 1
+        assert np.array_equal(np.bincount(store["slots"][b].ravel(), minlength=4),
+                              np.bincount(cfg.ravel(), minlength=4))
+    before = store["slots"].copy()
+    mod.wl_sweep(cfg, r, edges, lng, hist, E, bins, 1, bins, 3000, 1.0, 2, store=store)
+    assert np.array_equal(store["slots"][closed], before[closed])
+    assert np.array_equal(np.nonzero(store["open"] == 0)[0], np.nonzero(hist > 0)[0])
