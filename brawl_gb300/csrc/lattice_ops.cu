@@ -60,14 +60,29 @@ __global__ void site_energies_kernel(const EnergyJob* __restrict__ jobs, int n_j
   }
 }
 
-// energy = energy + e(site) over sites in order, then 0.5 * energy.
-__global__ void sum_sites_kernel(const EnergyJob* __restrict__ jobs, int n_jobs) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n_jobs) return;
+// energy = energy + e(site) over sites in order, then 0.5 * energy.  One
+// warp per chain: the warp loads 32 site energies at a time (the next 32
+// already in flight) and every lane runs the same ordered chain of adds on
+// them through shuffles, so the chain waits on the adds, not on the loads.
+constexpr int kSumWarps = 4;
+__global__ void __launch_bounds__(32 * kSumWarps) sum_sites_kernel(const EnergyJob* __restrict__ jobs,
+                                                                   int n_jobs) {
+  const int lane = threadIdx.x & 31;
+  const int c = blockIdx.x * kSumWarps + (threadIdx.x >> 5);
+  if (c >= n_jobs) return;  // the whole warp
   const EnergyJob& J = jobs[c];
+  const int n = J.g.n_sites;
+  const double* e = J.site_energy;
   double energy = 0.0;
-  for (int i = 0; i < J.g.n_sites; ++i) energy = __dadd_rn(energy, J.site_energy[i]);
-  *J.out = __dmul_rn(0.5, energy);
+  double v = lane < n ? e[lane] : 0.0;
+  for (int base = 0; base < n; base += 32) {
+    const int nxt = base + 32 + lane;
+    const double v_next = nxt < n ? e[nxt] : 0.0;
+    const int m = min(32, n - base);
+    for (int k = 0; k < m; ++k) energy = __dadd_rn(energy, __shfl_sync(kFull, v, k));
+    v = v_next;
+  }
+  if (lane == 0) *J.out = __dmul_rn(0.5, energy);
 }
 
 void launch_total_energy(const EnergyJob* d_jobs, int n_jobs, int64_t total_sites,
@@ -78,7 +93,7 @@ void launch_total_energy(const EnergyJob* d_jobs, int n_jobs, int64_t total_site
   BRAWL_CARVEOUT(site_energies_kernel);
   site_energies_kernel<<<(int)blocks, 256, 0, stream>>>(d_jobs, n_jobs, total_sites);
   BRAWL_CARVEOUT(sum_sites_kernel);
-  sum_sites_kernel<<<(n_jobs + 31) / 32, 32, 0, stream>>>(d_jobs, n_jobs);
+  sum_sites_kernel<<<(n_jobs + kSumWarps - 1) / kSumWarps, 32 * kSumWarps, 0, stream>>>(d_jobs, n_jobs);
 }
 
 __global__ void one_site_energy_kernel(const EnergyJob* __restrict__ job, int x, int y, int z,
