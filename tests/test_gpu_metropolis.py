@@ -472,3 +472,37 @@ def test_annealing_alro_matches_oracle():
     ref = reference_alro(mod, cfg.copy(), r, m)
     out = anneal.simulated_annealing(ch, m, 2, record_configs=False)
     assert np.array_equal(out["order_of_T"], ref)
+
+
+def test_largest_lattices_match_oracle():
+    """Maximum sizes in one batch: the batched workload's largest chain (bcc
+    L = 24, 27648 sites, 4 species, 6 shells: the shared-memory halo kernel
+    with every lane entry a neighbour) and an fcc L = 40 chain (256000
+    sites, 3 species, 3 shells), whose lattice exceeds shared memory and
+    stays in HBM; one sweep each, and each equals the oracle: accepts,
+    configuration, counters, energy and the stream's continuation."""
+    rng = np.random.default_rng(2424)
+    cases = [("bcc", 24, 4, 6, 600.0), ("fcc", 40, 3, 3, 900.0)]
+    chains, expect = [], []
+    for k, (lat, L, ns, nsh, T) in enumerate(cases):
+        V = random_V(rng, ns, nsh)
+        setup = B.Setup(lat, L, L, L, ns, nsh)
+        seed = 110179 + 11 * k
+        chains.append(dict(setup=setup, V=V, seed=seed, beta=1.0 / (T * B.K_B_IN_RY),
+                           species_concentrations=conc_vector(ns)))
+        trials = setup.n_atoms
+        expect.append((trials,) + _oracle_run(lat, (L, L, L), V, seed, T, trials, False, conc_vector(ns), None))
+    b = B.Batch(chains)
+    acc = b.metropolis(np.array([e[0] for e in expect]))
+    cnt = b.counters()
+    E = b.total_energy()
+    for k, (trials, mod, cfg, r, a, c, _) in enumerate(expect):
+        assert acc[k] == a, cases[k]
+        assert np.array_equal(b.config(k), cfg), cases[k]
+        row = dict(zip(B.COUNTER_NAMES, cnt[k]))
+        assert row["trials"] == c.trials and row["evaluated"] == c.evaluated
+        assert row["accepted"] == c.accepted and row["exp_tests"] == c.exp_tests
+        assert E[k] == mod.total_energy(cfg), cases[k]
+        cont = O.OracleRng(1)
+        cont.set_state_words(b.rng_state(k))
+        assert [cont.uniform() for _ in range(200)] == [r.uniform() for _ in range(200)]
