@@ -367,6 +367,9 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
     config_store (default: pre_sample) keeps config_per_bin on the device:
     pre-sampling then ends with merge_configs and load_window_config, and
     every ln f step with load_window_config, as the reference's do.
+    Pre-sampling is what makes every bin of every window stored; without it
+    a reload can draw a bin no walker has visited, which raises BrawlError
+    (the reference would load its zero-filled slot).
     optimise_windows (default: config_store) resizes the windows with
     mpi_window_optimise where wl.performance asks for it (0-3 after
     pre-sampling, 0-1 at every ln f step); it needs the store, which gives
