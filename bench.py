@@ -614,11 +614,23 @@ def main() -> int:
                            beta=1.0 / (float(wl["T"][r]) * K_B_IN_RY),
                            species_concentrations=wl["conc"]))
     batch = B.Batch(chains)
-    if args.speculation:
-        batch.set_speculation(args.speculation)
     sites = np.array([n_sites(int(L)) for L in wl["L"]], dtype=np.int64)
     trials = sites * args.sweeps_per_step
     trials_per_step = int(trials.sum())
+    if args.speculation:
+        batch.set_speculation(args.speculation)
+        cta_shape = {"trials_per_round": args.speculation, "picked_by": "--speculation"}
+    else:
+        # the CTA shape by measurement, before the warm-up and outside every
+        # timed region: one step's trials at each trials-per-round depth from
+        # the same state, which the library restores after each
+        try:
+            depth, ms = batch.autotune(trials, max_depth=4)
+            cta_shape = {"trials_per_round": int(depth), "picked_by": "autotune",
+                         "ms_per_depth": [round(float(x), 2) for x in ms]}
+        except Exception as exc:  # keep one warp per chain and say why
+            batch.set_speculation(1)
+            cta_shape = {"trials_per_round": 1, "picked_by": "default", "autotune_error": str(exc)[:200]}
 
     stream = torch.cuda.Stream()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
@@ -734,7 +746,7 @@ def main() -> int:
                        "sweeps_per_step": args.sweeps_per_step,
                        "trials_per_step": trials_per_step,
                        "l2": "flushed between steps (256 MiB write)",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}", "cta_shape": cta_shape},
             "e2e": {"value": e2e_value, "unit": "trials/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],

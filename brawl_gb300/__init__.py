@@ -148,6 +148,7 @@ def load(rebuild: bool = False):
         "brawl_batch_size": ([vp, vp], i),
         "brawl_batch_set_beta": ([vp, vp], i),
         "brawl_batch_set_speculation": ([vp, i], i),
+        "brawl_batch_autotune": ([vp, vp, i, vp, vp], i),
         "brawl_batch_metropolis_run": ([vp, vp, vp], i),
         "brawl_batch_metropolis_run_async": ([vp, vp, vp], i),
         "brawl_batch_sync": ([vp], i),
@@ -415,6 +416,16 @@ class Batch:
     def set_speculation(self, trials_per_round: int) -> None:
         """Trials per speculative round of the fcc/bcc kernel (1-4); speed only."""
         _check(load().brawl_batch_set_speculation(self._h, int(trials_per_round)))
+
+    def autotune(self, n_trials, max_depth: int = 4) -> tuple[int, np.ndarray]:
+        """Times n_trials of every chain at each trials-per-round depth
+        1..max_depth from the same state (restored after each) and keeps
+        the fastest; returns (depth, milliseconds per depth)."""
+        t = self._trials(n_trials)
+        ms = np.zeros(int(max_depth), dtype=np.float64)
+        chosen = C.c_int()
+        _check(load().brawl_batch_autotune(self._h, _ptr(t), int(max_depth), _ptr(ms), C.byref(chosen)))
+        return chosen.value, ms
 
     def _trials(self, n_trials) -> np.ndarray:
         return np.ascontiguousarray(np.broadcast_to(np.asarray(n_trials, dtype=np.int64), (self.n,)))

@@ -329,7 +329,8 @@ struct brawl_batch {
   std::vector<Model> models;
   std::vector<ChainJob> jobs;            // host images (pointers into the arena)
   std::vector<int> nbr_swap;
-  unsigned char* arena = nullptr;
+  unsigned char* arena = nullptr;        // every chain's mutable state and tables, one allocation
+  size_t arena_bytes = 0;
   ChainJob* d_jobs = nullptr;
   EnergyJob* d_ejobs = nullptr;
   AsroJob* d_ajob = nullptr;
@@ -614,8 +615,10 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
   if (object_stream(&b->stream) != cudaSuccess)
     return cleanup(fail(BRAWL_ECUDA, "stream create failed"));
   cudaError_t e = dalloc(&b->arena, total, b->stream);
+  b->arena_bytes = total;
   if (e != cudaSuccess) {
     b->arena = nullptr;
+    b->arena_bytes = 0;
     return cleanup(fail(BRAWL_ENOMEM, std::string("arena: ") + cudaGetErrorString(e)));
   }
   std::vector<unsigned char> h(total, 0);
@@ -726,6 +729,60 @@ int brawl_batch_set_speculation(brawl_batch* b, int trials_per_round) {
   if (!b || trials_per_round < 1 || trials_per_round > 4) return fail(BRAWL_EINVAL, "trials per round must be 1-4");
   b->spec_nc = trials_per_round;
   return BRAWL_OK;
+}
+
+// The CTA shape of the shared-memory chains, picked by measurement: every
+// depth of 1..max_depth trials per round (1: one warp per chain; d: the
+// d(d+1)/2-warp speculative rounds) runs the same trials from the same
+// state, timed with events on the batch's stream, and the arena (lattices,
+// streams, counters, status) is put back after each, so the results the
+// caller sees do not depend on the choice -- every depth is bit-exact.
+int brawl_batch_autotune(brawl_batch* b, const int64_t* n_trials, int max_depth, double* ms, int* chosen) {
+  if (!b || !n_trials || max_depth < 1 || max_depth > 4) return fail(BRAWL_EINVAL, "bad argument");
+  for (size_t c = 0; c < b->jobs.size(); ++c)
+    if (n_trials[c] < 0) return fail(BRAWL_EINVAL, "n_trials < 0");
+  cudaStream_t s = b->stream;
+  unsigned char* snap = nullptr;
+  if (dalloc(&snap, b->arena_bytes, s) != cudaSuccess) return fail(BRAWL_ENOMEM, "autotune snapshot");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const std::vector<unsigned long long> last = b->last_counters;
+  const int keep = b->spec_nc;
+  int rc = BRAWL_OK, best = keep;
+  float best_ms = 0.0f;
+  auto cuda = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && rc == BRAWL_OK) rc = fail(BRAWL_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return rc == BRAWL_OK;
+  };
+  if (cuda(cudaEventCreate(&e0), "event") && cuda(cudaEventCreate(&e1), "event") &&
+      cuda(cudaMemcpyAsync(snap, b->arena, b->arena_bytes, cudaMemcpyDeviceToDevice, s), "snapshot")) {
+    for (int d = 1; d <= max_depth && rc == BRAWL_OK; ++d) {
+      b->spec_nc = d;
+      if (!cuda(cudaEventRecord(e0, s), "event")) break;
+      const int r = run_metropolis(b, n_trials, nullptr, false, s, false);
+      if (r != BRAWL_OK) {
+        rc = r;
+        break;
+      }
+      float t = 0.0f;
+      if (!cuda(cudaEventRecord(e1, s), "event") || !cuda(cudaEventSynchronize(e1), "timed run") ||
+          !cuda(cudaEventElapsedTime(&t, e0, e1), "event"))
+        break;
+      if (!cuda(cudaMemcpyAsync(b->arena, snap, b->arena_bytes, cudaMemcpyDeviceToDevice, s), "restore")) break;
+      b->last_counters = last;
+      if (ms) ms[d - 1] = (double)t;
+      if (d == 1 || t < best_ms) {
+        best_ms = t;
+        best = d;
+      }
+    }
+    cuda(cudaStreamSynchronize(s), "restore");
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  dfree(snap, s);
+  b->spec_nc = rc == BRAWL_OK ? best : keep;
+  if (chosen) *chosen = b->spec_nc;
+  return rc;
 }
 
 int brawl_batch_set_beta(brawl_batch* b, const double* beta) {

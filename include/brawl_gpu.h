@@ -177,6 +177,13 @@ int brawl_batch_set_beta(brawl_batch *batch, const double *beta);
 /* Trials per speculative round of the fcc/bcc Metropolis kernel (1-4, 1 =
  * one trial at a time, the default).  Speed only: the trajectory is the same. */
 int brawl_batch_set_speculation(brawl_batch *batch, int trials_per_round);
+/* Picks the trials per round by measurement: n_trials[c] trials of every
+ * chain are timed at each depth 1..max_depth (<= 4) from the same state,
+ * which is restored after each run, so the batch's chains, streams and
+ * counters are as before the call.  ms (max_depth entries, may be NULL)
+ * gets each depth's time; chosen (may be NULL) the depth kept. */
+int brawl_batch_autotune(brawl_batch *batch, const int64_t *n_trials, int max_depth, double *ms,
+                         int *chosen);
 /* n_trials[c] Metropolis trials on every chain c, all chains in one launch.
  * accepted (may be NULL) receives each chain's accept sum for this call. */
 int brawl_batch_metropolis_run(brawl_batch *batch, const int64_t *n_trials, int64_t *accepted);

@@ -506,3 +506,35 @@ def test_largest_lattices_match_oracle():
         cont = O.OracleRng(1)
         cont.set_state_words(b.rng_state(k))
         assert [cont.uniform() for _ in range(200)] == [r.uniform() for _ in range(200)]
+
+
+def test_autotune_keeps_the_state_and_the_trajectories():
+    """brawl_batch_autotune times every trials-per-round depth from one
+    state and restores it after each: configurations, streams and counters
+    are unchanged by the call, and the runs after it still equal the
+    oracle's whatever depth it kept."""
+    rng = np.random.default_rng(65)
+    V = random_V(rng, 4, 6)
+    Ls = [4, 6, 3, 5]
+    chains, expect = [], []
+    for r, L in enumerate(Ls):
+        T = 200.0 * 5.0 ** (r / (len(Ls) - 1))
+        setup = B.Setup("bcc", L, L, L, 4, 6)
+        seed = 110179 + 11 * r
+        chains.append(dict(setup=setup, V=V, seed=seed, beta=1.0 / (T * B.K_B_IN_RY),
+                           species_concentrations=conc_vector(4)))
+        trials = 6 * setup.n_atoms
+        mod, cfg, r_, acc, c, _ = _oracle_run("bcc", (L, L, L), V, seed, T, trials, False, conc_vector(4), None)
+        expect.append((trials, cfg, acc, c))
+    b = B.Batch(chains)
+    before = ([b.config(k) for k in range(len(Ls))], [b.rng_state(k) for k in range(len(Ls))], b.counters())
+    depth, ms = b.autotune(np.array([3 * e[0] for e in expect]))
+    assert 1 <= depth <= 4 and ms.shape == (4,) and (ms > 0).all()
+    assert ms[depth - 1] == ms.min()
+    for k in range(len(Ls)):
+        assert np.array_equal(b.config(k), before[0][k])
+        assert np.array_equal(b.rng_state(k), before[1][k])
+    assert np.array_equal(b.counters(), before[2])
+    acc = b.metropolis(np.array([e[0] for e in expect]))
+    for k, (t, cfg, a, c) in enumerate(expect):
+        assert acc[k] == a and np.array_equal(b.config(k), cfg), Ls[k]
