@@ -307,3 +307,26 @@ def test_merge_and_load_draw_like_the_reference():
         s, e = windows[k // 2]
         assert bins[k] == s + int(u.random() * (e - s + 1)) and s <= bins[k] <= e
     assert W.loads == [(k, int(bins[k])) for k in range(4)]
+
+
+def test_window_optimise_properties_on_random_inputs():
+    """Whatever the steps and previous fractions: the windows tile 1..bins
+    without gaps, each keeps at least max(INT(0.02 bins), 2) bins, the new
+    fractions sum to 1, and create_overlap of the result gives every window
+    but the first an overlap with the one below."""
+    rng = np.random.default_rng(17)
+    for case in range(300):
+        nwin = int(rng.integers(2, 9))
+        bins = int(rng.integers(8 * nwin, 2000))
+        iv = WLD.divide_range(bins, nwin)
+        steps = rng.uniform(1e3, 1e7, nwin) * (rng.random(nwin) < 0.9) + 1.0
+        prev = rng.dirichlet(np.ones(nwin))
+        it = int(rng.integers(0, 6))
+        new, frac = WLD.window_optimise(it, iv, steps, prev, bins)
+        assert new[0][0] == 1 and new[-1][1] == bins, case
+        assert all(new[i][0] == new[i - 1][1] + 1 for i in range(1, nwin)), case
+        sizes = [e - s + 1 for s, e in new]
+        assert min(sizes) >= max(int(0.02 * bins), 2) and sum(sizes) == bins, case
+        assert abs(float(frac.sum()) - 1.0) < 1e-12, case
+        idx = WLD.create_overlap(new, 0.25)
+        assert all(idx[i][0] <= idx[i - 1][1] for i in range(1, nwin)), case
