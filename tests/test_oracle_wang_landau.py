@@ -167,11 +167,12 @@ BCC_NBRS = [(1, 1, 1), (1, 1, -1), (1, -1, 1), (1, -1, -1), (-1, 1, 1), (-1, 1, 
 
 
 def _py_sweeps_nbr(mod, n, cfg, rng, edges, lng, hist, e, bins, start, end, n_trials, f, period,
-                   nbr=True, radial=None):
+                   nbr=True, radial=None, store=None):
     """sweeps (src/wang-landau.F90:539-632) with select_sites_nbr (:1527-1532)
-    or select_sites, and the radial-density samples (:566-586), written out
-    from the reference, on a bcc lattice n x n x n; the site draw, the pair
-    energies and radial_densities come from the oracle."""
+    or select_sites, the radial-density samples (:566-586) and the
+    configuration store (:605-622), written out from the reference, on a bcc
+    lattice n x n x n; the site draw, the pair energies and radial_densities
+    come from the oracle."""
     W = 2 * n
     n_atoms = 2 * n ** 3
     acc = 0
@@ -206,6 +207,9 @@ def _py_sweeps_nbr(mod, n, cfg, rng, edges, lng, hist, e, bins, start, end, n_tr
             jb = ib
         if period > 0 and i % period == 0:
             hist[jb - start] += 1.0
+            if store is not None and store["open"][jb - 1]:
+                store["open"][jb - 1] = 0
+                store["slots"][jb - 1] = cfg
         lng[jb - 1] += f
     return acc, e
 
@@ -394,3 +398,37 @@ def test_sweeps_store_keeps_the_first_sampled_configuration_per_bin():
     mod.wl_sweep(cfg, r, edges, lng, hist, E, bins, 1, bins, 3000, 1.0, 2, store=store)
     assert np.array_equal(store["slots"][closed], before[closed])
     assert np.array_equal(np.nonzero(store["open"] == 0)[0], np.nonzero(hist > 0)[0])
+
+
+@pytest.mark.parametrize("nbr", [False, True])
+def test_sweeps_store_matches_python_restatement(nbr):
+    """The oracle's configuration store against the restatement above, over
+    two calls (the second one finds bins closed by the first)."""
+    rng = np.random.default_rng(81)
+    ns, nsh, n = 3, 2, 3
+    V = np.zeros((ns, ns, nsh))
+    for sh in range(nsh):
+        a = rng.uniform(-0.05, 0.05, size=(ns, ns))
+        V[:, :, sh] = (np.triu(a) + np.triu(a, 1).T) / 13.605693122
+    mod = O.OracleModel("bcc", n, n, n, V)
+    cfg, _ = mod.initial_setup(O.OracleRng(5), np.array([0.0, 1 / 3, 1 / 3, 1 / 3]), np.array([18, 18, 18]))
+    e0 = mod.total_energy(cfg)
+    bins = 60
+    edges = (e0 - 0.02) + np.arange(bins + 1) * (0.04 / bins)
+    start, end, period = 10, 50, 3
+    cfg_a, cfg_b = cfg.copy(), cfg.copy()
+    lng_a, lng_b = np.zeros(bins), np.zeros(bins)
+    hist_a, hist_b = np.zeros(end - start + 1), np.zeros(end - start + 1)
+    st_a = dict(slots=np.zeros((bins,) + cfg.shape, dtype=np.int8), open=np.ones(bins, dtype=np.uint8))
+    st_b = dict(slots=np.zeros((bins,) + cfg.shape, dtype=np.int8), open=np.ones(bins, dtype=np.uint8))
+    ra, rb = O.OracleRng(99), O.OracleRng(99)
+    e_a = e_b = e0
+    for _ in range(2):
+        acc_a, e_a, _ = mod.wl_sweep(cfg_a, ra, edges, lng_a, hist_a, e_a, bins, start, end, 1500, 0.5, period,
+                                     nbr_swap=nbr, store=st_a)
+        acc_b, e_b = _py_sweeps_nbr(mod, n, cfg_b, rb, edges, lng_b, hist_b, e_b, bins, start, end, 1500, 0.5,
+                                    period, nbr=nbr, store=st_b)
+        assert acc_a == acc_b and e_a == e_b
+    assert np.array_equal(st_a["open"], st_b["open"]) and (st_a["open"] == 0).any()
+    assert np.array_equal(st_a["slots"], st_b["slots"])
+    assert np.array_equal(cfg_a, cfg_b) and np.array_equal(hist_a, hist_b)
