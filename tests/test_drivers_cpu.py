@@ -330,3 +330,145 @@ def test_window_optimise_properties_on_random_inputs():
         assert abs(float(frac.sum()) - 1.0) < 1e-12, case
         idx = WLD.create_overlap(new, 0.25)
         assert all(idx[i][0] <= idx[i - 1][1] for i in range(1, nwin)), case
+
+
+class FakeWalkers:
+    """WangLandauWalkers' interface with scripted answers: every third
+    sweeps() call makes every walker flat, histograms are full, and the
+    calls are recorded."""
+
+    def __init__(self, walkers, edges):
+        self.walkers = [dict(w) for w in walkers]
+        self.n, self.bins = len(walkers), len(edges) - 1
+        self.log, self.calls, self.enabled = [], 0, False
+
+    def store_enable(self):
+        self.enabled = True
+        self.log.append("store_enable")
+
+    def enter_windows(self, *a, **k):
+        self.log.append("enter_windows")
+        return np.arange(self.n, dtype=np.int64) + 10
+
+    def set_config(self, k, cfg):
+        pass
+
+    def config(self, k):
+        return np.zeros((2, 2, 2), dtype=np.int8)
+
+    def sweeps(self, trials, f, period):
+        self.calls += 1
+        self.log.append("sweeps")
+        return np.zeros(self.n, dtype=np.int64)
+
+    def replica_exchange(self):
+        return 0, None, None
+
+    def flatness(self):
+        return np.full(self.n, 1.0 if self.calls % 3 == 0 else 0.5)
+
+    def hist(self, k):
+        w = self.walkers[k]
+        return np.full(w["end_idx"] - w["start_idx"] + 1, 5000.0)
+
+    def set_hist(self, k, h):
+        pass
+
+    def reset_hist(self):
+        self.log.append("reset_hist")
+
+    def average(self):
+        pass
+
+    def dos_combine(self):
+        self.log.append("dos_combine")
+        return np.zeros(self.bins)
+
+    def set_windows(self, s, e):
+        self.log.append(("set_windows", tuple(s), tuple(e)))
+        first = {}
+        for w in self.walkers:
+            first.setdefault(w["window"], len(first))
+        for w in self.walkers:
+            j = first[w["window"]]
+            w["start_idx"], w["end_idx"] = int(s[j]), int(e[j])
+
+    def store_flags(self):
+        return np.zeros((self.n, self.bins), dtype=bool)
+
+    def store_merge(self, pick):
+        self.log.append("merge")
+
+    def store_load(self, k, b):
+        w = self.walkers[k]
+        assert w["start_idx"] <= b <= w["end_idx"]
+        self.log.append(("load", k))
+
+    def close(self):
+        pass
+
+
+class FakeBatch:
+    def __init__(self, chains):
+        pass
+
+    def config(self, k):
+        return np.zeros((2, 2, 2), dtype=np.int8)
+
+    def close(self):
+        pass
+
+
+def _run_driver(monkeypatch, **kw):
+    made = []
+
+    def make(walkers, edges):
+        made.append(FakeWalkers(walkers, edges))
+        return made[-1]
+
+    monkeypatch.setattr(WLD, "WangLandauWalkers", make)
+    monkeypatch.setattr(WLD, "Batch", FakeBatch)
+    wl = I.WLParams(mc_sweeps=1, bins=200, num_windows=4, bin_overlap=0.25, tolerance=0.01,
+                    flatness=0.8, wl_f=0.05, energy_min=-50.0, energy_max=0.0)
+    for k, v in kw.pop("wl", {}).items():
+        setattr(wl, k, v)
+    setup = B.Setup("bcc", 2, 2, 2, 2, 1)
+    out = WLD.wang_landau(setup, np.zeros((2, 2, 1)), np.array([0.0, 0.5, 0.5]), wl, walkers_per_window=2,
+                          burn_in="reference", **kw)
+    return made[0], out
+
+
+def test_wang_landau_driver_sequence_with_store_and_windows(monkeypatch):
+    """pre-sampling -> mpi_window_optimise(0) -> merge_configs ->
+    load_window_config -> histograms reset; then at every ln f step new
+    windows and a reload of every walker (performance 0)."""
+    W, out = _run_driver(monkeypatch, pre_sample=True)
+    log = [x if isinstance(x, str) else x[0] for x in W.log]
+    assert log[0] == "store_enable" and W.enabled
+    first_sweep = log.index("sweeps")
+    assert log.index("store_enable") < first_sweep
+    # the end of pre-sampling
+    i = log.index("set_windows")
+    assert log[i + 1] == "merge" and log[i + 2:i + 2 + W.n] == ["load"] * W.n and log[i + 2 + W.n] == "reset_hist"
+    halvings = len(out["record"])
+    assert halvings == 3                       # 0.05 -> 0.00625 below 0.01
+    assert log.count("set_windows") == 1 + halvings
+    assert log.count("load") == W.n * (1 + halvings) and log.count("merge") == 1
+    assert len(out["window_sets"]) == 2 + halvings
+    for ws in out["window_sets"]:
+        assert ws[0][0] == 1 and ws[-1][1] == 200
+
+
+def test_wang_landau_driver_performance_gates_the_optimiser(monkeypatch):
+    # performance 2: the pre-sampling optimisation only (mpi_window_optimise
+    # runs for 0-3; the main loop calls it for 0-1)
+    W, out = _run_driver(monkeypatch, pre_sample=True, wl={"performance": 2})
+    assert [x[0] for x in W.log if not isinstance(x, str)].count("set_windows") == 1
+    assert len(out["window_sets"]) == 2
+    # no optimisation asked: the windows stay, the reloads still happen
+    W, out = _run_driver(monkeypatch, pre_sample=True, optimise_windows=False)
+    assert not any(not isinstance(x, str) and x[0] == "set_windows" for x in W.log)
+    assert len(out["window_sets"]) == 1 and sum(1 for x in W.log if x[0] == "load") > 0
+    # no pre-sampling: no store, no reloads
+    W, out = _run_driver(monkeypatch, pre_sample=False)
+    assert not W.enabled and not any(x[0] == "load" for x in W.log if not isinstance(x, str))
