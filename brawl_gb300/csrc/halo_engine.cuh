@@ -109,6 +109,123 @@ __device__ inline void ring_writeback(const uint32_t* mt, const uint32_t* tbuf, 
 }
 
 // ---------------------------------------------------------------------------
+// Site tables.  The site an fcc/bcc proposal draws from the three words at
+// ring positions (p, p+1, p+2) does not depend on the lattice, so it is
+// decoded for every position when the words are generated:
+//   ptab[p] = padded index | parity << 30   (parity: bcc z & 1, fcc x & 1)
+//   ctab[p] = x | y << 10 | z << 20          (doubled-grid coordinates)
+// (entries kRing + k mirror entries k, like the words' mirror).  A trial then
+// reads its sites with shared loads instead of decoding six words.  Entry p
+// is written when the block holding word p + 2 is generated, so the words a
+// trial may read (ring_ensure's n >= 6) always have their entries.
+// ---------------------------------------------------------------------------
+constexpr int32_t kPadMask = (1 << 30) - 1;
+
+struct SiteDraw {
+  uint32_t z2, n1, n2, x2;  // 2 n3, n1, n2, 2 n1
+  int32_t origin, SZ, SY;
+  int32_t bcc;
+};
+
+__device__ __forceinline__ SiteDraw make_site_draw(const Geom& g, const HaloGeom& H) {
+  SiteDraw S;
+  S.z2 = 2u * (uint32_t)g.n3;
+  S.n1 = (uint32_t)g.n1;
+  S.n2 = (uint32_t)g.n2;
+  S.x2 = 2u * (uint32_t)g.n1;
+  S.origin = H.origin;
+  S.SZ = H.SZ;
+  S.SY = H.SY;
+  S.bcc = g.lattice == kBcc;
+  return S;
+}
+
+// The site draw_site_halo gives for words (w0, w1, w2): its ptab and ctab
+// entries.
+__device__ __forceinline__ void site_entries(const SiteDraw& S, uint32_t w0, uint32_t w1,
+                                             uint32_t w2, int32_t& pe, int32_t& ce) {
+  const int z = (int)umulhi32(w0, S.z2);
+  int x, y, Yc, Xc, par;
+  if (S.bcc) {
+    const int p = z & 1;
+    Xc = (int)umulhi32(w1, S.n1);
+    Yc = (int)umulhi32(w2, S.n2);
+    x = 2 * Xc + p;
+    y = 2 * Yc + p;
+    par = p;
+  } else {
+    x = (int)umulhi32(w1, S.x2);
+    y = 2 * (int)umulhi32(w2, S.n2) + ((x + z) & 1);
+    Yc = y;
+    Xc = x >> 1;
+    par = x & 1;
+  }
+  pe = (S.origin + z * S.SZ + Yc * S.SY + Xc) | (par << 30);
+  ce = x | (y << 10) | (z << 20);
+}
+
+__device__ __forceinline__ void site_coords(int32_t ce, int& x, int& y, int& z) {
+  x = ce & 1023;
+  y = (ce >> 10) & 1023;
+  z = ce >> 20;
+}
+
+// Entries for positions [lo, hi) (hi <= kRing; words up to hi + 1 exist,
+// through the mirror), then the tables' mirrors when position 0 was among
+// them.
+__device__ __forceinline__ void site_table_fill(const SiteDraw& S, const uint32_t* tbuf,
+                                                int32_t* ptab, int32_t* ctab, int lo, int hi,
+                                                int lane) {
+  for (int p = lo + lane; p < hi; p += 32) {
+    int32_t pe, ce;
+    site_entries(S, tbuf[p], tbuf[p + 1], tbuf[p + 2], pe, ce);
+    ptab[p] = pe;
+    ctab[p] = ce;
+  }
+  __syncwarp();
+  if (lo == 0 && lane < kRingMirror) {
+    ptab[kRing + lane] = ptab[lane];
+    ctab[kRing + lane] = ctab[lane];
+  }
+  __syncwarp();
+}
+
+// ring_init plus the entries of every position whose three words are in
+// the initial block.
+__device__ __forceinline__ void ring_init_sites(const uint32_t* mt, uint32_t* tbuf, int32_t* ptab,
+                                                int32_t* ctab, const SiteDraw& S, int pos0,
+                                                int lane, Ring& R) {
+  ring_init(mt, tbuf, pos0, lane, R);
+  site_table_fill(S, tbuf, ptab, ctab, 0, kMTN - 2, lane);
+}
+
+// A new block into half h with its entries: the two positions before the
+// block (their last words are its first) and the block's first 622.  Out of
+// line: it runs once per 624 words, and the trial loop stays small.
+static __device__ __noinline__ void ring_generate_sites(uint32_t* mt, uint32_t* tbuf,
+                                                        int32_t* ptab, int32_t* ctab,
+                                                        const SiteDraw S, int h, int lane) {
+  ring_generate(mt, tbuf, h, lane);
+  if (h == 0) {
+    site_table_fill(S, tbuf, ptab, ctab, kRing - 2, kRing, lane);
+    site_table_fill(S, tbuf, ptab, ctab, 0, kMTN - 2, lane);
+  } else {
+    site_table_fill(S, tbuf, ptab, ctab, kMTN - 2, kRing - 2, lane);
+  }
+}
+
+// ring_ensure, keeping the site tables current.
+__device__ __forceinline__ void ring_ensure_sites(uint32_t* mt, uint32_t* tbuf, int32_t* ptab,
+                                                  int32_t* ctab, const SiteDraw& S, Ring& R,
+                                                  int n, int lane) {
+  if (R.avail < n) {
+    ring_generate_sites(mt, tbuf, ptab, ctab, S, R.next_half, lane);
+    R.avail += kMTN;
+    R.next_half ^= 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // halo lattice
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int halo_index(const HaloGeom& H, int Z, int Yp, int Xp) {
@@ -140,35 +257,27 @@ __device__ inline void halo_store(const Geom& g, const HaloGeom& H, const int8_t
   }
 }
 
-// Writes species s at canonical (Z, Y', X') and at its images; lanes 8k..8k+7
-// handle site k (k = 0, 1) through the 8 combinations of images per axis.
-__device__ __forceinline__ void halo_write_pair(const HaloGeom& H, int8_t* lat_p, int lane,
-                                                int Za, int Ya, int Xa, int sa_new, int Zb,
-                                                int Yb, int Xb, int sb_new) {
-  if (lane < 16) {
-    const bool b = lane >= 8;
-    const int combo = lane & 7;
-    int Z = b ? Zb : Za, Y = b ? Yb : Ya, X = b ? Xb : Xa;
-    const int s = b ? sb_new : sa_new;
-    bool ok = true;
-    if (combo & 1) {
-      if (X < H.hx) X += H.NX;
-      else if (X >= H.NX - H.hx) X -= H.NX;
-      else ok = false;
-    }
-    if (combo & 2) {
-      if (Y < H.hy) Y += H.NY;
-      else if (Y >= H.NY - H.hy) Y -= H.NY;
-      else ok = false;
-    }
-    if (combo & 4) {
-      if (Z < H.hz) Z += H.NZ;
-      else if (Z >= H.NZ - H.hz) Z -= H.NZ;
-      else ok = false;
-    }
-    if (ok) lat_p[halo_index(H, Z, Y, X)] = (int8_t)s;
-  }
-  __syncwarp();
+// The padded cell that lane `lane` writes when the pair is swapped, or -1:
+// lanes 8k..8k+7 take site k's canonical cell and its images (one
+// combination of image axes each; at most 8 copies).  Lanes take different
+// combinations, so every choice is a select, not a branch.
+__device__ __forceinline__ int halo_image_shift(int c, int h, int N) {
+  // the image shift of coordinate c on an axis with halo h, 0 when none
+  return c < h ? N : (c >= N - h ? -N : 0);
+}
+
+__device__ __forceinline__ int halo_image_index(const HaloGeom& H, int lane, int Za, int Ya,
+                                                int Xa, int Zb, int Yb, int Xb) {
+  const bool b = lane >= 8;
+  const int combo = lane & 7;
+  const int Z = b ? Zb : Za, Y = b ? Yb : Ya, X = b ? Xb : Xa;
+  const int sx = halo_image_shift(X, H.hx, H.NX);
+  const int sy = halo_image_shift(Y, H.hy, H.NY);
+  const int sz = halo_image_shift(Z, H.hz, H.NZ);
+  const bool ux = combo & 1, uy = combo & 2, uz = combo & 4;
+  const bool ok = lane < 16 && (!ux || sx != 0) && (!uy || sy != 0) && (!uz || sz != 0);
+  const int idx = halo_index(H, Z + (uz ? sz : 0), Y + (uy ? sy : 0), X + (ux ? sx : 0));
+  return ok ? idx : -1;
 }
 
 // draw_site for fcc and bcc, also giving the site's compact (Y', X') =
@@ -205,6 +314,18 @@ __device__ __forceinline__ bool pair_near(const Geom& g, const HaloGeom& H, int 
   dx = dx > g.n1 ? dx - W1 : (dx < -g.n1 ? dx + W1 : dx);
   dy = dy > g.n2 ? dy - W2 : (dy < -g.n2 ? dy + W2 : dy);
   return abs(dx) <= H.dmx && abs(dy) <= H.dmy;
+}
+
+// pair_near without early exits (every lane evaluates all three axes, so
+// it compiles to selects and can be issued ahead of the species test).
+__device__ __forceinline__ bool pair_near_flat(const Geom& g, const HaloGeom& H, int ax, int ay,
+                                               int az, int bx, int by, int bz) {
+  int dz = bz - az, dx = bx - ax, dy = by - ay;
+  const int W1 = 2 * g.n1, W2 = 2 * g.n2, W3 = 2 * g.n3;
+  dz = dz > g.n3 ? dz - W3 : (dz < -g.n3 ? dz + W3 : dz);
+  dx = dx > g.n1 ? dx - W1 : (dx < -g.n1 ? dx + W1 : dx);
+  dy = dy > g.n2 ? dy - W2 : (dy < -g.n2 ? dy + W2 : dy);
+  return (abs(dz) <= H.dmz) & (abs(dx) <= H.dmx) & (abs(dy) <= H.dmy);
 }
 
 // Per-lane entry plan of the halo tier: for entry j of this lane's site, the

@@ -92,7 +92,7 @@ __device__ inline void build_axis_tables(const Geom& g, int32_t* tabs, const uin
 
 // Shared-memory layout of a chain staged with a halo (halo_engine.cuh).
 struct HaloLayout {
-  uint32_t mt, tbuf, V, ents, sstart, I, lat, total;
+  uint32_t mt, tbuf, ptab, ctab, V, ents, sstart, I, lat, total;
   int32_t F_off, D_off;
 };
 
@@ -105,7 +105,9 @@ __host__ __device__ inline HaloLayout halo_layout(const Geom& g, const HaloGeom&
   const uint32_t nD = nsp * nsp * (uint32_t)g.nsh * nsp;
   L.mt = 0;
   L.tbuf = align_up(kMTN * 4, 16);
-  L.V = align_up(L.tbuf + kTbufWords * 4, 16);
+  L.ptab = align_up(L.tbuf + kTbufWords * 4, 16);  // the site tables, one int32 per word each
+  L.ctab = L.ptab + kTbufWords * 4;
+  L.V = align_up(L.ctab + kTbufWords * 4, 16);
   L.ents = L.V + (uint32_t)(g.ns * g.ns * g.nsh) * 8;
   L.sstart = L.ents + (uint32_t)g.z * 4;
   L.I = align_up(L.sstart + (uint32_t)(g.nsh + 1) * 2, 16);
@@ -163,6 +165,25 @@ __device__ inline double site_energy_ref(const Geom& g, const int8_t* lat, const
     total = sh == 0 ? e : __dadd_rn(total, e);
   }
   return total;
+}
+
+// total_energy's ordered sum (src/bw_hamiltonian.f90:67-79): energy =
+// energy + e(site) over the sites in order, then 0.5 * energy, for one warp.
+// The warp loads 32 site energies at a time (the next 32 already in flight)
+// and every lane runs the same ordered chain of adds on them through
+// shuffles, so the chain waits on the adds, not on the loads.  Every lane
+// returns the result.
+__device__ inline double ordered_half_sum_warp(const double* __restrict__ e, int n, int lane) {
+  double energy = 0.0;
+  double v = lane < n ? e[lane] : 0.0;
+  for (int base = 0; base < n; base += 32) {
+    const int nxt = base + 32 + lane;
+    const double v_next = nxt < n ? e[nxt] : 0.0;
+    const int m = min(32, n - base);
+    for (int k = 0; k < m; ++k) energy = __dadd_rn(energy, __shfl_sync(kFull, v, k));
+    v = v_next;
+  }
+  return __dmul_rn(0.5, energy);
 }
 
 struct InitJob {

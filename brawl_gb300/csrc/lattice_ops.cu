@@ -60,10 +60,8 @@ __global__ void site_energies_kernel(const EnergyJob* __restrict__ jobs, int n_j
   }
 }
 
-// energy = energy + e(site) over sites in order, then 0.5 * energy.  One
-// warp per chain: the warp loads 32 site energies at a time (the next 32
-// already in flight) and every lane runs the same ordered chain of adds on
-// them through shuffles, so the chain waits on the adds, not on the loads.
+// energy = energy + e(site) over sites in order, then 0.5 * energy; one
+// warp per chain (ordered_half_sum_warp).
 constexpr int kSumWarps = 4;
 __global__ void __launch_bounds__(32 * kSumWarps) sum_sites_kernel(const EnergyJob* __restrict__ jobs,
                                                                    int n_jobs) {
@@ -71,18 +69,8 @@ __global__ void __launch_bounds__(32 * kSumWarps) sum_sites_kernel(const EnergyJ
   const int c = blockIdx.x * kSumWarps + (threadIdx.x >> 5);
   if (c >= n_jobs) return;  // the whole warp
   const EnergyJob& J = jobs[c];
-  const int n = J.g.n_sites;
-  const double* e = J.site_energy;
-  double energy = 0.0;
-  double v = lane < n ? e[lane] : 0.0;
-  for (int base = 0; base < n; base += 32) {
-    const int nxt = base + 32 + lane;
-    const double v_next = nxt < n ? e[nxt] : 0.0;
-    const int m = min(32, n - base);
-    for (int k = 0; k < m; ++k) energy = __dadd_rn(energy, __shfl_sync(kFull, v, k));
-    v = v_next;
-  }
-  if (lane == 0) *J.out = __dmul_rn(0.5, energy);
+  const double energy = ordered_half_sum_warp(J.site_energy, J.g.n_sites, lane);
+  if (lane == 0) *J.out = energy;
 }
 
 void launch_total_energy(const EnergyJob* d_jobs, int n_jobs, int64_t total_sites,

@@ -3,6 +3,8 @@
 // kernel for every lattice that fits.  One warp (CTA) per chain; trials in
 // the reference's order (monte_carlo_step_lattice / _nbr,
 // src/metropolis.F90:751-891) on the chain's own mt19937ar stream.
+#include <climits>
+
 #include "halo_engine.cuh"
 #include "kernels.cuh"
 
@@ -68,10 +70,41 @@ __device__ __noinline__ int halo_exact_decision(const ChainJob* __restrict__ Jg,
   return acc | 2 | (st.fp64 ? 4 : 0) | (st.cr ? 8 : 0);
 }
 
+// Log-domain acceptance thresholds: the uphill decision as two integer
+// compares of the fixed-point energy change against bounds taken from the
+// acceptance word (no exponential of the change).  The reference accepts an uphill move iff u < exp(-beta dE_ref)
+// (src/metropolis.F90:802), i.e. iff t > beta dE_ref log2(e) with
+// t = -log2(u) = 32 - log2(w) for u = w 2^-32.  With k = beta 2^-S log2(e)
+// and the fixed-point dE within band quanta of dE_ref 2^S, the move is
+// certainly accepted when dE < (t - e)/k - band and certainly rejected when
+// dE > (t + e)/k + band, where e = 1e-4 bounds the error of t as computed
+// here (float conversion of w, lg2.approx, the subtraction: together below
+// 2e-5 on [0, 32]) with room to spare.  The float products carry a further
+// relative 1e-6 and the thresholds are rounded towards the undecided side.
+// Between the two, and for w = 0, the exact tier decides.
+struct AcceptThresholds {
+  int acc_below;  // dE < acc_below: accepted
+  int rej_above;  // dE > rej_above: rejected
+};
+
+__device__ __forceinline__ AcceptThresholds accept_thresholds(uint32_t w, float inv_k, float band_f) {
+  AcceptThresholds T;
+  float lw;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(lw) : "f"(__uint2float_rn(w)));
+  const float t = 32.0f - lw;
+  const float a = __fmul_rn(__fmul_rn(t - 1e-4f, inv_k), 1.0f - 1e-6f) - band_f - 1.0f;
+  const float r = __fmul_rn(__fmul_rn(t + 1e-4f, inv_k), 1.0f + 1e-6f) + band_f + 1.0f;
+  // fixed-point changes stay within +-2^30: clamp before converting
+  T.acc_below = w == 0u ? INT_MIN : __float2int_rd(fminf(a, 1073741824.0f));
+  T.rej_above = w == 0u ? INT_MAX : __float2int_ru(fminf(r, 2147483520.0f));
+  return T;
+}
+
 template <int NJ, bool FULL>
 __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __restrict__ jobs) {
   extern __shared__ __align__(16) unsigned char smem[];
   extern __shared__ uint32_t s_u32[];
+  extern __shared__ int32_t s_i32[];
   extern __shared__ int8_t s_i8[];
   const ChainJob* Jg = jobs + blockIdx.x;
   if (Jg->status && *Jg->status != 0) return;  // the chain's input was flagged: no trial runs
@@ -83,6 +116,8 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   const HaloLayout L = halo_layout(g, H);
   uint32_t* mt = reinterpret_cast<uint32_t*>(smem + L.mt);
   uint32_t* tbuf = reinterpret_cast<uint32_t*>(smem + L.tbuf);
+  int32_t* ptab = reinterpret_cast<int32_t*>(smem + L.ptab);
+  int32_t* ctab = reinterpret_cast<int32_t*>(smem + L.ctab);
   double* V = reinterpret_cast<double*>(smem + L.V);
   uint32_t* ents = reinterpret_cast<uint32_t*>(smem + L.ents);
   int16_t* sstart = reinterpret_cast<int16_t*>(smem + L.sstart);
@@ -100,14 +135,16 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   for (int i = lane; i <= g.nsh; i += 32) sstart[i] = Jg->shell_start[i];
   __syncwarp();
   halo_fill(g, H, Jg->lat, lat, lane);
+  const SiteDraw S = make_site_draw(g, H);
   Ring R;
-  ring_init(mt, tbuf, (int)rng[kMTN], lane, R);
+  ring_init_sites(mt, tbuf, ptab, ctab, S, (int)rng[kMTN], lane, R);
   HaloPlan<NJ> P;
   make_halo_plan<NJ>(g, H, ents, lane, P);
   __syncwarp();
 
   const int lat_off = (int)L.lat;
   const int tb = (int)(L.tbuf / 4);
+  const int pt = (int)(L.ptab / 4), ct = (int)(L.ctab / 4);
   const int I_off = (int)(L.I / 4);
   const int D_abs = I_off + L.D_off;
   const HaloLat hl = {g.sz, g.sy, H.origin, H.SZ, H.SY, lat_off};
@@ -115,10 +152,12 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
   const int ys = g.ys;
   const int nbr_swap = Jg->nbr_swap;
   const int band = Jg->band;
-  const float nbql2 = -Jg->beta_q_l2, c0 = exp2_filter_c0(Jg->beta_band);
+  const float inv_k = 1.0f / Jg->beta_q_l2, band_f = (float)band;
   const int64_t n_trials = Jg->n_trials;
   const int n_peek = nbr_swap ? 5 : 7;
   const int n_base = nbr_swap ? 4 : 6;
+  // lanes 0-7 write site 1's cells of an accepted swap, lanes 8-15 site 2's
+  const bool img_b = lane >= 8;
   // 32-bit tallies (a launch runs fewer than 2^31 trials per chain, see
   // launch_metropolis_halo); the words drawn follow from them: n_base per
   // trial plus the uniforms
@@ -132,33 +171,49 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
 
   for (int t = 0; t < nt; ++t) {
     gens += R.avail < n_peek ? 1u : 0u;
-    ring_ensure(mt, tbuf, R, n_peek, lane);
+    ring_ensure_sites(mt, tbuf, ptab, ctab, S, R, n_peek, lane);
     const int wb = tb + R.idx;
     SitePair p;
-    int Ya, Xa, Yb, Xb;
-    draw_site_halo(g, bcc, s_u32[wb], s_u32[wb + 1], s_u32[wb + 2], p.ax, p.ay, p.az, Ya, Xa);
+    int Ya, Xa, Yb, Xb, pa, pb, ea = 0, eb = 0;
     if (nbr_swap) {
+      draw_site_halo(g, bcc, s_u32[wb], s_u32[wb + 1], s_u32[wb + 2], p.ax, p.ay, p.az, Ya, Xa);
       draw_nbr(g, s_u32[wb + 3], p.ax, p.ay, p.az, p.bx, p.by, p.bz);
       Yb = p.by >> ys;
       Xb = p.bx >> 1;
+      pa = H.origin + p.az * H.SZ + Ya * H.SY + Xa;
+      pb = H.origin + p.bz * H.SZ + Yb * H.SY + Xb;
     } else {
-      draw_site_halo(g, bcc, s_u32[wb + 3], s_u32[wb + 4], s_u32[wb + 5], p.bx, p.by, p.bz, Yb, Xb);
+      // the two sites from the site table: padded index and parity
+      ea = s_i32[pt + R.idx];
+      eb = s_i32[pt + R.idx + 3];
+      pa = ea & kPadMask;
+      pb = eb & kPadMask;
     }
-    const int pa = H.origin + p.az * H.SZ + Ya * H.SY + Xa;
-    const int pb = H.origin + p.bz * H.SZ + Yb * H.SY + Xb;
     p.sa = s_i8[lat_off + pa];
     p.sb = s_i8[lat_off + pb];
     int consumed = n_base;
     int accept = 1;  // same species: accepted without an energy evaluation or a draw
     if (p.sa != p.sb) {
       ++b_eval;
-      const bool near = pair_near(g, H, p.ax, p.ay, p.az, p.bx, p.by, p.bz);
-      int dE;
-      if (!near) {
-        const bool par_a = bcc ? (p.az & 1) : (p.ax & 1);
-        const bool par_b = bcc ? (p.bz & 1) : (p.bx & 1);
-        dE = halo_delta<NJ, FULL>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
+      bool par_a, par_b;
+      if (nbr_swap) {
+        par_a = bcc ? (p.az & 1) : (p.ax & 1);
+        par_b = bcc ? (p.bz & 1) : (p.bx & 1);
       } else {
+        site_coords(s_i32[ct + R.idx], p.ax, p.ay, p.az);
+        site_coords(s_i32[ct + R.idx + 3], p.bx, p.by, p.bz);
+        Ya = p.ay >> ys;
+        Xa = p.ax >> 1;
+        Yb = p.by >> ys;
+        Xb = p.bx >> 1;
+        par_a = ea >> 30;
+        par_b = eb >> 30;
+      }
+      // the fast-tier sum is issued first and the near test fills its loads'
+      // latency; a neighbouring pair (which the fast sum assumes away) takes
+      // the general sum instead
+      int dE = halo_delta<NJ, FULL>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
+      if (pair_near_flat(g, H, p.ax, p.ay, p.az, p.bx, p.by, p.bz)) {
         dE = halo_delta_general(Jg, (int)L.ents, I_off, L.F_off, hl, p.ax, p.ay, p.az,
                                 p.az * g.sz + Ya * g.sy + Xa, p.bx, p.by, p.bz,
                                 p.bz * g.sz + Yb * g.sy + Xb, p.sa, p.sb, lane);
@@ -169,7 +224,8 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
         accept = 1;
       } else if (dE > band) {
         consumed = n_base + 1;
-        accept = fast_ex2_decision(nbql2, c0, dE, wu);
+        const AcceptThresholds th = accept_thresholds(wu, inv_k, band_f);
+        accept = dE < th.acc_below ? 1 : (dE > th.rej_above ? 0 : -1);
       }
       if (accept < 0) {
         ++b_exact;
@@ -181,7 +237,11 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
         c_fp64 += (r >> 2) & 1;
         c_cr += (r >> 3) & 1;
       }
-      if (accept) halo_write_pair(H, lat, lane, p.az, Ya, Xa, p.sb, p.bz, Yb, Xb, p.sa);
+      if (accept) {
+        const int img = halo_image_index(H, lane, p.az, Ya, Xa, p.bz, Yb, Xb);
+        if (img >= 0) s_i8[lat_off + img] = (int8_t)(img_b ? p.sa : p.sb);
+        __syncwarp();
+      }
     }
     b_acc += accept;
     ring_consume(R, consumed);

@@ -142,8 +142,9 @@ int brawl_counters(brawl_ctx *ctx, int64_t *counters);
  * library, held by every device that loads it until the process exits;
  * lattices with more sites are rejected with BRAWL_EINVAL.  The work is
  * queued on `stream` (a cudaStream_t, NULL for the default stream) and the
- * call returns without waiting.  The first call on each device (with that
- * device current) does a one-time set-up, so make it before any stream
+ * call returns without waiting.  The first call made with a given CUDA
+ * context current (per device, its primary context for runtime-API callers)
+ * does a one-time set-up of that context, so make it before any stream
  * capture.  Calls share the scratch array: calls that overlap on the GPU
  * race.  The config must hold species 1..n_species on every lattice site. */
 int brawl_total_energy_noalloc(const brawl_setup *setup, const double *d_V_ex,

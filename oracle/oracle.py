@@ -20,13 +20,23 @@ SC, BCC, FCC = 0, 1, 2
 LATTICE_IDS = {"simple_cubic": SC, "sc": SC, "bcc": BCC, "fcc": FCC}
 
 
+def reference_dir() -> str:
+    """Where a checkout of the reference is looked for: $BRAWL_REFERENCE_DIR,
+    else a `reference` directory beside this repository."""
+    env = os.environ.get("BRAWL_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
 def build(ref: bool = False) -> None:
     """Compile liboracle.so (and, with ref=True, the reference's own
     mt19937ar.c into _ref/ where its sources are present) with the committed
     Makefile."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref-if-present"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref-if-present", "REF_DIR=" + reference_dir()],
+                       check=True)
 
 
 class Rng(C.Structure):

@@ -61,4 +61,8 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # the reference checkout: the first argument, else $BRAWL_REFERENCE_DIR
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BRAWL_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout>  (or set BRAWL_REFERENCE_DIR)")
+    main(ref)

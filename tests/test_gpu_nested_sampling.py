@@ -60,3 +60,41 @@ def test_nested_sampling_golden_configuration():
     lim = nsg.iterate(nsp.n_iter)[0]
     assert np.array_equal(lim, limits_o)
     assert np.array_equal(nsg.energies(0), energies_o)
+
+
+# The nested-sampling workload's own shape (fcc 6^3, 5 species, 3 shells,
+# V uniform +-0.08 eV, K = 1024 walkers, 2000-step walks), for 20
+# iterations; and a small-K run on the same lattice that reaches the
+# adaptive extra_steps branch (src/nested_sampling.f90:129-144): with
+# n_at * 0.05 = 54 and 20-step walks, every check at i_iter = K/2, K, ...
+# finds fewer than 54 accepted steps and lengthens the walks.
+SHAPE_CASES = [
+    # lattice, n, ns, nsh, K, n_steps, n_iter, seed
+    ("fcc", (6, 6, 6), 5, 3, 1024, 2000, 20, 31),
+    ("fcc", (6, 6, 6), 5, 3, 8, 20, 120, 32),
+]
+
+
+@pytest.mark.parametrize("case", SHAPE_CASES, ids=lambda c: f"{c[0]}-{c[1]}-K{c[4]}")
+def test_nested_sampling_workload_shape_matches_oracle(case):
+    lattice, n, ns, nsh, K, n_steps, n_iter, seed = case
+    rng = np.random.default_rng(seed)
+    V = random_V(rng, ns, nsh, 0.08)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    nums = equi_numbers(setup.n_atoms, ns)
+    mod = O.OracleModel(lattice, *n, V)
+    r = O.OracleRng(seed)
+    limits_o, walkers_o, energies_o, acc_o = mod.ns_run(r, conc_vector(ns), nums, K, n_steps,
+                                                        n_iter)
+    run = dict(setup=setup, V=V, seed=seed, n_walkers=K, n_steps=n_steps,
+               species_concentrations=conc_vector(ns), species_numbers=nums)
+    nsg = B.NestedSampling([run])
+    lim = nsg.iterate(n_iter)[0]
+    assert np.array_equal(lim, limits_o)
+    assert np.array_equal(nsg.energies(0), energies_o)
+    for w in range(0, K, max(1, K // 64)):
+        assert np.array_equal(nsg.walker_config(0, w), walkers_o[w])
+    c = nsg.counters(0)
+    if K < 2 * n_iter:
+        # the walks were lengthened: more steps than n_iter * n_steps
+        assert c["trials"] > n_iter * n_steps
