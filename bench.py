@@ -221,15 +221,65 @@ def committed_traffic() -> dict | None:
     return None
 
 
+class UtilSampler:
+    """utilization.gpu (the fraction of time a kernel ran) every 200 ms."""
+
+    def __init__(self, device_index: int):
+        self.vals = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=utilization.gpu", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(device_index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            try:
+                self.vals.append((time.perf_counter(), float(line.strip())))
+            except ValueError:
+                pass
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return self.vals
+
+
+def _mean_util(samples, t_lo, t_hi):
+    v = [u for t, u in samples if t_lo <= t <= t_hi]
+    return float(np.mean(v)) / 100.0 if v else None
+
+
 def serving_leg(args) -> dict:
-    """The mixed job stream through the serving loop (brawl_serve_*):
-    Poisson arrivals at args.serve_rate jobs/s, latency = finish - submit
-    per job, throughput = swap trials of all jobs / makespan."""
+    """The serving stream through the continuous-batching loop
+    (brawl_serve_*), on the mixed workload's ranges: fcc/bcc, L in [6, 32],
+    2-5 species, 2-6 shells, anneals of 100-2000 sweeps, Wang-Landau windows
+    and nested-sampling runs.  Two phases.
+    latency: Poisson arrivals at args.serve_rate jobs/s (below capacity),
+      latency = finish - submit per job, p50/p99 overall and by kind, the
+      device's busy fraction while jobs arrive;
+    saturation: arrivals far above capacity for args.serve_sat_seconds;
+      throughput = work the scheduler handed out per second once the resident
+      set has filled (trials; Wang-Landau summed over walkers; nested
+      sampling walk steps), and the busy fraction over the same window."""
     from brawl_gb300 import serving as SV
+    dev = torch_device_index()
+    out = {}
+    # ---- latency phase
     jobs = SV.stream_jobs(args.serve_jobs, master_seed=424242, L_range=(6, args.serve_L_max),
                           sweeps_range=(100, args.serve_sweeps_max))
     rng = np.random.default_rng(99)
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, len(jobs)))
+    util = UtilSampler(dev)
     with SV.Server() as srv:
         ids = []
         t0 = time.perf_counter()
@@ -238,6 +288,7 @@ def serving_leg(args) -> dict:
             if dt > 0:
                 time.sleep(dt)
             ids.append(srv.submit(job))
+        t_arrived = time.perf_counter()
         res = []
         for i in ids:
             try:
@@ -247,6 +298,8 @@ def serving_leg(args) -> dict:
                             "t_finish": 0.0, "trials": 0})
         makespan = time.perf_counter() - t0
         stats = srv.stats()
+        prof = srv.profile()
+    samples = util.stop()
     ok = [r for r in res if r["status"] == 0]
     failed = {}
     for job, r in zip(jobs, res):
@@ -261,21 +314,73 @@ def serving_leg(args) -> dict:
             by_kind.setdefault(job["kind"], []).append(r["t_finish"] - r["t_submit"])
     trials = sum(SV.job_trials(j) for j, r in zip(jobs, res) if r["status"] == 0 and j["kind"] != "ns")
     ns_steps = sum(int(r["trials"]) for j, r in zip(jobs, res) if r["status"] == 0 and j["kind"] == "ns")
-    return {
-        "stream": f"{len(jobs)} jobs of the seeded mixed stream: fcc/bcc, L in [6,{args.serve_L_max}], "
-                  f"2-5 species (Dirichlet composition), 2-6 shells; anneal {100}-{args.serve_sweeps_max} "
-                  "sweeps over 4 temperatures, WL window (4 walkers x 20 one-sweep calls), "
-                  "NS run (64 walkers, 100 iterations of one-sweep walks)",
-        "arrivals": f"Poisson, {args.serve_rate} jobs/s",
+    counts = {k: sum(1 for j in jobs if j["kind"] == k) for k in ("anneal", "wl", "ns")}
+    out["latency"] = {
+        "stream": f"{len(jobs)} jobs (of the 10^4 of the full stream) of the seeded mixed stream: "
+                  f"fcc/bcc, L in [6,{args.serve_L_max}], 2-5 species (Dirichlet composition), "
+                  f"2-6 shells, V uniform +-0.05 eV; anneal 100-{args.serve_sweeps_max} sweeps over "
+                  "4 temperatures, WL window (4 walkers, 256 bins, 20 one-sweep calls), NS run "
+                  "(64 walkers, 100 iterations of one-sweep walks)",
+        "jobs_by_kind": counts,
+        "arrivals": f"Poisson, {args.serve_rate} jobs/s over {arrivals[-1]:.0f} s",
         "jobs_ok": len(ok), "jobs_failed": failed,
         "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
         "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
         "p50_queue_s": float(np.percentile(queue, 50)) if len(queue) else None,
+        "p99_queue_s": float(np.percentile(queue, 99)) if len(queue) else None,
         "p50_by_kind_s": {k: float(np.percentile(v, 50)) for k, v in by_kind.items()},
+        "p99_by_kind_s": {k: float(np.percentile(v, 99)) for k, v in by_kind.items()},
         "makespan_s": makespan,
         "trials_per_s": (trials + ns_steps) / makespan,
+        "gpu_busy_while_arriving": _mean_util(samples, t0, t_arrived),
         "rounds": stats["rounds"],
+        "busy_s_by_pipeline": {k: round(v["busy_s"], 2) for k, v in prof.items()},
     }
+    # ---- saturation phase
+    n_sat = int(args.serve_sat_rate * args.serve_sat_seconds)
+    if n_sat > 0:
+        jobs = SV.stream_jobs(n_sat, master_seed=525252, L_range=(6, args.serve_L_max),
+                              sweeps_range=(100, args.serve_sweeps_max))
+        arrivals = np.cumsum(rng.exponential(1.0 / args.serve_sat_rate, len(jobs)))
+        util = UtilSampler(dev)
+        series = []
+        with SV.Server() as srv:
+            t0 = time.perf_counter()
+            k = 0
+            t_next = t0
+            while time.perf_counter() - t0 < args.serve_sat_seconds:
+                now = time.perf_counter() - t0
+                while k < len(jobs) and arrivals[k] <= now:
+                    srv.submit(jobs[k])
+                    k += 1
+                if time.perf_counter() >= t_next:
+                    p = srv.profile()
+                    st = srv.stats()
+                    series.append((time.perf_counter(), sum(v["work"] for v in p.values()),
+                                   st["resident"], st["queued"]))
+                    t_next += 1.0
+                time.sleep(0.005)
+            # the window: from a third of the phase to its end
+        samples = util.stop()
+        lo = series[len(series) // 3]
+        hi = series[-1]
+        out["saturation"] = {
+            "arrivals": f"Poisson, {args.serve_sat_rate} jobs/s for {args.serve_sat_seconds} s "
+                        "(far above capacity: the queue grows)",
+            "window_s": hi[0] - lo[0],
+            "trials_per_s": (hi[1] - lo[1]) / (hi[0] - lo[0]),
+            "resident_jobs": [lo[2], hi[2]],
+            "queued_jobs": [lo[3], hi[3]],
+            "gpu_busy": _mean_util(samples, lo[0], hi[0]),
+            "note": "work handed out by the scheduler per second: swap trials of anneal chains "
+                    "and Wang-Landau walkers, nested-sampling walk steps at n_steps per iteration",
+        }
+    return out
+
+
+def torch_device_index() -> int:
+    import torch
+    return torch.cuda.current_device() if torch.cuda.is_available() else 0
 
 
 # neighbours within the first k shells (k = 1, 2, ...)
@@ -562,10 +667,12 @@ def main() -> int:
     ap.add_argument("--sweeps-per-step", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--serve-jobs", type=int, default=150)
-    ap.add_argument("--serve-rate", type=float, default=15.0)
-    ap.add_argument("--serve-L-max", type=int, default=16)
-    ap.add_argument("--serve-sweeps-max", type=int, default=500)
+    ap.add_argument("--serve-jobs", type=int, default=900)
+    ap.add_argument("--serve-rate", type=float, default=10.0)
+    ap.add_argument("--serve-L-max", type=int, default=32)
+    ap.add_argument("--serve-sweeps-max", type=int, default=2000)
+    ap.add_argument("--serve-sat-rate", type=float, default=80.0)
+    ap.add_argument("--serve-sat-seconds", type=float, default=45.0)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--walker-legs", default="wl,ns",
                     help="Wang-Landau / nested-sampling legs to run (wl, ns; empty for none)")

@@ -120,6 +120,15 @@ __host__ __device__ inline HaloLayout halo_layout(const Geom& g, const HaloGeom&
 
 int lane_entries_for(int max_z);
 
+// Load the code of every kernel variant a translation unit launches (module
+// loading is lazy by default; a launch that first loads code waits for the
+// kernels already running on the device).
+void preload_metropolis_kernels();
+void preload_halo_kernels();
+void preload_ns_kernels();
+void preload_wl_kernels();
+void preload_lattice_kernels();
+
 // Metropolis swap trials for chains staged with a halo (fcc/bcc that fit).
 // Speculative rounds of nc (2-4) trials per chain, nc(nc+1)/2 warps per CTA
 // (metropolis_spec.cu); spec_static_smem is the static shared memory the

@@ -251,4 +251,15 @@ void launch_unpack_batch(const GridJob* d_jobs, int n_jobs, int64_t total_cells,
   if (n_jobs > 0) unpack_batch_kernel<<<batch_grid(n_jobs, total_cells), 256, 0, stream>>>(d_jobs, d_grids);
 }
 
+void preload_lattice_kernels() {
+  cudaFuncAttributes a;
+  cudaFuncGetAttributes(&a, initial_setup_kernel);
+  cudaFuncGetAttributes(&a, site_energies_kernel);
+  cudaFuncGetAttributes(&a, sum_sites_kernel);
+  cudaFuncGetAttributes(&a, pack_kernel);
+  cudaFuncGetAttributes(&a, unpack_kernel);
+  cudaFuncGetAttributes(&a, pack_batch_kernel);
+  cudaFuncGetAttributes(&a, unpack_batch_kernel);
+}
+
 }  // namespace brawl

@@ -214,4 +214,23 @@ void launch_metropolis(const ChainJob* d_jobs, int n_jobs, bool lattice_in_smem,
   }
 }
 
+// Loads every variant's code now (module loading is lazy by default, and a
+// first launch that loads code waits for the kernels already running).
+template <int NJ>
+static void preload_nj(cudaFuncAttributes& a) {
+  cudaFuncGetAttributes(&a, metropolis_kernel<NJ, true, true>);
+  cudaFuncGetAttributes(&a, metropolis_kernel<NJ, true, false>);
+  cudaFuncGetAttributes(&a, metropolis_kernel<NJ, false, true>);
+  cudaFuncGetAttributes(&a, metropolis_kernel<NJ, false, false>);
+}
+
+void preload_metropolis_kernels() {
+  cudaFuncAttributes a;
+  preload_nj<2>(a);
+  preload_nj<4>(a);
+  preload_nj<6>(a);
+  preload_nj<8>(a);
+  preload_nj<11>(a);
+}
+
 }  // namespace brawl

@@ -297,4 +297,14 @@ void launch_metropolis_halo(const ChainJob* d_jobs, int n_jobs, uint32_t smem_by
   }
 }
 
+void preload_halo_kernels() {
+  cudaFuncAttributes a;
+  cudaFuncGetAttributes(&a, metropolis_halo_kernel<2, false>);
+  cudaFuncGetAttributes(&a, metropolis_halo_kernel<4, false>);
+  cudaFuncGetAttributes(&a, metropolis_halo_kernel<4, true>);
+  cudaFuncGetAttributes(&a, metropolis_halo_kernel<6, false>);
+  cudaFuncGetAttributes(&a, metropolis_halo_kernel<8, false>);
+  cudaFuncGetAttributes(&a, metropolis_halo_kernel<11, false>);
+}
+
 }  // namespace brawl

@@ -344,4 +344,21 @@ void launch_ns_iterate(NsRun* d_runs, int n_runs, uint32_t smem_bytes, int max_z
   else launch_ns_d<false>(d_runs, n_runs, smem_bytes, max_z, stream);
 }
 
+template <bool kUseD>
+static void preload_ns_d(cudaFuncAttributes& a) {
+  cudaFuncGetAttributes(&a, ns_iterate_kernel<2, kUseD>);
+  cudaFuncGetAttributes(&a, ns_iterate_kernel<4, kUseD>);
+  cudaFuncGetAttributes(&a, ns_iterate_kernel<6, kUseD>);
+  cudaFuncGetAttributes(&a, ns_iterate_kernel<8, kUseD>);
+  cudaFuncGetAttributes(&a, ns_iterate_kernel<11, kUseD>);
+}
+
+void preload_ns_kernels() {
+  cudaFuncAttributes a;
+  preload_ns_d<true>(a);
+  preload_ns_d<false>(a);
+  cudaFuncGetAttributes(&a, ns_init_kernel);
+  cudaFuncGetAttributes(&a, ns_jitter_kernel);
+}
+
 }  // namespace brawl

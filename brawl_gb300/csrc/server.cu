@@ -171,9 +171,18 @@ __global__ void ns_unstage_kernel(const NsRun* __restrict__ from, NsRun* const* 
 }
 
 // One job kind's pipeline.
+// A round's chains, walkers or runs are launched in up to 1 + kSide groups
+// of similar shared-memory size, the first on the pipeline's stream and the
+// others on side streams forked from it and joined back: one launch sized
+// for the largest lattice would give every small one the same shared
+// memory and leave most of each SM's slots empty.
+constexpr int kSide = 3;
+
 struct Pipe {
   cudaStream_t s = nullptr;
   cudaEvent_t ev = nullptr;
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t ev_fork = nullptr, ev_side[kSide] = {};
   bool inflight = false;
   std::vector<JobP> jobs;      // resident
   std::vector<JobP> launched;  // in the in-flight round, in staged order
@@ -246,6 +255,12 @@ struct Pipe {
     for (void* p : {(void*)h_stage, (void*)h_eout, (void*)h_st, (void*)h_acc, (void*)h_tns, (void*)h_wl,
                     (void*)h_flat, (void*)h_limits})
       if (p) cudaFreeHost(p);
+    for (int g = 0; g < kSide; ++g) {
+      if (side[g]) cudaStreamSynchronize(side[g]);
+      if (ev_side[g]) cudaEventDestroy(ev_side[g]);
+      if (side[g]) cudaStreamDestroy(side[g]);
+    }
+    if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev) cudaEventDestroy(ev);
     if (s) cudaStreamDestroy(s);
   }
@@ -264,6 +279,50 @@ int stage_copy(Pipe& P, void* dst, const void* src, size_t bytes) {
     SV_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, P.s));
     SV_CUDA(cudaStreamSynchronize(P.s));  // pageable source: keep it alive until copied
   }
+  return BRAWL_OK;
+}
+
+bool make_side_streams(Pipe& P, int prio) {
+  for (int g = 0; g < kSide; ++g)
+    if (cudaStreamCreateWithPriority(&P.side[g], cudaStreamNonBlocking, prio) != cudaSuccess ||
+        cudaEventCreateWithFlags(&P.ev_side[g], cudaEventDisableTiming) != cudaSuccess)
+      return false;
+  return true;
+}
+
+// Groups of a round's items in staged order, which is by decreasing shared
+// memory: a new group starts where an item needs less than two thirds of
+// its group's first (largest), so it would fit 1.5 times as many CTAs per
+// SM; the last group takes the rest.
+struct Group {
+  int first, count;
+};
+
+std::vector<Group> smem_groups(const std::vector<uint32_t>& smem) {
+  std::vector<Group> gs;
+  for (int i = 0; i < (int)smem.size(); ++i) {
+    if (gs.empty() || ((int)gs.size() <= kSide && 3ull * smem[i] < 2ull * smem[gs.back().first]))
+      gs.push_back({i, 0});
+    gs.back().count += 1;
+  }
+  return gs;
+}
+
+// Launches group g with launch(first, count, stream): group 0 on the
+// pipeline's stream, the others on side streams that wait for the work
+// queued so far and that the pipeline's stream waits for afterwards.
+template <class F>
+int launch_groups(Pipe& P, const std::vector<Group>& gs, F launch) {
+  if (gs.empty()) return BRAWL_OK;
+  if (gs.size() > 1) SV_CUDA(cudaEventRecord(P.ev_fork, P.s));
+  for (size_t g = 0; g < gs.size(); ++g) {
+    cudaStream_t st = g == 0 ? P.s : P.side[g - 1];
+    if (g > 0) SV_CUDA(cudaStreamWaitEvent(st, P.ev_fork, 0));
+    launch(gs[g].first, gs[g].count, st);
+    SV_CUDA(cudaGetLastError());
+    if (g > 0) SV_CUDA(cudaEventRecord(P.ev_side[g - 1], st));
+  }
+  for (size_t g = 1; g < gs.size(); ++g) SV_CUDA(cudaStreamWaitEvent(P.s, P.ev_side[g - 1], 0));
   return BRAWL_OK;
 }
 
@@ -582,11 +641,14 @@ int launch_anneal(brawl_server* S, Pipe& P) {
   std::vector<ChainJob> staged;
   std::vector<EnergyJob> ej;
   P.launched.clear();
-  uint32_t halo_smem = 0, lat_smem = 0, glob_smem = 0;
-  int halo_min_z = 0, halo_z = 0, table_z = 0;
+  uint32_t lat_smem = 0, glob_smem = 0;
+  int table_z = 0;
   bool use_D = true;
   SV_TRY(grow(P.d_tns, P.tns_cap, std::max<size_t>(P.jobs.size(), 1), P.s));
   const double t_round = round_ns(S, P.jobs);
+  std::stable_sort(P.jobs.begin(), P.jobs.end(), [](const JobP& a, const JobP& b) {
+    return a->slot.halo_smem > b->slot.halo_smem;
+  });
   for (int pass = 0; pass < 2; ++pass)
     for (auto& j : P.jobs) {
       if (j->slot.halo != (pass == 0 ? 1 : 0)) continue;
@@ -601,11 +663,7 @@ int launch_anneal(brawl_server* S, Pipe& P) {
         j->e_idx = (int)ej.size();
         ej.push_back(j->slot.energy);
       }
-      if (pass == 0) {
-        halo_smem = std::max(halo_smem, j->slot.halo_smem);
-        halo_min_z = halo_z == 0 ? (int)c.g.z : std::min(halo_min_z, (int)c.g.z);
-        halo_z = std::max(halo_z, (int)c.g.z);
-      } else {
+      if (pass == 1) {
         lat_smem = std::max(lat_smem, j->slot.smem_lat_bytes);
         glob_smem = std::max(glob_smem, j->slot.smem_glob_bytes);
         table_z = std::max(table_z, (int)c.g.z);
@@ -617,8 +675,20 @@ int launch_anneal(brawl_server* S, Pipe& P) {
   const int n = (int)staged.size();
   SV_TRY(grow(P.d_chain, P.chain_cap, (size_t)n, P.s));
   SV_TRY(stage_copy(P, P.d_chain, staged.data(), n * sizeof(ChainJob)));
-  if (nh > 0)
-    launch_halo_chains(P.d_chain, nh, halo_smem, halo_min_z, halo_z, kDefaultSpeculation, S->max_optin, P.s);
+  if (nh > 0) {
+    std::vector<uint32_t> sm(nh);
+    for (int k = 0; k < nh; ++k) sm[k] = P.launched[k]->slot.halo_smem;
+    SV_TRY(launch_groups(P, smem_groups(sm), [&](int first, int count, cudaStream_t st) {
+      int zmin = 0, zmax = 0;
+      for (int k = first; k < first + count; ++k) {
+        const int z = staged[k].g.z;
+        zmin = zmax == 0 ? z : std::min(zmin, z);
+        zmax = std::max(zmax, z);
+      }
+      launch_halo_chains(P.d_chain + first, count, sm[first], zmin, zmax, kDefaultSpeculation,
+                         S->max_optin, st);
+    }));
+  }
   if (n - nh > 0) {
     const bool smem_lat = lat_smem <= (uint32_t)S->max_optin;
     launch_metropolis(P.d_chain + nh, n - nh, smem_lat, use_D, smem_lat ? lat_smem : glob_smem, table_z, P.s);
@@ -641,9 +711,12 @@ int launch_wl(brawl_server* S, Pipe& P) {
   std::vector<WlGroup> groups;
   std::vector<EnergyJob> ej;
   std::vector<int> ej_walker;
-  uint32_t smem = 0;
-  int max_bins = 0, max_z = 0;
-  bool all_D = true;
+  std::vector<uint32_t> w_smem;
+  std::vector<int> w_z;
+  std::vector<char> w_D;
+  int max_bins = 0;
+  std::stable_sort(P.jobs.begin(), P.jobs.end(),
+                   [](const JobP& a, const JobP& b) { return api_wl_smem(a->wl) > api_wl_smem(b->wl); });
   P.launched = P.jobs;
   P.call_ends.assign(P.launched.size(), 0);
   size_t n_all = 0;
@@ -678,12 +751,12 @@ int launch_wl(brawl_server* S, Pipe& P) {
       }
       staged.push_back(W);
     }
-    smem = std::max(smem, api_wl_smem(j.wl));
     int jz = 0;
     bool jd = true;
     api_wl_variant(j.wl, &jz, &jd);
-    max_z = std::max(max_z, jz);
-    all_D = all_D && jd;
+    w_smem.insert(w_smem.end(), w.size(), api_wl_smem(j.wl));
+    w_z.insert(w_z.end(), w.size(), jz);
+    w_D.insert(w_D.end(), w.size(), jd ? 1 : 0);
     max_bins = std::max(max_bins, j.d.wl_bins);
   }
   const int n = (int)staged.size();
@@ -697,7 +770,15 @@ int launch_wl(brawl_server* S, Pipe& P) {
   SV_TRY(grow_host(P.h_flat, P.h_flat_cap, (size_t)n));
   SV_TRY(stage_copy(P, P.d_wl, staged.data(), n * sizeof(WlWalker)));
   if (!groups.empty()) SV_TRY(stage_copy(P, P.d_groups, groups.data(), groups.size() * sizeof(WlGroup)));
-  launch_wl_sweeps(P.d_wl, n, smem, max_z, all_D, P.s);
+  SV_TRY(launch_groups(P, smem_groups(w_smem), [&](int first, int count, cudaStream_t st) {
+    int max_z = 0;
+    bool all_D = true;
+    for (int k = first; k < first + count; ++k) {
+      max_z = std::max(max_z, w_z[k]);
+      all_D = all_D && w_D[k];
+    }
+    launch_wl_sweeps(P.d_wl + first, count, w_smem[first], max_z, all_D, st);
+  }));
   if (!groups.empty()) launch_wl_average(P.d_groups, (int)groups.size(), P.d_wl, max_bins, 1, P.s);
   launch_wl_flatness(P.d_wl, n, P.d_flat, P.s);
   SV_CUDA(cudaGetLastError());
@@ -709,13 +790,16 @@ int launch_wl(brawl_server* S, Pipe& P) {
 }
 
 int launch_ns(brawl_server* S, Pipe& P) {
+  std::stable_sort(P.jobs.begin(), P.jobs.end(),
+                   [](const JobP& a, const JobP& b) { return api_ns_smem(a->ns) > api_ns_smem(b->ns); });
   P.launched = P.jobs;
   const int n = (int)P.launched.size();
   std::vector<NsRun*> src(n);
   std::vector<int> ints(2 * n);
-  uint32_t smem = 0;
-  int total = 0, max_z = 0;
-  bool all_D = true;
+  std::vector<uint32_t> r_smem(n);
+  std::vector<int> r_z(n);
+  std::vector<char> r_D(n);
+  int total = 0;
   const double t_round = round_ns(S, P.launched);
   for (int k = 0; k < n; ++k) {
     Job& j = *P.launched[k];
@@ -724,12 +808,12 @@ int launch_ns(brawl_server* S, Pipe& P) {
     ints[k] = (int)j.quantum;
     ints[n + k] = total;
     total += (int)j.quantum;
-    smem = std::max(smem, api_ns_smem(j.ns));
+    r_smem[k] = api_ns_smem(j.ns);
     int jz = 0;
     bool jd = true;
     api_ns_variant(j.ns, &jz, &jd);
-    max_z = std::max(max_z, jz);
-    all_D = all_D && jd;
+    r_z[k] = jz;
+    r_D[k] = jd ? 1 : 0;
   }
   P.lim_off.assign(ints.begin() + n, ints.end());
   SV_TRY(grow(P.d_ns, P.ns_cap, (size_t)n, P.s));
@@ -743,7 +827,15 @@ int launch_ns(brawl_server* S, Pipe& P) {
   BRAWL_CARVEOUT(ns_stage_kernel);
   ns_stage_kernel<<<(n + 63) / 64, 64, 0, P.s>>>(P.d_ns, P.d_ns_src, n, P.d_limits, P.d_ns_int, P.d_ns_int + n,
                                                   P.d_tns);
-  launch_ns_iterate(P.d_ns, n, smem, max_z, all_D, P.s);
+  SV_TRY(launch_groups(P, smem_groups(r_smem), [&](int first, int count, cudaStream_t st) {
+    int max_z = 0;
+    bool all_D = true;
+    for (int k = first; k < first + count; ++k) {
+      max_z = std::max(max_z, r_z[k]);
+      all_D = all_D && r_D[k];
+    }
+    launch_ns_iterate(P.d_ns + first, count, r_smem[first], max_z, all_D, st);
+  }));
   BRAWL_CARVEOUT(ns_unstage_kernel);
   ns_unstage_kernel<<<(n + 63) / 64, 64, 0, P.s>>>(P.d_ns, P.d_ns_src, n);
   SV_CUDA(cudaGetLastError());
@@ -767,7 +859,10 @@ int launch_round(brawl_server* S, int kind) {
   P.inflight = true;
   P.t_launched = S->now();
   int64_t work = 0;
-  for (auto& j : P.launched) work += j->quantum * (kind == kWl ? j->d.wl_walkers : 1);
+  // trials; Wang-Landau: of every walker; nested sampling: walk steps at
+  // n_steps per iteration (adaptive extra steps not counted)
+  for (auto& j : P.launched)
+    work += j->quantum * (kind == kWl ? j->d.wl_walkers : (kind == kNs ? j->d.ns_steps : 1));
   std::lock_guard<std::mutex> lk(S->mu);  // telemetry is read by brawl_serve_profile
   P.launch_s += P.t_launched - t0;
   P.work += work;
@@ -1069,6 +1164,20 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
   if (S->o.max_trials < 0) S->o.max_trials = 0;
   if (S->o.max_iterations < 0) S->o.max_iterations = 0;
   cudaDeviceGetAttribute(&S->max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, S->device);
+  // every kernel a round may launch is loaded now: a round that first used
+  // a variant would otherwise wait for every round in flight
+  preload_metropolis_kernels();
+  preload_halo_kernels();
+  preload_ns_kernels();
+  preload_wl_kernels();
+  preload_lattice_kernels();
+  {
+    cudaFuncAttributes a;
+    cudaFuncGetAttributes(&a, gather_kernel);
+    cudaFuncGetAttributes(&a, ns_stage_kernel);
+    cudaFuncGetAttributes(&a, ns_unstage_kernel);
+  }
+  cudaGetLastError();
   {
     // keep freed stream-ordered memory in this process's pool for reuse
     cudaMemPool_t pool;
@@ -1088,6 +1197,8 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
     // rounds run at the lowest priority: set-up and read-back of jobs go first
     if (cudaStreamCreateWithPriority(&P.s, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
         cudaEventCreateWithFlags(&P.ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&P.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        !make_side_streams(P, prio_lo) ||
         grow_host(P.h_stage, P.h_stage_cap, kPinnedStage) != BRAWL_OK ||
         grow_host(P.h_eout, P.h_eout_cap, kPinnedEntries) != BRAWL_OK ||
         grow_host(P.h_st, P.h_st_cap, kPinnedEntries) != BRAWL_OK ||

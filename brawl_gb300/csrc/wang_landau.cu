@@ -922,4 +922,21 @@ void launch_wl_store_merge(const WlWalker* d_walkers, int n, int bins, const int
   wl_store_merge_kernel<<<grid, 256, 0, stream>>>(d_walkers, n, d_pick);
 }
 
+template <bool kUseD>
+static void preload_wl_d(cudaFuncAttributes& a) {
+  cudaFuncGetAttributes(&a, wl_sweep_kernel<2, kUseD>);
+  cudaFuncGetAttributes(&a, wl_sweep_kernel<4, kUseD>);
+  cudaFuncGetAttributes(&a, wl_sweep_kernel<6, kUseD>);
+  cudaFuncGetAttributes(&a, wl_sweep_kernel<8, kUseD>);
+  cudaFuncGetAttributes(&a, wl_sweep_kernel<11, kUseD>);
+}
+
+void preload_wl_kernels() {
+  cudaFuncAttributes a;
+  preload_wl_d<true>(a);
+  preload_wl_d<false>(a);
+  cudaFuncGetAttributes(&a, wl_average_kernel);
+  cudaFuncGetAttributes(&a, wl_flatness_kernel);
+}
+
 }  // namespace brawl

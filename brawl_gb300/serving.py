@@ -141,7 +141,9 @@ class Server:
         self._setups.pop(jid, None)
 
     def profile(self) -> dict:
-        """Per pipeline: rounds, device-busy, launch and settle seconds, work handed out."""
+        """Per pipeline: rounds, device-busy, launch and settle seconds, work
+        handed out (trials; Wang-Landau summed over walkers; nested sampling
+        walk steps at n_steps per iteration)."""
         v = np.zeros(15)
         _check(load().brawl_serve_profile(self._h, _ptr(v)))
         return {k: {"rounds": int(v[5 * i]), "busy_s": v[5 * i + 1], "launch_s": v[5 * i + 2],

@@ -467,7 +467,9 @@ int brawl_serve_release(brawl_server *server, uint64_t id);
 int brawl_serve_stats(brawl_server *server, int64_t stats[4]);
 /* Per pipeline (anneal, Wang-Landau, nested sampling), 5 values each:
  * rounds, seconds from launch to completion seen, seconds spent launching,
- * seconds spent settling, trials (NS: iterations) handed out. */
+ * seconds spent settling, trials handed out (Wang-Landau: summed over the
+ * walkers; nested sampling: walk steps at n_steps per iteration, adaptive
+ * extra steps not counted). */
 int brawl_serve_profile(brawl_server *server, double profile[15]);
 
 #ifdef __cplusplus
