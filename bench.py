@@ -497,6 +497,8 @@ def walker_legs(args) -> dict:
                          "note": "algorithmic bytes over host-timed calls; latency-bound walkers"},
             "cpu_baseline": _wl_cpu(setup, V, cfgs[0], edges, bins, period),
         }
+        if args.wl_seconds > 0:
+            out["wang_landau"]["windows_run"] = _wl_windows_run(args, setup, V, conc)
     if "ns" in args.walker_legs:
         rng = np.random.default_rng(20263)
         ns, nsh = 5, 3
@@ -549,6 +551,73 @@ def walker_legs(args) -> dict:
             "cpu_baseline": _ns_cpu(V, conc),
         }
     return out
+
+
+def _wl_windows_run(args, setup, V, conc) -> dict:
+    """The Wang-Landau workload's own layout through the driver
+    (brawl_gb300.wang_landau): 32000 bins split by divide_range into 32
+    windows of 1000 bins, each extended downwards by create_overlap (bin
+    overlap 0.25), 4 walkers per window (128), flatness 0.8, ln f from 1,
+    sweeps() calls of 10^4 trials per walker with replica exchange between
+    adjacent windows after every call, the in-window averages and
+    dos_combine at every halving.  The energy range (meV/atom) runs from the
+    lowest energy of a pilot anneal (8 chains, 300 K, 300 sweeps) to the
+    highest of 128 random configurations; the walkers enter their windows
+    by the temperature search.  The run is bounded by args.wl_seconds; the
+    time to ln f < 1e-6 (20 halvings) is extrapolated from the halvings
+    reached: the sweeps() calls per halving are fitted as c_k = a r^k on
+    the measured ones (least squares on log c_k) and the remaining
+    halvings cost their fitted calls at the run's seconds per call."""
+    import torch
+    import brawl_gb300 as B
+    from brawl_gb300 import inputs as I
+    from brawl_gb300 import wang_landau as WLD
+    N = setup.n_atoms
+    pilot = B.Batch([dict(setup=setup, V=V, seed=31 + k, beta=1.0 / (300.0 * B.K_B_IN_RY),
+                          species_concentrations=conc) for k in range(8)])
+    pilot.metropolis(300 * N)
+    e_lo = float(pilot.total_energy().min())
+    pilot.close()
+    rnd = B.Batch([dict(setup=setup, V=V, seed=1000 + k, beta=0.0, species_concentrations=conc)
+                   for k in range(128)])
+    e_hi = float(rnd.total_energy().max())
+    rnd.close()
+    to_mev = B.RY_TO_EV * 1000.0 / N
+    p = I.WLParams(mc_sweeps=0, bins=32000, num_windows=32, bin_overlap=float(np.float32(0.25)),
+                   tolerance=1e-6, flatness=float(np.float32(0.8)), wl_f=1.0,
+                   energy_min=float(np.float32(e_lo * to_mev)), energy_max=float(np.float32(e_hi * to_mev)))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = WLD.wang_landau(setup, V, conc, p, walkers_per_window=4, trials_per_call=10_000,
+                          deadline_s=args.wl_seconds, burn_in="temperature")
+    torch.cuda.synchronize()
+    total = time.perf_counter() - t0
+    rec = res["record"]
+    calls = res["calls"]
+    loop_s = args.wl_seconds if not rec or rec[-1]["wl_f"] > p.tolerance else rec[-1]["seconds"]
+    per_call = loop_s / max(1, calls)
+    c_k, prev = [], 0
+    for r in rec:
+        c_k.append(r["calls"] - prev)
+        prev = r["calls"]
+    est = None
+    if len(c_k) >= 2:
+        k = np.arange(1, len(c_k) + 1)
+        b, a = np.polyfit(k, np.log(np.maximum(c_k, 1)), 1)
+        fitted = [float(np.exp(a + b * kk)) for kk in range(len(c_k) + 1, 21)]
+        est = loop_s + (sum(fitted) - (calls - prev) if fitted else 0.0) * per_call
+    return {
+        "layout": "bcc 12^3, 4 species, 4 shells; 32000 bins, 32 windows (divide_range, "
+                  "create_overlap 0.25), 4 walkers each; exchange after every 10^4-trial call",
+        "energy_range_mev_per_atom": [p.energy_min, p.energy_max],
+        "seconds": total, "loop_seconds": loop_s, "calls": calls,
+        "trials_per_s": 128 * 10_000 * calls / loop_s,
+        "ln_f_reached": rec[-1]["wl_f"] if rec else 1.0,
+        "calls_per_halving": c_k,
+        "seconds_to_ln_f_1e-6_extrapolated": est,
+        "extrapolation": "calls per halving fitted as a*r^k on the measured halvings; "
+                         "the halvings up to 2^-20 < 1e-6 at the run's seconds per call",
+    }
 
 
 def anneal_leg(args) -> dict:
@@ -667,7 +736,7 @@ def main() -> int:
     ap.add_argument("--sweeps-per-step", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--serve-jobs", type=int, default=900)
+    ap.add_argument("--serve-jobs", type=int, default=600)
     ap.add_argument("--serve-rate", type=float, default=10.0)
     ap.add_argument("--serve-L-max", type=int, default=32)
     ap.add_argument("--serve-sweeps-max", type=int, default=2000)
@@ -679,6 +748,8 @@ def main() -> int:
     ap.add_argument("--walker-legs-only", action="store_true",
                     help="run only the walker legs and print their JSON")
     ap.add_argument("--wl-calls", type=int, default=5)
+    ap.add_argument("--wl-seconds", type=float, default=60.0,
+                    help="budget of the Wang-Landau run on the workload's window layout (0: skip)")
     ap.add_argument("--ns-iterations", type=int, default=50)
     ap.add_argument("--anneal-leg", type=int, default=1, help="time the one-chain annealing case (0: skip)")
     ap.add_argument("--anneal-cpu-temperatures", type=int, default=3)

@@ -46,6 +46,9 @@ namespace brawl {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMTN = 624;
+// Words mirrored past the end of a ring of tempered words (halo_engine.cuh),
+// so that up to this many consecutive words can be read without wrapping.
+constexpr int kRingMirror = 96;
 // trials per speculative round of the halo Metropolis kernel (1: one trial
 // at a time); brawl_batch_set_speculation overrides it per batch
 constexpr int kDefaultSpeculation = 1;

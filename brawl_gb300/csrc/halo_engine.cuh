@@ -42,13 +42,13 @@ __device__ __forceinline__ uint32_t mt_untemper(uint32_t y) {
 }
 
 // Ring of two tempered blocks in tbuf[0, 1248), plus a mirror of the first
-// 32 words at tbuf[1248, 1280) so the words of a trial (or of a round of
-// speculated trials) never wrap.  `idx` is the
+// kRingMirror words at tbuf[1248, 1248 + kRingMirror) so the words of a
+// trial (or of a round of speculated trials, or of a batch of redraws)
+// never wrap.  `idx` is the
 // ring slot of the next word, `avail` the generated words not yet consumed
 // (0..1248), `next_half` the half the next generated block goes to; mt holds
 // the newest generated block, untempered.
 constexpr int kRing = 2 * kMTN;
-constexpr int kRingMirror = 32;
 
 struct Ring {
   int idx;
@@ -62,7 +62,8 @@ static __device__ __noinline__ void ring_generate(uint32_t* mt, uint32_t* tbuf, 
   mt_twist_warp(mt, lane);
   uint32_t* dst = tbuf + next_half * kMTN;
   for (int i = lane; i < kMTN; i += 32) dst[i] = mt_temper(mt[i]);
-  if (next_half == 0 && lane < kRingMirror) tbuf[kRing + lane] = mt_temper(mt[lane]);
+  if (next_half == 0)
+    for (int i = lane; i < kRingMirror; i += 32) tbuf[kRing + i] = mt_temper(mt[i]);
   __syncwarp();
 }
 
@@ -70,14 +71,14 @@ static __device__ __noinline__ void ring_generate(uint32_t* mt, uint32_t* tbuf, 
 __device__ __forceinline__ void ring_init(const uint32_t* mt, uint32_t* tbuf, int pos0, int lane,
                                           Ring& R) {
   for (int i = lane; i < kMTN; i += 32) tbuf[i] = mt_temper(mt[i]);
-  if (lane < kRingMirror) tbuf[kRing + lane] = mt_temper(mt[lane]);
+  for (int i = lane; i < kRingMirror; i += 32) tbuf[kRing + i] = mt_temper(mt[i]);
   R.idx = pos0;
   R.avail = kMTN - pos0;
   R.next_half = 1;
   __syncwarp();
 }
 
-// Makes n <= 32 words available from R.idx.  A block is only generated when
+// Makes n <= kRingMirror words available from R.idx.  A block is only generated when
 // fewer than n remain, so the half it overwrites has been consumed.
 __device__ __forceinline__ void ring_ensure(uint32_t* mt, uint32_t* tbuf, Ring& R, int n,
                                             int lane) {
@@ -183,10 +184,11 @@ __device__ __forceinline__ void site_table_fill(const SiteDraw& S, const uint32_
     ctab[p] = ce;
   }
   __syncwarp();
-  if (lo == 0 && lane < kRingMirror) {
-    ptab[kRing + lane] = ptab[lane];
-    ctab[kRing + lane] = ctab[lane];
-  }
+  if (lo == 0)
+    for (int i = lane; i < kRingMirror; i += 32) {
+      ptab[kRing + i] = ptab[i];
+      ctab[kRing + i] = ctab[i];
+    }
   __syncwarp();
 }
 

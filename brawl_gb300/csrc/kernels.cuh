@@ -96,7 +96,7 @@ struct HaloLayout {
   int32_t F_off, D_off;
 };
 
-constexpr int kTbufWords = 2 * kMTN + 32;  // the ring and its mirror
+constexpr int kTbufWords = 2 * kMTN + kRingMirror;  // the ring and its mirror
 
 __host__ __device__ inline HaloLayout halo_layout(const Geom& g, const HaloGeom& H) {
   HaloLayout L;

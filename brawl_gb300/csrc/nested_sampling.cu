@@ -92,6 +92,11 @@ __device__ __forceinline__ long long gap_up(double limit, double E, int S) {
 }
 
 
+// site-2 redraws tried at once, one per lane (3 words each, within the
+// ring's mirror)
+constexpr int kRedraws = 32;
+static_assert(3 * kRedraws <= kRingMirror, "redraw words must fit the ring's mirror");
+
 template <int NJ, bool kUseD>
 __global__ void __launch_bounds__(32, 1) ns_iterate_kernel(NsRun* __restrict__ runs) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -210,19 +215,41 @@ __global__ void __launch_bounds__(32, 1) ns_iterate_kernel(NsRun* __restrict__ r
       ring_consume(ring, 3);
       p.ai = compact_index(g, p.ax, p.ay, p.az);
       p.sa = lat[p.ai];
+      // site 2 is redrawn until its species differs from site 1's: the
+      // redraws are consecutive word triples, so lane k tries the k-th next
+      // one and the first lane that finds another species ends the loop
+      // (kRedraws at a time)
       int tries = 0;
-      do {
-        ring_ensure(mt, tbuf, ring, 3, lane);
-        draw_site(g, tbuf[ring.idx], tbuf[ring.idx + 1], tbuf[ring.idx + 2], p.bx, p.by, p.bz);
-        ring_consume(ring, 3);
-        p.bi = compact_index(g, p.bx, p.by, p.bz);
-        p.sb = lat[p.bi];
-        c_draws += 3;
-        if (++tries > (1 << 24)) {
+      for (;;) {
+        ring_ensure(mt, tbuf, ring, 3 * kRedraws, lane);
+        int bx = 0, by = 0, bz = 0, bi = 0, sb = 0;
+        bool other = false;
+        if (lane < kRedraws) {
+          const int o = ring.idx + 3 * lane;
+          draw_site(g, tbuf[o], tbuf[o + 1], tbuf[o + 2], bx, by, bz);
+          bi = compact_index(g, bx, by, bz);
+          sb = lat[bi];
+          other = sb != p.sa;
+        }
+        const unsigned hit = __ballot_sync(kFull, other);
+        const int used = hit ? __ffs(hit) : kRedraws;  // redraws consumed
+        ring_consume(ring, 3 * used);
+        c_draws += 3 * used;
+        tries += used;
+        if (hit) {
+          const int k = used - 1;
+          p.bx = __shfl_sync(kFull, bx, k);
+          p.by = __shfl_sync(kFull, by, k);
+          p.bz = __shfl_sync(kFull, bz, k);
+          p.bi = __shfl_sync(kFull, bi, k);
+          p.sb = __shfl_sync(kFull, sb, k);
+          break;
+        }
+        if (tries > (1 << 24)) {
           status = kStatusBadSpecies;  // a single species: the reference loops forever
           break;
         }
-      } while (p.sb == p.sa);
+      }
       if (status != kStatusOk) break;
       c_draws += 3;
       ++c_steps;

@@ -30,6 +30,7 @@ result with a 1% NRMSE criterion), which is the comparison made here.
 from __future__ import annotations
 
 import math
+import time
 
 import numpy as np
 
@@ -292,7 +293,7 @@ def pre_sampling(W: WangLandauWalkers, wl, walkers_per_window: int, n_atoms: int
     histogram set to n_atoms + 1 once.  mc_steps (optional, per window)
     gets wl_mc_steps: every walker's trials until its own criterion held
     (:774-776).  Returns the sweeps() calls made."""
-    trials = wl.mc_sweeps * n_atoms
+    trials = wl.mc_sweeps * n_atoms if trials_per_call is None else int(trials_per_call)
     period = int(0.02 * float(np.float32(n_atoms)))
     nwin = wl.num_windows
     done = np.zeros(nwin, dtype=bool)
@@ -358,7 +359,8 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
                 exchange: bool = True, max_calls: int = 1_000_000, log=None, radial=None,
                 burn_in: str = "temperature", numbers=None, pre_sample: bool = False,
                 config_store: bool | None = None, optimise_windows: bool | None = None,
-                store_seed: int = 0) -> dict:
+                store_seed: int = 0, trials_per_call: int | None = None,
+                deadline_s: float | None = None) -> dict:
     """Runs the main loop to wl.tolerance.  wl: the wl_input fields
     (mc_sweeps, bins, num_windows, bin_overlap, tolerance, flatness, wl_f,
     energy_min, energy_max, performance).  radial (optional): dict(wc_range,
@@ -376,6 +378,10 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
     the walkers configurations inside their new windows.  The draws the
     reference takes from gfortran's random_number come from numpy's
     generator seeded with store_seed.
+
+    trials_per_call (default mc_sweeps * n_atoms) sets the trials of every
+    sweeps() call, i.e. the replica-exchange interval.  deadline_s stops the
+    main loop after that many seconds (wall clock) like max_calls does.
 
     Returns the combined ln g, the bin edges, the windows (the last ones)
     and every set used, the iteration record and, with radial samples,
@@ -429,7 +435,7 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
         W.radial_enable(radial["wc_range"], radial["shells"], radial["radial_samples"], walkers_per_window)
         rad_state["rho_saved"] = False
     f = float(wl.wl_f)
-    trials = wl.mc_sweeps * n_atoms
+    trials = wl.mc_sweeps * n_atoms if trials_per_call is None else int(trials_per_call)
     period = int(0.02 * float(np.float32(n_atoms)))
     pre_calls = 0
     nwin = wl.num_windows
@@ -458,7 +464,10 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
     record = []
     calls = 0
     lng = np.zeros(wl.bins)
+    t_start = time.perf_counter()
     while f > wl.tolerance and calls < max_calls:
+        if deadline_s is not None and time.perf_counter() - t_start > deadline_s:
+            break
         W.sweeps(trials, f, period)
         calls += 1
         for k in range(n):
@@ -482,7 +491,7 @@ def wang_landau(setup: Setup, V, conc, wl, walkers_per_window: int = 1, seed0: i
             if store:
                 load_window_config(W, windows, walkers_per_window, host_rng)
             it += 1
-            record.append({"calls": calls, "wl_f": f})
+            record.append({"calls": calls, "wl_f": f, "seconds": time.perf_counter() - t_start})
             if log:
                 log(f"ln f -> {f:.3e} after {calls} sweeps() calls")
     if radial is not None:

@@ -98,3 +98,27 @@ def test_nested_sampling_workload_shape_matches_oracle(case):
     if K < 2 * n_iter:
         # the walks were lengthened: more steps than n_iter * n_steps
         assert c["trials"] > n_iter * n_steps
+
+
+def test_nested_sampling_rare_species_redraws_match_oracle():
+    """A composition with a few atoms of one species (the mixed serving
+    stream's Dirichlet draws give such lattices): site 2 is redrawn many
+    times per step, and the warp tries ten redraws at once; the stream,
+    the walks and the ceilings must stay the oracle's bit for bit."""
+    lattice, n, ns, nsh, K, n_steps, n_iter, seed = "bcc", (4, 3, 5), 2, 3, 8, 30, 40, 41
+    rng = np.random.default_rng(seed)
+    V = random_V(rng, ns, nsh, 0.05)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    nums = np.array([setup.n_atoms - 3, 3], dtype=np.int64)
+    conc = np.concatenate([[0.0], nums / setup.n_atoms])
+    mod = O.OracleModel(lattice, *n, V)
+    r = O.OracleRng(seed)
+    limits_o, walkers_o, energies_o, _ = mod.ns_run(r, conc, nums, K, n_steps, n_iter)
+    run = dict(setup=setup, V=V, seed=seed, n_walkers=K, n_steps=n_steps,
+               species_concentrations=conc, species_numbers=nums)
+    nsg = B.NestedSampling([run])
+    lim = nsg.iterate(n_iter)[0]
+    assert np.array_equal(lim, limits_o)
+    assert np.array_equal(nsg.energies(0), energies_o)
+    for w in range(K):
+        assert np.array_equal(nsg.walker_config(0, w), walkers_o[w])

@@ -436,3 +436,67 @@ def test_wang_landau_store_merge_windows_match_oracle():
         assert O.wl_bin_index(mod0.total_energy(cfgs[k]), bin_edges, bins) == b
     check_all()
     run_calls(2)
+
+
+def test_wang_landau_divided_windows_exchange_match_oracle():
+    """The Wang-Landau workload's layout, reduced: bcc 6^3, 4 species, 4
+    shells, the bins of create_energy_bins split by divide_range into 8
+    windows extended by create_overlap (bin overlap 0.25), 4 walkers per
+    window placed in their windows by the driver's temperature search; then
+    cycles of sweeps() and replica exchange between adjacent windows, the
+    device against the oracle bit for bit (ln g, histograms, partners,
+    exchanges, configurations, streams)."""
+    from brawl_gb300 import wang_landau as WLD
+    lattice, n, ns, nsh, nwin, per_window, bins = "bcc", (6, 6, 6), 4, 4, 8, 4, 400
+    rng = np.random.default_rng(91)
+    V = random_V(rng, ns, nsh)
+    setup = B.Setup(lattice, *n, ns, nsh)
+    N = setup.n_atoms
+    conc = conc_vector(ns)
+    pilot = B.Batch([dict(setup=setup, V=V, seed=5 + k, beta=1.0 / (T * B.K_B_IN_RY),
+                          species_concentrations=conc) for k, T in enumerate([300.0, 1e12])])
+    pilot.metropolis(200 * N)
+    E = pilot.total_energy()
+    pilot.close()
+    to_mev = B.RY_TO_EV * 1000.0 / N
+    emin, emax = float(np.float32(E[0] * to_mev)), float(np.float32(E[1] * to_mev))
+    edges = WLD.create_energy_bins(N, emin, emax, bins)
+    windows = WLD.create_overlap(WLD.divide_range(bins, nwin), float(np.float32(0.25)))
+    starts, ends = [w[0] for w in windows], [w[1] for w in windows]
+    nw = nwin * per_window
+    seeds = [110179 + 11 * r for r in range(nw)]
+    targets = []
+    for r in range(nw):
+        s, e = windows[r // per_window]
+        lo_e, hi_e = edges[s - 1], edges[e]
+        c = abs(hi_e - lo_e) * 0.1
+        targets.append((lo_e + c, hi_e - c))
+    cfgs0, _ = WLD._burn_in(setup, V, [1000 + r for r in range(nw)], conc, targets, N)
+    walkers = [dict(setup=setup, V=V, seed=seeds[r], config=cfgs0[r], start_idx=starts[r // per_window],
+                    end_idx=ends[r // per_window], window=r // per_window) for r in range(nw)]
+    mods = [O.OracleModel(lattice, *n, V) for _ in walkers]
+    cfgs = [w["config"].copy() for w in walkers]
+    rngs = [O.OracleRng(w["seed"]) for w in walkers]
+    lngs = [np.zeros(bins) for _ in walkers]
+    hists = [np.zeros(w["end_idx"] - w["start_idx"] + 1) for w in walkers]
+    wl = B.WangLandauWalkers(walkers, edges)
+    period = int(0.02 * float(np.float32(N)))
+    attempted = 0
+    for cycle in range(4):
+        acc_o = _emulate(mods, cfgs, rngs, walkers, edges, lngs, hists, 1000, 1.0, period)
+        assert list(wl.sweeps(1000, 1.0, period)) == acc_o
+        Es = [mods[k].total_energy(cfgs[k]) for k in range(nw)]
+        na_o, partner_o, exch_o = O.wl_replica_exchange(starts, ends, per_window, edges, Es, lngs,
+                                                        rngs, cfgs)
+        na_g, partner_g, exch_g = wl.replica_exchange()
+        assert na_g == na_o
+        assert np.array_equal(partner_g, partner_o)
+        assert np.array_equal(exch_g, exch_o)
+        attempted += int((partner_o >= 0).sum())
+        for k in range(nw):
+            assert np.array_equal(wl.config(k), cfgs[k])
+            assert np.array_equal(wl.lng(k), lngs[k])
+            assert np.array_equal(wl.hist(k), hists[k])
+    assert attempted > 0
+    for k in range(nw):
+        assert np.array_equal(wl.genrand(k, 8), np.array([rngs[k].uniform() for _ in range(8)]))
