@@ -293,7 +293,7 @@ def pre_sampling(W: WangLandauWalkers, wl, walkers_per_window: int, n_atoms: int
     histogram set to n_atoms + 1 once.  mc_steps (optional, per window)
     gets wl_mc_steps: every walker's trials until its own criterion held
     (:774-776).  Returns the sweeps() calls made."""
-    trials = wl.mc_sweeps * n_atoms if trials_per_call is None else int(trials_per_call)
+    trials = wl.mc_sweeps * n_atoms
     period = int(0.02 * float(np.float32(n_atoms)))
     nwin = wl.num_windows
     done = np.zeros(nwin, dtype=bool)
