@@ -210,6 +210,49 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def smem_bandwidth_gbs() -> float | None:
+    """The device's shared-memory bandwidth (GB/s) from the library's own
+    streaming-load kernel, measured outside every timed region."""
+    import ctypes as C
+    import brawl_gb300 as B
+    v = C.c_double(0.0)
+    try:
+        rc = B.load().brawl_smem_bandwidth(C.byref(v))
+    except Exception:
+        return None
+    return v.value / 1e9 if rc == 0 and v.value > 0 else None
+
+
+def committed_smem() -> dict | None:
+    """Shared-memory bytes and issue activity of the Metropolis kernel from
+    the committed ncu summary (profiles/metropolis_batched_smem.json)."""
+    p = os.path.join(ROOT, "profiles", "metropolis_batched_smem.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def roofline_object(achieved_gbs, smem_peak, peaks, traffic, alg_per_step) -> dict:
+    """The Metropolis kernel against the ceiling that bounds it: its bytes
+    are served from shared memory (DRAM traffic per launch is the lattices'
+    staging only), so the peak is the measured shared-memory bandwidth; the
+    HBM copy rate is given beside it."""
+    out = {"bound": "smem", "achieved": achieved_gbs, "unit": "GB/s",
+           "peak": smem_peak, "frac": (achieved_gbs / smem_peak) if smem_peak else None,
+           "peak_source": "measured in this run (brawl_smem_bandwidth)",
+           "traffic": traffic, "algorithmic_bytes_per_step": alg_per_step,
+           "hbm": {"peak": peaks["hbm_gbs"], "frac": achieved_gbs / peaks["hbm_gbs"],
+                   "peak_source": peaks["source"]},
+           "note": "latency-bound sequential chains (one warp per chain, a dependent chain of "
+                   "shared loads, a warp reduction and a decision per trial); achieved = the "
+                   "canonical algorithmic bytes per trial over the kernel's event time"}
+    cs = committed_smem()
+    if cs:
+        out["ncu"] = cs
+    return out
+
+
 def committed_traffic() -> dict | None:
     """DRAM traffic per launch of the Metropolis kernel on the 1024-replica
     workload, from the committed ncu summary
@@ -855,6 +898,7 @@ def main() -> int:
     alg_bytes = 2 * T_all + (2 + 2 * z + 32 * z) * T_eval + 4 * draws
     achieved_gbs = alg_bytes / dev_s / 1e9
     peaks = measured_peaks()
+    smem_peak = smem_bandwidth_gbs()
     traffic = None
     tr = committed_traffic()
     if tr and tr.get("dram_bytes_per_launch") and args.replicas == 1024:
@@ -927,12 +971,8 @@ def main() -> int:
                        "parallelism": f"replicas x{world}", "cta_shape": cta_shape},
             "e2e": {"value": e2e_value, "unit": "trials/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
-            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
-                         "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
-                         "traffic": traffic, "peak_source": peaks["source"],
-                         "algorithmic_bytes_per_step": alg_bytes / args.steps,
-                         "note": "latency-bound sequential chains; bytes are the canonical "
-                                 "algorithmic bytes per trial, mostly served from shared memory"},
+            "roofline": roofline_object(achieved_gbs, smem_peak, peaks, traffic,
+                                        alg_bytes / args.steps),
             "cpu_baseline": cpu,
             "plain_gpu": {"value": plain_value, "unit": "trials/s",
                           "sample": f"{len(sample)} replicas, 1 sweep each, one launch per replica"},

@@ -132,6 +132,12 @@ int brawl_alro_reset(brawl_ctx *ctx);
 /* Cumulative counters of this chain (BRAWL_NUM_COUNTERS values). */
 int brawl_counters(brawl_ctx *ctx, int64_t *counters);
 
+/* No counterpart in the reference.  The shared-memory bandwidth of the
+ * current device in bytes/s (a streaming 16-byte-load kernel on every SM,
+ * the best of three timed launches): the ceiling the sampling kernels,
+ * whose lattices and tables live in shared memory, are measured against. */
+int brawl_smem_bandwidth(double *bytes_per_s);
+
 /* No counterpart in the reference.  The total energy of brawl_total_energy,
  * bit-identical, for callers that cannot allocate device memory -- a host
  * that gives all device memory to its own pool at start-up, or one that
