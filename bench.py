@@ -604,9 +604,9 @@ def _wl_windows_run(args, setup, V, conc) -> dict:
     sweeps() calls of 10^4 trials per walker with replica exchange between
     adjacent windows after every call, the in-window averages and
     dos_combine at every halving.  The energy range (meV/atom) runs from the
-    lowest energy of a pilot anneal (8 chains, 300 K, 300 sweeps) to the
-    highest of 128 random configurations; the walkers enter their windows
-    by the temperature search.  The run is bounded by args.wl_seconds; the
+    mean energy of a pilot anneal (8 chains, 300 K, 300 sweeps) to the mean
+    of 128 random configurations (the energies the temperature search that
+    places the walkers in their windows can reach).  The run is bounded by args.wl_seconds; the
     time to ln f < 1e-6 (20 halvings) is extrapolated from the halvings
     reached: the sweeps() calls per halving are fitted as c_k = a r^k on
     the measured ones (least squares on log c_k) and the remaining
@@ -619,11 +619,11 @@ def _wl_windows_run(args, setup, V, conc) -> dict:
     pilot = B.Batch([dict(setup=setup, V=V, seed=31 + k, beta=1.0 / (300.0 * B.K_B_IN_RY),
                           species_concentrations=conc) for k in range(8)])
     pilot.metropolis(300 * N)
-    e_lo = float(pilot.total_energy().min())
+    e_lo = float(pilot.total_energy().mean())
     pilot.close()
     rnd = B.Batch([dict(setup=setup, V=V, seed=1000 + k, beta=0.0, species_concentrations=conc)
                    for k in range(128)])
-    e_hi = float(rnd.total_energy().max())
+    e_hi = float(rnd.total_energy().mean())
     rnd.close()
     to_mev = B.RY_TO_EV * 1000.0 / N
     p = I.WLParams(mc_sweeps=0, bins=32000, num_windows=32, bin_overlap=float(np.float32(0.25)),
