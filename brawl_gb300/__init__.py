@@ -166,6 +166,12 @@ def load(rebuild: bool = False):
         "brawl_batch_alro_get": ([vp, i, vp], i),
         "brawl_batch_alro_reset": ([vp], i),
         "brawl_batch_radial_densities": ([vp, i, i, vp, vp], i),
+        "brawl_batch_sampling_reset": ([vp, i], i),
+        "brawl_batch_energy_sample": ([vp, vp], i),
+        "brawl_batch_asro_sample": ([vp, i, vp, vp], i),
+        "brawl_batch_temperature_stats": ([vp, i64, i64, d, d, i, vp, vp], i),
+        "brawl_batch_asro_stats": ([vp, i64, vp, vp], i),
+        "brawl_smem_bandwidth": ([vp], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -515,6 +521,47 @@ class Batch:
         out = np.zeros(wc_range, dtype=np.float64)
         _check(load().brawl_batch_lattice_shells(self._h, c, wc_range, _ptr(out)))
         return out
+
+    # -- sampling sums of the annealing loop, on the device ---------------------
+    def sampling_reset(self, wc_range: int = 0) -> None:
+        """Zero every chain's E, E^2 (and, wc_range >= 1, radial-density)
+        sums and note the accepted counts: the start of a sampling loop."""
+        self._samp_wc = int(wc_range)
+        _check(load().brawl_batch_sampling_reset(self._h, int(wc_range)))
+
+    def energy_sample(self, energies: bool = True) -> np.ndarray | None:
+        """Every chain's total_energy added to its sums; returns them."""
+        out = np.zeros(self.n, dtype=np.float64) if energies else None
+        _check(load().brawl_batch_energy_sample(self._h, None if out is None else _ptr(out)))
+        return out
+
+    def asro_sample(self, c: int, shells, rho: bool = True) -> np.ndarray | None:
+        """Chain c's radial_densities added to its sums; returns them."""
+        shells = np.ascontiguousarray(shells, dtype=np.float64)
+        ns = self.setups[c].n_species
+        out = np.zeros((shells.shape[0], ns, ns), dtype=np.float64) if rho else None
+        _check(load().brawl_batch_asro_sample(self._h, c, _ptr(shells), None if out is None else _ptr(out)))
+        return out
+
+    def temperature_stats(self, n_save_energy: int, n_mc_steps: int, temp: float, sim_temp: float,
+                          with_energies: bool = True):
+        """(per-chain energies_of_T, C_of_T, acceptance_of_T; their averages
+        over the chains), formed on the device."""
+        per = np.zeros(3 * self.n, dtype=np.float64)
+        av = np.zeros(3, dtype=np.float64)
+        _check(load().brawl_batch_temperature_stats(self._h, int(n_save_energy), int(n_mc_steps), float(temp),
+                                                    float(sim_temp), int(bool(with_energies)), _ptr(per),
+                                                    _ptr(av)))
+        return per.reshape(3, self.n), av
+
+    def asro_stats(self, n_save_asro: int):
+        """(per-chain rho_of_T (n, wc, ns, ns), its average over the chains)."""
+        ns = self.setups[0].n_species
+        wc = self._samp_wc
+        per = np.zeros((self.n, wc, ns, ns), dtype=np.float64)
+        av = np.zeros((wc, ns, ns), dtype=np.float64)
+        _check(load().brawl_batch_asro_stats(self._h, int(n_save_asro), _ptr(per), _ptr(av)))
+        return per, av
 
     # -- ALRO (store_state) of every chain --------------------------------------
     def alro_add(self) -> None:

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbrawl_gpu.so")
 SOURCES = ["metropolis.cu", "metropolis_halo.cu", "metropolis_spec.cu", "lattice_ops.cu", "asro.cu", "capi.cu", "noalloc.cu", "nested_sampling.cu", "wang_landau.cu", "server.cu",
-           "peaks.cu"]
+           "peaks.cu", "sampling.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]

@@ -364,6 +364,19 @@ struct brawl_batch {
   double* d_alro = nullptr;              // ALRO counts: per chain ns x n_sites
   int64_t* d_alro_off = nullptr;
   std::vector<int64_t> alro_off;
+  // sampling sums of the annealing loop (sampling.cu): one block holding
+  // step_E and step_Esq (2n), the accepted counts at the loop's start (n),
+  // n_atoms (n), the temperature's statistics (3n + 3), then the radial
+  // densities' sums (n m) and statistics ((n + 1) m), m = wc ns^2
+  unsigned char* d_samp = nullptr;
+  int samp_wc = -1;                      // wc_range the block was laid out for
+  double* d_sums = nullptr;
+  unsigned long long* d_acc0 = nullptr;
+  double* d_natoms = nullptr;
+  double* d_tstats = nullptr;
+  double* d_rho_sum = nullptr;
+  double* d_rho_stats = nullptr;
+  unsigned long long* d_mask = nullptr;  // ASRO class masks (64)
 };
 
 struct brawl_ctx {
@@ -710,7 +723,7 @@ int brawl_batch_destroy(brawl_batch* b) {
   if (b->stream) {
     for (const void* p : {(const void*)b->arena, (const void*)b->d_site_e, (const void*)b->d_grid,
                           (const void*)b->d_grids, (const void*)b->d_gjobs, (const void*)b->d_scratch,
-                          (const void*)b->d_alro, (const void*)b->d_alro_off})
+                          (const void*)b->d_alro, (const void*)b->d_alro_off, (const void*)b->d_samp})
       dfree(p, b->stream);
     cudaStreamSynchronize(b->stream);
     cudaStreamDestroy(b->stream);
@@ -1030,12 +1043,11 @@ int brawl_batch_counters(brawl_batch* b, int64_t* counters) {
   return BRAWL_OK;
 }
 
-int brawl_batch_radial_densities(brawl_batch* b, int c, int wc_range, const double* shells,
-                                 double* rho) {
-  if (!b || !shells || !rho || c < 0 || c >= (int)b->jobs.size() || wc_range < 1 || wc_range > 64)
-    return fail(BRAWL_EINVAL, "bad argument");
+// The ASRO pair counts of chain c queued on the batch's stream; *d_counts
+// receives their device address (in the batch's scratch).
+static int queue_asro_counts(brawl_batch* b, int c, int wc_range, const double* shells, AsroPlan& plan,
+                             unsigned long long** d_counts) {
   const Geom& g = b->models[c].g;
-  AsroPlan plan;
   TRY(make_asro_plan(g, wc_range, shells, plan) == 0 ? BRAWL_OK
                                                      : fail(BRAWL_EINVAL, "bad ASRO plan"));
   const int nsp = g.ns + 1;
@@ -1066,10 +1078,140 @@ int brawl_batch_radial_densities(brawl_batch* b, int c, int wc_range, const doub
   CUDA_TRY(cudaMemcpyAsync(b->d_ajob, &aj, sizeof(aj), cudaMemcpyHostToDevice, b->stream));
   launch_asro(b->d_ajob, g, plan.n_class, b->stream);
   CUDA_TRY(cudaGetLastError());
+  *d_counts = d_cnt;
+  return BRAWL_OK;
+}
+
+int brawl_batch_radial_densities(brawl_batch* b, int c, int wc_range, const double* shells,
+                                 double* rho) {
+  if (!b || !shells || !rho || c < 0 || c >= (int)b->jobs.size() || wc_range < 1 || wc_range > 64)
+    return fail(BRAWL_EINVAL, "bad argument");
+  const Geom& g = b->models[c].g;
+  AsroPlan plan;
+  unsigned long long* d_cnt = nullptr;
+  TRY(queue_asro_counts(b, c, wc_range, shells, plan, &d_cnt));
+  const int nsp = g.ns + 1;
+  const size_t n_counts = (size_t)nsp * nsp * plan.n_class + nsp;
   std::vector<unsigned long long> cnt(n_counts);
   CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_cnt, n_counts * 8, cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   finish_asro(g, wc_range, plan, cnt.data(), rho);
+  return BRAWL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Sampling reductions of the annealing loop (sampling.cu)
+// ---------------------------------------------------------------------------
+// The sampling block, laid out for wc_range (0: no radial densities); every
+// chain must have the same species count when wc_range > 0.
+static int ensure_sampling(brawl_batch* b, int wc_range) {
+  const int n = (int)b->jobs.size();
+  if (b->d_samp && b->samp_wc == wc_range) return BRAWL_OK;
+  int ns = b->models[0].g.ns;
+  if (wc_range > 0)
+    for (int c = 1; c < n; ++c)
+      if (b->models[c].g.ns != ns) return fail(BRAWL_EINVAL, "radial-density sums need equal species counts");
+  const size_t m = wc_range > 0 ? (size_t)wc_range * ns * ns : 0;
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t o_sums = 0, o_acc0 = al(o_sums + 2 * n * 8), o_nat = al(o_acc0 + n * 8),
+               o_t = al(o_nat + n * 8), o_rs = al(o_t + (3 * n + 3) * 8), o_rst = al(o_rs + n * m * 8),
+               o_mask = al(o_rst + (n + 1) * m * 8), total = al(o_mask + 64 * 8);
+  dfree(b->d_samp, b->stream);
+  b->d_samp = nullptr;
+  CUDA_TRY(dalloc(&b->d_samp, total, b->stream));
+  b->samp_wc = wc_range;
+  b->d_sums = reinterpret_cast<double*>(b->d_samp + o_sums);
+  b->d_acc0 = reinterpret_cast<unsigned long long*>(b->d_samp + o_acc0);
+  b->d_natoms = reinterpret_cast<double*>(b->d_samp + o_nat);
+  b->d_tstats = reinterpret_cast<double*>(b->d_samp + o_t);
+  b->d_rho_sum = reinterpret_cast<double*>(b->d_samp + o_rs);
+  b->d_rho_stats = reinterpret_cast<double*>(b->d_samp + o_rst);
+  b->d_mask = reinterpret_cast<unsigned long long*>(b->d_samp + o_mask);
+  std::vector<double> nat(n);
+  for (int c = 0; c < n; ++c) nat[c] = (double)b->models[c].g.n_sites;
+  CUDA_TRY(cudaMemcpyAsync(b->d_natoms, nat.data(), n * 8, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaMemsetAsync(b->d_samp, 0, o_nat, b->stream));
+  if (m) CUDA_TRY(cudaMemsetAsync(b->d_rho_sum, 0, n * m * 8, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_sampling_reset(brawl_batch* b, int wc_range) {
+  if (!b || wc_range < 0 || wc_range > 64) return fail(BRAWL_EINVAL, "bad argument");
+  TRY(ensure_sampling(b, wc_range));
+  const int n = (int)b->jobs.size();
+  const size_t m = wc_range > 0 ? (size_t)wc_range * b->models[0].g.ns * b->models[0].g.ns : 0;
+  CUDA_TRY(cudaMemsetAsync(b->d_sums, 0, 2 * n * 8, b->stream));
+  if (m) CUDA_TRY(cudaMemsetAsync(b->d_rho_sum, 0, n * m * 8, b->stream));
+  launch_acceptance_snapshot(b->d_counters, b->d_acc0, n, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_energy_sample(brawl_batch* b, double* energies) {
+  if (!b) return fail(BRAWL_EINVAL, "null argument");
+  if (!b->d_samp) return fail(BRAWL_EINVAL, "brawl_batch_sampling_reset first");
+  const int n = (int)b->jobs.size();
+  TRY(queue_batch_energy(b));
+  launch_energy_accumulate(b->d_energy, b->d_sums, n, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  if (energies)
+    CUDA_TRY(cudaMemcpyAsync(energies, b->d_energy, n * 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_asro_sample(brawl_batch* b, int c, const double* shells, double* rho) {
+  if (!b || !shells || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad argument");
+  if (!b->d_samp || b->samp_wc < 1)
+    return fail(BRAWL_EINVAL, "brawl_batch_sampling_reset with wc_range >= 1 first");
+  const Geom& g = b->models[c].g;
+  const int wc = b->samp_wc;
+  const size_t m = (size_t)wc * g.ns * g.ns;
+  AsroPlan plan;
+  unsigned long long* d_cnt = nullptr;
+  TRY(queue_asro_counts(b, c, wc, shells, plan, &d_cnt));
+  if (plan.n_class > 64) return fail(BRAWL_EINVAL, "too many ASRO offset classes");
+  CUDA_TRY(cudaMemcpyAsync(b->d_mask, plan.class_mask.data(), plan.class_mask.size() * 8,
+                           cudaMemcpyHostToDevice, b->stream));
+  double* rho_out = b->d_rho_stats;  // staging for this sample
+  launch_asro_finish(d_cnt, b->d_mask, plan.n_class, g.ns, wc, rho ? rho_out : nullptr,
+                     b->d_rho_sum + (size_t)c * m, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  if (rho) CUDA_TRY(cudaMemcpyAsync(rho, rho_out, m * 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_temperature_stats(brawl_batch* b, int64_t n_save_energy, int64_t n_mc_steps, double temp,
+                                  double sim_temp, int with_energies, double* per_chain, double* average) {
+  if (!b || !per_chain || !average || n_mc_steps < 1 || (with_energies && n_save_energy < 1))
+    return fail(BRAWL_EINVAL, "bad argument");
+  if (!b->d_samp) return fail(BRAWL_EINVAL, "brawl_batch_sampling_reset first");
+  const int n = (int)b->jobs.size();
+  launch_temperature_stats(n, b->d_sums, b->d_counters, b->d_acc0, b->d_natoms, (double)n_save_energy,
+                           sim_temp, temp, (double)(float)n_mc_steps, with_energies ? 1 : 0, b->d_tstats,
+                           b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(per_chain, b->d_tstats, 3 * n * 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(average, b->d_tstats + 3 * n, 3 * 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_asro_stats(brawl_batch* b, int64_t n_save_asro, double* per_chain, double* average) {
+  if (!b || !per_chain || !average || n_save_asro < 1) return fail(BRAWL_EINVAL, "bad argument");
+  if (!b->d_samp || b->samp_wc < 1)
+    return fail(BRAWL_EINVAL, "brawl_batch_sampling_reset with wc_range >= 1 first");
+  const int n = (int)b->jobs.size();
+  const int m = b->samp_wc * b->models[0].g.ns * b->models[0].g.ns;
+  launch_asro_stats(n, m, b->d_rho_sum, (double)n_save_asro, b->d_rho_stats, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(per_chain, b->d_rho_stats, (size_t)n * m * 8, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(average, b->d_rho_stats + (size_t)n * m, (size_t)m * 8, cudaMemcpyDeviceToHost,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
   return BRAWL_OK;
 }
 

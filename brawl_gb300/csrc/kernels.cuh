@@ -120,6 +120,18 @@ __host__ __device__ inline HaloLayout halo_layout(const Geom& g, const HaloGeom&
 
 int lane_entries_for(int max_z);
 
+// Sampling reductions of the annealing loop on the device (sampling.cu).
+void launch_energy_accumulate(const double* d_e, double* d_sums, int n, cudaStream_t s);
+void launch_acceptance_snapshot(const unsigned long long* d_counters, unsigned long long* d_acc0, int n,
+                                cudaStream_t s);
+void launch_asro_finish(const unsigned long long* d_counts, const unsigned long long* d_mask, int n_class,
+                        int ns, int wc, double* d_rho_out, double* d_rho_sum, cudaStream_t s);
+void launch_temperature_stats(int n, const double* d_sums, const unsigned long long* d_counters,
+                              const unsigned long long* d_acc0, const double* d_n_atoms, double n_save,
+                              double sim_temp, double temp, double n_mc_real, int with_energies,
+                              double* d_out, cudaStream_t s);
+void launch_asro_stats(int n, int m, const double* d_rho_sum, double n_save, double* d_out, cudaStream_t s);
+
 // Load the code of every kernel variant a translation unit launches (module
 // loading is lazy by default; a launch that first loads code waits for the
 // kernels already running on the device).

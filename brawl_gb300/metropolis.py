@@ -160,13 +160,17 @@ def simulated_annealing_ensemble(batch: Batch, metropolis, wc_range: int, record
     sweep block one launch for all chains.  Each chain's outputs are what
     simulated_annealing gives for it alone; "average" holds the ensemble
     averages of comms_reduce_metropolis_results: the rank sum in rank order
-    divided by real(p)."""
+    divided by real(p).  The sampling reductions run on the device
+    (brawl_batch_sampling_reset / energy_sample / asro_sample /
+    temperature_stats / asro_stats): the E and E^2 sums, the radial-density
+    sums, the per-temperature energies, heat capacities, acceptance rates and
+    radial densities and their averages over the chains; the host only
+    collects the trajectory rows and the results."""
     m = metropolis
     n = batch.n
     if any(b != bool(m.nbr_swap) for b in batch.nbr_swap):
         raise ValueError("the batch's chains must be created with nbr_swap = metropolis.nbr_swap")
     ns = batch.setups[0].n_species
-    n_atoms = np.array([s.n_atoms for s in batch.setups], dtype=np.float64)
     shells = [batch.lattice_shells(c, wc_range) for c in range(n)]
     n_save_energy = _f32_floor_div(m.n_mc_steps, m.n_sample_steps)
     n_save_asro = _f32_floor_div(m.n_mc_steps, m.n_sample_steps_asro)
@@ -180,11 +184,14 @@ def simulated_annealing_ensemble(batch: Batch, metropolis, wc_range: int, record
         "initial_configs": [], "final_configs": [],
         "order_of_T": (np.zeros((Ts,) + batch.setups[c].grid_shape + (1, ns)) if m.calculate_alro else None),
     } for c in range(n)]
+    av = {"acceptance_of_T": np.zeros(Ts)}
+    if m.calculate_energies:
+        av["energies_of_T"] = np.zeros(Ts)
+        av["C_of_T"] = np.zeros(Ts)
+    if m.calculate_asro:
+        av["rho_of_T"] = np.zeros((Ts, wc_range, ns, ns))
     asro = [np.zeros((wc_range, ns, ns)) for _ in range(n)]
     for j in range(Ts):
-        r_dens = [np.zeros((wc_range, ns, ns)) for _ in range(n)]
-        step_E = np.zeros(n)
-        step_Esq = np.zeros(n)
         temp = m.T + float(j) * m.delta_T
         sim_temp = temp * K_B_IN_RY
         beta = 1.0 / sim_temp if sim_temp != 0.0 else float("inf")
@@ -194,6 +201,7 @@ def simulated_annealing_ensemble(batch: Batch, metropolis, wc_range: int, record
         burn = m.burn_in_start if j == 0 else m.burn_in
         if burn and m.n_burn_in_steps > 0:
             batch.metropolis(m.n_burn_in_steps)
+        batch.sampling_reset(wc_range if m.calculate_asro else 0)
         energy = batch.total_energy() if m.calculate_energies else np.zeros(n)
         if m.calculate_asro:
             asro = [batch.radial_densities(c, shells[c]) for c in range(n)]
@@ -207,17 +215,13 @@ def simulated_annealing_ensemble(batch: Batch, metropolis, wc_range: int, record
                 o["initial_configs"].append(batch.config(c))
         n_sweeps = m.n_mc_steps // m.n_sample_steps
         n_sweep_steps = m.n_mc_steps // n_sweeps
-        accepted = np.zeros(n, dtype=np.int64)
         for i in range(1, n_sweeps + 1):
-            accepted += batch.metropolis(n_sweep_steps)
+            batch.metropolis(n_sweep_steps)
             step_n = i * n_sweep_steps
             if m.calculate_energies:
-                energy = batch.total_energy()
-                step_E = step_E + energy
-                step_Esq = step_Esq + energy * energy
+                energy = batch.energy_sample()
             if m.calculate_asro and step_n % m.n_sample_steps_asro == 0:
-                asro = [batch.radial_densities(c, shells[c]) for c in range(n)]
-                r_dens = [r + a for r, a in zip(r_dens, asro)]
+                asro = [batch.asro_sample(c, shells[c]) for c in range(n)]
             if m.calculate_alro and step_n % m.n_sample_steps_alro == 0:
                 batch.alro_add()
             if step_n % m.n_sample_steps_trajectory == 0:
@@ -225,19 +229,23 @@ def simulated_annealing_ensemble(batch: Batch, metropolis, wc_range: int, record
                     outs[c]["traj_step"].append(step_n)
                     outs[c]["traj_energy"].append(energy[c])
                     outs[c]["traj_asro"].append(asro[c].copy())
+        per, avT = batch.temperature_stats(n_save_energy if m.calculate_energies else 1, m.n_mc_steps,
+                                           temp, sim_temp, bool(m.calculate_energies))
+        av["acceptance_of_T"][j] = avT[2]
+        if m.calculate_energies:
+            av["energies_of_T"][j] = avT[0]
+            av["C_of_T"][j] = avT[1]
+        if m.calculate_asro:
+            rho_c, rho_av = batch.asro_stats(n_save_asro)
+            av["rho_of_T"][j] = rho_av
         for c in range(n):
             o = outs[c]
-            o["acceptance_of_T"][j] = float(accepted[c]) / float(np.float32(m.n_mc_steps))
+            o["acceptance_of_T"][j] = per[2][c]
             if m.calculate_energies:
-                ne = float(n_save_energy)
-                o["energies_of_T"][j] = step_E[c] / ne / n_atoms[c]
-                mean = step_E[c] / ne
-                C = (step_Esq[c] / ne - mean * mean) / (sim_temp * temp) / n_atoms[c]
-                if C < 0.0 or temp <= 0.0:
-                    C = 0.0
-                o["C_of_T"][j] = C
+                o["energies_of_T"][j] = per[0][c]
+                o["C_of_T"][j] = per[1][c]
             if m.calculate_asro:
-                o["rho_of_T"][j] = r_dens[c] / float(n_save_asro)
+                o["rho_of_T"][j] = rho_c[c]
             if m.calculate_alro:
                 o["order_of_T"][j] = batch.alro(c) / float(np.float32(n_save_alro))
             if record_configs:
@@ -246,13 +254,4 @@ def simulated_annealing_ensemble(batch: Batch, metropolis, wc_range: int, record
         o["traj_step"] = np.array(o["traj_step"], dtype=np.int64)
         o["traj_energy"] = np.array(o["traj_energy"])
         o["traj_asro"] = np.array(o["traj_asro"])
-    p = float(np.float32(n))
-    av = {}
-    keys = ["acceptance_of_T"] + (["energies_of_T", "C_of_T"] if m.calculate_energies else []) + \
-        (["rho_of_T"] if m.calculate_asro else [])
-    for k in keys:
-        s = outs[0][k]
-        for o in outs[1:]:
-            s = s + o[k]
-        av[k] = s / p
     return {"ranks": outs, "average": av}

@@ -208,6 +208,33 @@ int brawl_batch_set_config(brawl_batch *batch, int chain, const int8_t *config);
  * concatenated in chain order (the host side of the ensemble). */
 int brawl_batch_get_configs(brawl_batch *batch, int8_t *configs);
 int brawl_batch_set_configs(brawl_batch *batch, const int8_t *configs);
+/* Sampling sums of metropolis_simulated_annealing kept on the device for
+ * every chain (src/metropolis.F90:360-430): the FP64 sums step_E and
+ * step_Esq of the sampled total energies, the sums r_densities of the
+ * sampled radial densities (wc_range >= 1; every chain must then have the
+ * same species count) and the accepted count at the start of the sampling
+ * loop.  brawl_batch_sampling_reset zeroes them (call it after a
+ * temperature's burn-in); brawl_batch_energy_sample adds every chain's
+ * total_energy (returned in energies[n] when not NULL, for trajectories);
+ * brawl_batch_asro_sample adds chain c's radial_densities (rho, optional,
+ * gets them in the layout of brawl_batch_radial_densities). */
+int brawl_batch_sampling_reset(brawl_batch *batch, int wc_range);
+int brawl_batch_energy_sample(brawl_batch *batch, double *energies);
+int brawl_batch_asro_sample(brawl_batch *batch, int chain, const double *shells, double *rho);
+/* The temperature's results (src/metropolis.F90:410-428): per_chain[3n] =
+ * energies_of_T (n), C_of_T (n), acceptance_of_T (n), computed on the
+ * device from the sums with the reference's arithmetic; average[3] = each
+ * summed over the chains in chain order and divided by real(n), as
+ * comms_reduce_metropolis_results averages the ranks (src/comms.F90:
+ * 122-160).  with_energies = 0: energies_of_T and C_of_T are 0. */
+int brawl_batch_temperature_stats(brawl_batch *batch, int64_t n_save_energy, int64_t n_mc_steps,
+                                  double temp, double sim_temp, int with_energies,
+                                  double *per_chain, double *average);
+/* rho_of_T = r_densities / n_save_asro per chain (per_chain[n * wc*ns*ns])
+ * and its average over the chains (average[wc*ns*ns]), as above. */
+int brawl_batch_asro_stats(brawl_batch *batch, int64_t n_save_asro, double *per_chain,
+                           double *average);
+
 /* set_configs, metropolis_run and get_configs as one call from host
  * buffers (every chain's grid, as set_configs takes them; configs_out may be
  * configs_in): page-locked buffers are read and written in place by the
