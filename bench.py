@@ -233,7 +233,7 @@ def committed_smem() -> dict | None:
     return None
 
 
-def roofline_object(achieved_gbs, smem_peak, peaks, traffic, alg_per_step) -> dict:
+def roofline_object(achieved_gbs, smem_peak, peaks, traffic, alg_per_step, trials_per_s) -> dict:
     """The Metropolis kernel against the ceiling that bounds it: its bytes
     are served from shared memory (DRAM traffic per launch is the lattices'
     staging only), so the peak is the measured shared-memory bandwidth; the
@@ -250,6 +250,12 @@ def roofline_object(achieved_gbs, smem_peak, peaks, traffic, alg_per_step) -> di
     cs = committed_smem()
     if cs:
         out["ncu"] = cs
+        # the shared-memory bytes the kernel moves per trial (ncu wavefronts
+        # of the committed capture) at this run's rate, against the ceiling
+        bpt = cs["smem_wavefronts_per_trial"] * cs["bytes_per_wavefront"]
+        gbs = bpt * trials_per_s / 1e9
+        out["smem_traffic"] = {"bytes_per_trial": bpt, "achieved": gbs, "unit": "GB/s",
+                               "frac": (gbs / smem_peak) if smem_peak else None}
     return out
 
 
@@ -972,7 +978,7 @@ def main() -> int:
             "e2e": {"value": e2e_value, "unit": "trials/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "roofline": roofline_object(achieved_gbs, smem_peak, peaks, traffic,
-                                        alg_bytes / args.steps),
+                                        alg_bytes / args.steps, T_all / dev_s),
             "cpu_baseline": cpu,
             "plain_gpu": {"value": plain_value, "unit": "trials/s",
                           "sample": f"{len(sample)} replicas, 1 sweep each, one launch per replica"},
