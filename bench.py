@@ -849,12 +849,14 @@ def main() -> int:
         cta_shape = {"trials_per_round": args.speculation, "picked_by": "--speculation"}
     else:
         # the CTA shape by measurement, before the warm-up and outside every
-        # timed region: one step's trials at each trials-per-round depth from
-        # the same state, which the library restores after each
+        # timed region: per class of chains (lattice, L, species, shells),
+        # each in its own launch with its own shared memory, the trials per
+        # round from one sweep of every chain at each depth, from the same
+        # state, which the library restores after each try
         try:
-            depth, ms = batch.autotune(trials, max_depth=4)
-            cta_shape = {"trials_per_round": int(depth), "picked_by": "autotune",
-                         "ms_per_depth": [round(float(x), 2) for x in ms]}
+            tuned = batch.autotune_classes(sites, max_depth=4)
+            cta_shape = {"picked_by": "autotune per chain class (whole-batch time, median of 3)",
+                         "tuning_sample": "one sweep of every chain", **tuned}
         except Exception as exc:  # keep one warp per chain and say why
             batch.set_speculation(1)
             cta_shape = {"trials_per_round": 1, "picked_by": "default", "autotune_error": str(exc)[:200]}

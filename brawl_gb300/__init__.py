@@ -172,6 +172,9 @@ def load(rebuild: bool = False):
         "brawl_batch_temperature_stats": ([vp, i64, i64, d, d, i, vp, vp], i),
         "brawl_batch_asro_stats": ([vp, i64, vp, vp], i),
         "brawl_smem_bandwidth": ([vp], i),
+        "brawl_batch_autotune_classes": ([vp, vp, i, vp, vp, vp], i),
+        "brawl_batch_chain_classes": ([vp, vp], i),
+        "brawl_batch_set_class_depths": ([vp, vp], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -432,6 +435,38 @@ class Batch:
         chosen = C.c_int()
         _check(load().brawl_batch_autotune(self._h, _ptr(t), int(max_depth), _ptr(ms), C.byref(chosen)))
         return chosen.value, ms
+
+    def autotune_classes(self, n_trials, max_depth: int = 4) -> dict:
+        """Trials per round picked per class of shared-memory chains (see
+        brawl_batch_autotune_classes); returns per class its chains'
+        lattice, L, species, shells, chain count, depth and ms per depth."""
+        t = self._trials(n_trials)
+        cls = np.zeros(self.n, dtype=np.int32)
+        _check(load().brawl_batch_chain_classes(self._h, _ptr(cls)))
+        nk = int(cls.max()) + 1 if (cls >= 0).any() else 0
+        depths = np.zeros(max(nk, 1), dtype=np.int32)
+        ms = np.zeros(max(nk, 1) * int(max_depth), dtype=np.float64)
+        n = C.c_int()
+        _check(load().brawl_batch_autotune_classes(self._h, _ptr(t), int(max_depth), _ptr(depths), _ptr(ms),
+                                                   C.byref(n)))
+        out = []
+        for k in range(n.value):
+            c = int(np.nonzero(cls == k)[0][0])
+            s = self.setups[c]
+            out.append({"lattice": {0: "sc", 1: "bcc", 2: "fcc"}[s.lattice], "L": list(s.n),
+                        "species": s.n_species, "shells": s.interaction_range,
+                        "chains": int((cls == k).sum()), "trials_per_round": int(depths[k]),
+                        "ms_per_depth": [round(float(x), 2) for x in ms[k * max_depth:(k + 1) * max_depth]]})
+        return {"classes": out}
+
+    def chain_classes(self) -> np.ndarray:
+        cls = np.zeros(self.n, dtype=np.int32)
+        _check(load().brawl_batch_chain_classes(self._h, _ptr(cls)))
+        return cls
+
+    def set_class_depths(self, depths) -> None:
+        d = np.ascontiguousarray(depths, dtype=np.int32)
+        _check(load().brawl_batch_set_class_depths(self._h, _ptr(d)))
 
     def _trials(self, n_trials) -> np.ndarray:
         return np.ascontiguousarray(np.broadcast_to(np.asarray(n_trials, dtype=np.int64), (self.n,)))

@@ -357,6 +357,17 @@ struct brawl_batch {
   int halo_min_z = 0, halo_max_z = 0;
   std::vector<ChainJob> staged;          // jobs in launch order
   int n_halo_launch = 0;
+  // classes of the shared-memory chains: chains of one (lattice, n1, n2, n3,
+  // species, shells) share a class; each class is launched on its own
+  // stream with its own shared memory, unrolling and trials per round
+  std::vector<int> cls;                  // per chain: class, or -1 (not a halo chain)
+  std::vector<uint32_t> class_smem;
+  std::vector<int> class_z, class_depth;
+  std::vector<int> class_first, class_count;  // in launch order (upload_jobs)
+  std::vector<cudaStream_t> side;        // one per class beyond the first
+  std::vector<cudaEvent_t> ev_side;
+  cudaEvent_t ev_fork = nullptr;
+  bool per_class = false;                // class depths chosen (brawl_batch_autotune_classes)
   std::vector<unsigned long long> last_counters;
   int device = 0;
   int max_optin = 0;
@@ -414,17 +425,34 @@ int ensure_grid(brawl_batch* b, size_t bytes) {
 // each group by decreasing trial count so the longest chains start first.
 int upload_jobs(brawl_batch* b) {
   const int n = (int)b->jobs.size();
+  const int nk = (int)b->class_smem.size();
+  // classes by their longest chain, longest first; chains by trials
+  std::vector<int64_t> class_most(nk, 0);
+  for (int c = 0; c < n; ++c)
+    if (b->cls[c] >= 0) class_most[b->cls[c]] = std::max(class_most[b->cls[c]], b->jobs[c].n_trials);
+  std::vector<int> corder(nk), crank(nk);
+  for (int k = 0; k < nk; ++k) corder[k] = k;
+  std::stable_sort(corder.begin(), corder.end(), [&](int x, int y) { return class_most[x] > class_most[y]; });
+  for (int r = 0; r < nk; ++r) crank[corder[r]] = r;
   std::vector<int> order(n);
   for (int c = 0; c < n; ++c) order[c] = c;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     if (b->halo[x] != b->halo[y]) return b->halo[x] > b->halo[y];
+    if (b->halo[x] && b->per_class && b->cls[x] != b->cls[y]) return crank[b->cls[x]] < crank[b->cls[y]];
     return b->jobs[x].n_trials > b->jobs[y].n_trials;
   });
   b->staged.resize(n);
   b->n_halo_launch = 0;
+  b->class_first.assign(nk, 0);
+  b->class_count.assign(nk, 0);
   for (int k = 0; k < n; ++k) {
     b->staged[k] = b->jobs[order[k]];
     b->n_halo_launch += b->halo[order[k]];
+    const int cl = b->cls[order[k]];
+    if (cl >= 0) {
+      if (b->class_count[cl] == 0) b->class_first[cl] = k;
+      b->class_count[cl] += 1;
+    }
   }
   CUDA_TRY(cudaMemcpyAsync(b->d_jobs, b->staged.data(), n * sizeof(ChainJob),
                            cudaMemcpyHostToDevice, b->stream));
@@ -453,6 +481,46 @@ int set_chain_config(brawl_batch* b, int c, const int8_t* config) {
 
 int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, bool serial,
                         cudaStream_t stream, bool wait);
+
+// Side streams for the classes beyond the first (created once).
+int ensure_side_streams(brawl_batch* b) {
+  const size_t need = b->class_smem.empty() ? 0 : b->class_smem.size() - 1;
+  if (!b->ev_fork) CUDA_TRY(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  while (b->side.size() < need) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    b->side.push_back(st);
+    b->ev_side.push_back(ev);
+  }
+  return BRAWL_OK;
+}
+
+// The shared-memory chains of every class (only = -1) or of class `only`,
+// each class in its own launch with its own shared memory, unrolling and
+// trials per round: the first on `stream`, the others on side streams
+// forked from it and joined back.
+int launch_classes(brawl_batch* b, cudaStream_t stream, int only) {
+  TRY(ensure_side_streams(b));
+  const int nk = (int)b->class_smem.size();
+  std::vector<int> ks;
+  for (int k = 0; k < nk; ++k)
+    if (b->class_count[k] > 0 && (only < 0 || k == only)) ks.push_back(k);
+  std::sort(ks.begin(), ks.end(), [&](int x, int y) { return b->class_first[x] < b->class_first[y]; });
+  if (ks.size() > 1) CUDA_TRY(cudaEventRecord(b->ev_fork, stream));
+  for (size_t i = 0; i < ks.size(); ++i) {
+    const int k = ks[i];
+    cudaStream_t st = i == 0 ? stream : b->side[i - 1];
+    if (i > 0) CUDA_TRY(cudaStreamWaitEvent(st, b->ev_fork, 0));
+    launch_halo_chains(b->d_jobs + b->class_first[k], b->class_count[k], b->class_smem[k], b->class_z[k],
+                       b->class_z[k], b->class_depth[k], b->max_optin, st);
+    CUDA_TRY(cudaGetLastError());
+    if (i > 0) CUDA_TRY(cudaEventRecord(b->ev_side[i - 1], st));
+  }
+  for (size_t i = 1; i < ks.size(); ++i) CUDA_TRY(cudaStreamWaitEvent(stream, b->ev_side[i - 1], 0));
+  return BRAWL_OK;
+}
 
 // Kernel launches run fewer than 2^31 trials per chain (their tallies are
 // 32-bit); longer runs are split into consecutive launches, which continue
@@ -513,7 +581,9 @@ int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accept
       CUDA_TRY(cudaStreamSynchronize(stream));
     }
   } else {
-    if (nh > 0)
+    if (nh > 0 && b->per_class)
+      TRY(launch_classes(b, stream, -1));
+    else if (nh > 0)
       launch_halo_chains(b->d_jobs, nh, b->halo_smem, b->halo_min_z, b->halo_max_z, b->spec_nc,
                          b->max_optin, stream);
     if (n - nh > 0)
@@ -574,6 +644,7 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
     need_gmem = std::max(need_gmem, smem_layout(b->models[c].g, false).total);
   }
   b->halo.assign(n_chains, 0);
+  b->cls.assign(n_chains, -1);
   for (int c = 0; c < n_chains; ++c) {
     const Model& m = b->models[c];
     HaloGeom H;
@@ -581,6 +652,22 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
     make_halo(m.g, H, ok);
     if (ok && halo_layout(m.g, H).total <= (uint32_t)max_optin) {
       b->halo[c] = 1;
+      int k = 0;
+      for (; k < c; ++k) {
+        if (b->cls[k] < 0) continue;
+        const Geom& o = b->models[k].g;
+        if (o.lattice == m.g.lattice && o.n1 == m.g.n1 && o.n2 == m.g.n2 && o.n3 == m.g.n3 &&
+            o.ns == m.g.ns && o.nsh == m.g.nsh)
+          break;
+      }
+      if (k < c) {
+        b->cls[c] = b->cls[k];
+      } else {
+        b->cls[c] = (int)b->class_smem.size();
+        b->class_smem.push_back(halo_layout(m.g, H).total);
+        b->class_z.push_back((int)m.g.z);
+        b->class_depth.push_back(kDefaultSpeculation);
+      }
       b->halo_smem = std::max(b->halo_smem, halo_layout(m.g, H).total);
       b->halo_min_z = b->halo_max_z == 0 ? (int)m.g.z : std::min(b->halo_min_z, (int)m.g.z);
       b->halo_max_z = std::max(b->halo_max_z, (int)m.g.z);
@@ -726,6 +813,12 @@ int brawl_batch_destroy(brawl_batch* b) {
                           (const void*)b->d_alro, (const void*)b->d_alro_off, (const void*)b->d_samp})
       dfree(p, b->stream);
     cudaStreamSynchronize(b->stream);
+    for (size_t k = 0; k < b->side.size(); ++k) {
+      cudaStreamSynchronize(b->side[k]);
+      cudaEventDestroy(b->ev_side[k]);
+      cudaStreamDestroy(b->side[k]);
+    }
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     cudaStreamDestroy(b->stream);
   }
   delete b;
@@ -741,6 +834,110 @@ int brawl_batch_size(brawl_batch* b, int* n) {
 int brawl_batch_set_speculation(brawl_batch* b, int trials_per_round) {
   if (!b || trials_per_round < 1 || trials_per_round > 4) return fail(BRAWL_EINVAL, "trials per round must be 1-4");
   b->spec_nc = trials_per_round;
+  return BRAWL_OK;
+}
+
+// Trials per round chosen per class of shared-memory chains, by
+// measurement of the whole batch: the classes in order of decreasing work
+// (the class holding the longest chains first), each class's depth 1..
+// max_depth tried while the others keep theirs, every try run three times
+// from the same state (restored after each) and the median kept; a deeper
+// round is taken only when it is at least 2% faster.  Every depth is
+// bit-exact, so the results never depend on the choice.
+int brawl_batch_autotune_classes(brawl_batch* b, const int64_t* n_trials, int max_depth, int* depths,
+                                 double* ms, int* n_classes) {
+  if (!b || !n_trials || max_depth < 1 || max_depth > 4) return fail(BRAWL_EINVAL, "bad argument");
+  for (size_t c = 0; c < b->jobs.size(); ++c)
+    if (n_trials[c] < 0) return fail(BRAWL_EINVAL, "n_trials < 0");
+  const int nk = (int)b->class_smem.size();
+  if (n_classes) *n_classes = nk;
+  if (nk == 0) return BRAWL_OK;
+  cudaStream_t s = b->stream;
+  unsigned char* snap = nullptr;
+  if (dalloc(&snap, b->arena_bytes, s) != cudaSuccess) return fail(BRAWL_ENOMEM, "autotune snapshot");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const std::vector<unsigned long long> last = b->last_counters;
+  const std::vector<int> keep = b->class_depth;
+  const bool keep_pc = b->per_class;
+  int rc = BRAWL_OK;
+  auto cuda = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && rc == BRAWL_OK) rc = fail(BRAWL_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return rc == BRAWL_OK;
+  };
+  std::vector<double> work(nk, 0.0);
+  for (size_t c = 0; c < b->jobs.size(); ++c)
+    if (b->cls[c] >= 0) work[b->cls[c]] += (double)n_trials[c];
+  std::vector<int> order(nk);
+  for (int k = 0; k < nk; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+  b->per_class = true;
+  b->class_depth.assign(nk, 1);
+  auto timed = [&](float& out) {
+    std::vector<float> t(3, 0.0f);
+    for (int r = 0; r < 3 && rc == BRAWL_OK; ++r) {
+      if (!cuda(cudaEventRecord(e0, s), "event")) return;
+      const int q = run_metropolis(b, n_trials, nullptr, false, s, false);
+      if (q != BRAWL_OK) {
+        rc = q;
+        return;
+      }
+      if (!cuda(cudaEventRecord(e1, s), "event") || !cuda(cudaEventSynchronize(e1), "timed run") ||
+          !cuda(cudaEventElapsedTime(&t[r], e0, e1), "event"))
+        return;
+      if (!cuda(cudaMemcpyAsync(b->arena, snap, b->arena_bytes, cudaMemcpyDeviceToDevice, s), "restore")) return;
+      b->last_counters = last;
+    }
+    std::sort(t.begin(), t.end());
+    out = t[1];
+  };
+  if (cuda(cudaEventCreate(&e0), "event") && cuda(cudaEventCreate(&e1), "event") &&
+      cuda(cudaMemcpyAsync(snap, b->arena, b->arena_bytes, cudaMemcpyDeviceToDevice, s), "snapshot")) {
+    for (int k : order) {
+      float best_t = 0.0f;
+      int best_d = 1;
+      for (int d = 1; d <= max_depth && rc == BRAWL_OK; ++d) {
+        b->class_depth[k] = d;
+        float t = 0.0f;
+        timed(t);
+        if (rc != BRAWL_OK) break;
+        if (ms) ms[k * max_depth + d - 1] = (double)t;
+        if (d == 1 || t < 0.98f * best_t) {
+          best_t = t;
+          best_d = d;
+        }
+      }
+      b->class_depth[k] = best_d;
+      if (rc != BRAWL_OK) break;
+    }
+    cuda(cudaStreamSynchronize(s), "restore");
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  dfree(snap, s);
+  if (rc != BRAWL_OK) {
+    b->class_depth = keep;
+    b->per_class = keep_pc;
+  }
+  if (depths)
+    for (int k = 0; k < nk; ++k) depths[k] = b->class_depth[k];
+  return rc;
+}
+
+// Trials per round of every class, set by the caller (1-4 each); every
+// class then runs in its own launch.
+int brawl_batch_set_class_depths(brawl_batch* b, const int* depths) {
+  if (!b || !depths) return fail(BRAWL_EINVAL, "null argument");
+  for (size_t k = 0; k < b->class_depth.size(); ++k)
+    if (depths[k] < 1 || depths[k] > 4) return fail(BRAWL_EINVAL, "trials per round must be 1-4");
+  for (size_t k = 0; k < b->class_depth.size(); ++k) b->class_depth[k] = depths[k];
+  b->per_class = true;
+  return BRAWL_OK;
+}
+
+// The class of every chain (-1: not a shared-memory chain).
+int brawl_batch_chain_classes(brawl_batch* b, int* classes) {
+  if (!b || !classes) return fail(BRAWL_EINVAL, "null argument");
+  for (size_t c = 0; c < b->cls.size(); ++c) classes[c] = b->cls[c];
   return BRAWL_OK;
 }
 

@@ -191,6 +191,24 @@ int brawl_batch_set_speculation(brawl_batch *batch, int trials_per_round);
  * gets each depth's time; chosen (may be NULL) the depth kept. */
 int brawl_batch_autotune(brawl_batch *batch, const int64_t *n_trials, int max_depth, double *ms,
                          int *chosen);
+/* Shared-memory chains are grouped in classes (same lattice, n1, n2, n3,
+ * species and shells); after this call every class runs in its own launch,
+ * concurrently with the others, with its own shared memory, unrolling and
+ * trials per round.  The depths are picked per class by timing the whole
+ * batch (n_trials[c] trials of every chain, three runs per try, from the
+ * same state, restored after each): the classes in order of decreasing
+ * work, each class's depths 1..max_depth with the others fixed, a deeper
+ * round kept only when 2% faster.  depths (n_classes entries, may be NULL)
+ * gets the choice, ms (n_classes * max_depth, may be NULL) the median time
+ * of every try, n_classes (may be NULL) the class count.  Speed only: the
+ * trajectories do not depend on the depths. */
+int brawl_batch_autotune_classes(brawl_batch *batch, const int64_t *n_trials, int max_depth,
+                                 int *depths, double *ms, int *n_classes);
+/* Trials per round of every class (n_classes entries, 1-4 each), set by
+ * the caller; every class then runs in its own launch as above. */
+int brawl_batch_set_class_depths(brawl_batch *batch, const int *depths);
+/* The class of every chain (-1: not a shared-memory chain). */
+int brawl_batch_chain_classes(brawl_batch *batch, int *classes);
 /* n_trials[c] Metropolis trials on every chain c, all chains in one launch.
  * accepted (may be NULL) receives each chain's accept sum for this call. */
 int brawl_batch_metropolis_run(brawl_batch *batch, const int64_t *n_trials, int64_t *accepted);

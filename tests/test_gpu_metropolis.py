@@ -538,3 +538,41 @@ def test_autotune_keeps_the_state_and_the_trajectories():
     acc = b.metropolis(np.array([e[0] for e in expect]))
     for k, (t, cfg, a, c) in enumerate(expect):
         assert acc[k] == a and np.array_equal(b.config(k), cfg), Ls[k]
+
+
+def test_classes_run_their_own_depths_and_autotune_keeps_state():
+    """Shared-memory chains in classes (lattice, L, species, shells), each
+    class in its own launch: with different trials per round per class the
+    runs equal the oracle's; brawl_batch_autotune_classes leaves the state
+    as it found it and reports a depth per class."""
+    rng = np.random.default_rng(66)
+    V = random_V(rng, 4, 6)
+    Ls = [4, 6, 4, 6, 5]
+    chains, expect = [], []
+    for r, L in enumerate(Ls):
+        T = 300.0 * 4.0 ** (r / (len(Ls) - 1))
+        setup = B.Setup("bcc", L, L, L, 4, 6)
+        seed = 110179 + 11 * r
+        chains.append(dict(setup=setup, V=V, seed=seed, beta=1.0 / (T * B.K_B_IN_RY),
+                           species_concentrations=conc_vector(4)))
+        trials = 5 * setup.n_atoms
+        mod, cfg, r_, acc, c, _ = _oracle_run("bcc", (L, L, L), V, seed, T, trials, False, conc_vector(4), None)
+        expect.append((trials, cfg, acc, c))
+    b = B.Batch(chains)
+    cls = b.chain_classes()
+    assert cls[0] == cls[2] and cls[1] == cls[3] and len(set(cls.tolist())) == 3
+    before = ([b.config(k) for k in range(len(Ls))], [b.rng_state(k) for k in range(len(Ls))], b.counters())
+    tuned = b.autotune_classes(np.array([2 * e[0] for e in expect]))
+    assert len(tuned["classes"]) == 3
+    assert all(1 <= c["trials_per_round"] <= 4 for c in tuned["classes"])
+    for k in range(len(Ls)):
+        assert np.array_equal(b.config(k), before[0][k])
+        assert np.array_equal(b.rng_state(k), before[1][k])
+    assert np.array_equal(b.counters(), before[2])
+    b.set_class_depths([3, 1, 2])
+    half = [e[0] // 2 for e in expect]
+    acc1 = b.metropolis(np.array(half))
+    b.set_class_depths([1, 4, 1])
+    acc2 = b.metropolis(np.array([e[0] - h for e, h in zip(expect, half)]))
+    for k, (t, cfg, a, c) in enumerate(expect):
+        assert acc1[k] + acc2[k] == a and np.array_equal(b.config(k), cfg), Ls[k]
