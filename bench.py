@@ -990,7 +990,8 @@ def main() -> int:
             "nested_sampling": walkers.get("nested_sampling"),
             "anneal_one_chain": anneal,
             "clocks": clk,
-            "gpu_launches": args.steps,
+            # one launch per chain class per step
+            "gpu_launches": args.steps * max(1, len(cta_shape.get("classes", [])) or 1),
             "counters": {"trials": T_all, "evaluated": T_eval, "draws": draws,
                          "accepted": int(d[3]), "exp_tests": int(d[4]),
                          "exact_path": int(d[5]), "exp_fp64": int(d[6]), "exp_cr": int(d[7])},
