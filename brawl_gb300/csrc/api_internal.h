@@ -46,4 +46,12 @@ uint32_t api_ns_smem(brawl_ns* ns);
 void api_ns_variant(brawl_ns* ns, int* max_z, bool* all_D);
 std::string api_last_error();
 
+// Waits for a stream.  In a thread that set_blocking_waits(true) the wait
+// sleeps on a blocking-sync event instead of spinning: the serving loop's
+// worker threads, many more than the host cores' share left for the
+// scheduler, wait this way whatever flags the CUDA context was created
+// with.  Elsewhere it is cudaStreamSynchronize.
+cudaError_t stream_wait(cudaStream_t s);
+void set_blocking_waits(bool on);
+
 }  // namespace brawl

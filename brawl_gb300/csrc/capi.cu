@@ -399,12 +399,12 @@ namespace {
 int check_status(brawl_batch* b) {
   std::vector<int32_t> st(b->jobs.size());
   CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_status, st.size() * 4, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   for (size_t i = 0; i < st.size(); ++i)
     if (st[i] != 0) {
       int32_t zero = 0;
       cudaMemcpyAsync(b->d_status + i, &zero, 4, cudaMemcpyHostToDevice, b->stream);
-      cudaStreamSynchronize(b->stream);
+      stream_wait(b->stream);
       return fail(BRAWL_ESTATE, "device check failed on chain " + std::to_string(i) + " (code " +
                                     std::to_string(st[i]) + ")");
     }
@@ -463,7 +463,7 @@ int read_counters(brawl_batch* b, std::vector<unsigned long long>& out) {
   out.resize(b->jobs.size() * kNumCounters);
   CUDA_TRY(cudaMemcpyAsync(out.data(), b->d_counters, out.size() * 8, cudaMemcpyDeviceToHost,
                            b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -578,7 +578,7 @@ int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accept
         launch_metropolis(b->d_jobs + k, 1, b->smem_lat, b->use_D, b->smem_bytes, b->max_z,
                           stream);
       CUDA_TRY(cudaGetLastError());
-      CUDA_TRY(cudaStreamSynchronize(stream));
+      CUDA_TRY(stream_wait(stream));
     }
   } else {
     if (nh > 0 && b->per_class)
@@ -592,7 +592,7 @@ int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accept
     CUDA_TRY(cudaGetLastError());
   }
   if (!wait) return BRAWL_OK;
-  CUDA_TRY(cudaStreamSynchronize(stream));
+  CUDA_TRY(stream_wait(stream));
   std::vector<unsigned long long> cnt;
   TRY(read_counters(b, cnt));
   if (accepted)
@@ -757,7 +757,7 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
   b->d_energy = reinterpret_cast<double*>(b->arena + off_energy);
   std::memcpy(&h[off_jobs], b->jobs.data(), n_chains * sizeof(ChainJob));
   e = cudaMemcpyAsync(b->arena, h.data(), total, cudaMemcpyHostToDevice, b->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e == cudaSuccess) e = stream_wait(b->stream);
   if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
   b->last_counters.assign((size_t)n_chains * kNumCounters, 0);
   // configurations: given ones are packed, the others drawn by initial_setup
@@ -790,7 +790,7 @@ int brawl_batch_create(const brawl_chain_desc* chains, int n_chains, brawl_batch
                     b->stream);
     launch_initial_setup(d_init, (int)init.size(), b->stream);
     dfree(d_init, b->stream);
-    e = cudaStreamSynchronize(b->stream);
+    e = stream_wait(b->stream);
     if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
     int r = check_status(b);
     if (r != BRAWL_OK) return cleanup(r);
@@ -812,9 +812,9 @@ int brawl_batch_destroy(brawl_batch* b) {
                           (const void*)b->d_grids, (const void*)b->d_gjobs, (const void*)b->d_scratch,
                           (const void*)b->d_alro, (const void*)b->d_alro_off, (const void*)b->d_samp})
       dfree(p, b->stream);
-    cudaStreamSynchronize(b->stream);
+    stream_wait(b->stream);
     for (size_t k = 0; k < b->side.size(); ++k) {
-      cudaStreamSynchronize(b->side[k]);
+      stream_wait(b->side[k]);
       cudaEventDestroy(b->ev_side[k]);
       cudaStreamDestroy(b->side[k]);
     }
@@ -909,7 +909,7 @@ int brawl_batch_autotune_classes(brawl_batch* b, const int64_t* n_trials, int ma
       b->class_depth[k] = best_d;
       if (rc != BRAWL_OK) break;
     }
-    cuda(cudaStreamSynchronize(s), "restore");
+    cuda(stream_wait(s), "restore");
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
@@ -985,7 +985,7 @@ int brawl_batch_autotune(brawl_batch* b, const int64_t* n_trials, int max_depth,
         best = d;
       }
     }
-    cuda(cudaStreamSynchronize(s), "restore");
+    cuda(stream_wait(s), "restore");
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
@@ -1064,7 +1064,7 @@ int brawl_batch_total_energy(brawl_batch* b, double* energies) {
   TRY(queue_batch_energy(b));
   const int n = (int)b->jobs.size();
   CUDA_TRY(cudaMemcpyAsync(energies, b->d_energy, n * 8, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1076,7 +1076,7 @@ int brawl_batch_get_config(brawl_batch* b, int c, int8_t* config) {
   launch_unpack(g, b->jobs[c].lat, b->d_grid, b->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(config, b->d_grid, grid, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1100,7 +1100,7 @@ static int ensure_grids(brawl_batch* b) {
   CUDA_TRY(dalloc(&b->d_grids, (size_t)off, b->stream));
   CUDA_TRY(dalloc(&b->d_gjobs, n * sizeof(GridJob), b->stream));
   CUDA_TRY(cudaMemcpyAsync(b->d_gjobs, gj.data(), n * sizeof(GridJob), cudaMemcpyHostToDevice, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   b->total_cells = off;
   return BRAWL_OK;
 }
@@ -1112,7 +1112,7 @@ int brawl_batch_get_configs(brawl_batch* b, int8_t* configs) {
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(configs, b->d_grids, (size_t)b->total_cells, cudaMemcpyDeviceToHost,
                            b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1160,7 +1160,7 @@ int brawl_batch_metropolis_host(brawl_batch* b, const int8_t* configs_in, const 
   CUDA_TRY(cudaGetLastError());
   if (!dst)
     CUDA_TRY(cudaMemcpyAsync(configs_out, b->d_grids, (size_t)b->total_cells, cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
+  CUDA_TRY(stream_wait(s));
   std::vector<unsigned long long> cnt;
   TRY(read_counters(b, cnt));
   if (accepted)
@@ -1207,7 +1207,7 @@ int brawl_batch_alro_get(brawl_batch* b, int c, double* order) {
   std::vector<double> cnt((size_t)g.ns * g.n_sites);
   CUDA_TRY(cudaMemcpyAsync(cnt.data(), b->d_alro + b->alro_off[c], cnt.size() * 8, cudaMemcpyDeviceToHost,
                            b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   // order(species, basis, x, y, z), species fastest; empty cells stay 0
   const int W1 = 2 * g.n1, W2 = 2 * g.n2, W3 = 2 * g.n3, ns = g.ns;
   std::fill(order, order + (size_t)ns * W1 * W2 * W3, 0.0);
@@ -1228,7 +1228,7 @@ int brawl_batch_alro_get(brawl_batch* b, int c, double* order) {
 int brawl_batch_rng_get(brawl_batch* b, int c, uint32_t state[625]) {
   if (!b || !state || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad argument");
   CUDA_TRY(cudaMemcpyAsync(state, b->jobs[c].rng, (kMTN + 1) * 4, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1291,7 +1291,7 @@ int brawl_batch_radial_densities(brawl_batch* b, int c, int wc_range, const doub
   const size_t n_counts = (size_t)nsp * nsp * plan.n_class + nsp;
   std::vector<unsigned long long> cnt(n_counts);
   CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_cnt, n_counts * 8, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   finish_asro(g, wc_range, plan, cnt.data(), rho);
   return BRAWL_OK;
 }
@@ -1329,7 +1329,7 @@ static int ensure_sampling(brawl_batch* b, int wc_range) {
   CUDA_TRY(cudaMemcpyAsync(b->d_natoms, nat.data(), n * 8, cudaMemcpyHostToDevice, b->stream));
   CUDA_TRY(cudaMemsetAsync(b->d_samp, 0, o_nat, b->stream));
   if (m) CUDA_TRY(cudaMemsetAsync(b->d_rho_sum, 0, n * m * 8, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1342,7 +1342,7 @@ int brawl_batch_sampling_reset(brawl_batch* b, int wc_range) {
   if (m) CUDA_TRY(cudaMemsetAsync(b->d_rho_sum, 0, n * m * 8, b->stream));
   launch_acceptance_snapshot(b->d_counters, b->d_acc0, n, b->stream);
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1355,7 +1355,7 @@ int brawl_batch_energy_sample(brawl_batch* b, double* energies) {
   CUDA_TRY(cudaGetLastError());
   if (energies)
     CUDA_TRY(cudaMemcpyAsync(energies, b->d_energy, n * 8, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1377,7 +1377,7 @@ int brawl_batch_asro_sample(brawl_batch* b, int c, const double* shells, double*
                      b->d_rho_sum + (size_t)c * m, b->stream);
   CUDA_TRY(cudaGetLastError());
   if (rho) CUDA_TRY(cudaMemcpyAsync(rho, rho_out, m * 8, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1393,7 +1393,7 @@ int brawl_batch_temperature_stats(brawl_batch* b, int64_t n_save_energy, int64_t
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(per_chain, b->d_tstats, 3 * n * 8, cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(cudaMemcpyAsync(average, b->d_tstats + 3 * n, 3 * 8, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1408,7 +1408,7 @@ int brawl_batch_asro_stats(brawl_batch* b, int64_t n_save_asro, double* per_chai
   CUDA_TRY(cudaMemcpyAsync(per_chain, b->d_rho_stats, (size_t)n * m * 8, cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(cudaMemcpyAsync(average, b->d_rho_stats + (size_t)n * m, (size_t)m * 8, cudaMemcpyDeviceToHost,
                            b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1464,7 +1464,7 @@ int brawl_set_interactions(brawl_ctx* ctx, const double* V_ex) {
                            cudaMemcpyHostToDevice, b->stream));
   CUDA_TRY(cudaMemcpyAsync(const_cast<int32_t*>(j.F), m.F.data(), m.F.size() * 4,
                            cudaMemcpyHostToDevice, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   const double beta = j.beta;
   b->models[0] = m;
   j.band = m.band;
@@ -1509,7 +1509,7 @@ int brawl_rng_set(brawl_ctx* ctx, const uint32_t state[625]) {
   }
   brawl_batch* b = ctx->b;
   CUDA_TRY(cudaMemcpyAsync(b->jobs[0].rng, state, (kMTN + 1) * 4, cudaMemcpyHostToDevice, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1564,7 +1564,7 @@ int brawl_initial_setup(brawl_ctx* ctx, double* conc, const int64_t* numbers) {
   cudaMemcpyAsync(d, &ij, sizeof(ij), cudaMemcpyHostToDevice, b->stream);
   launch_initial_setup(d, 1, b->stream);
   dfree(d, b->stream);
-  cudaError_t e = cudaStreamSynchronize(b->stream);
+  cudaError_t e = stream_wait(b->stream);
   if (e != cudaSuccess) return fail(BRAWL_ECUDA, cudaGetErrorString(e));
   TRY(check_status(b));
   std::copy(c.begin(), c.end(), conc);
@@ -1606,7 +1606,7 @@ int brawl_site_energy(brawl_ctx* ctx, const int idx[4], double* energy) {
   launch_site_energy(b->d_ejobs, x, y, z, b->d_energy, b->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(energy, b->d_energy, 8, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -1695,7 +1695,7 @@ extern "C" int brawl_ns_destroy(brawl_ns* ns) {
   if (ns->stream) {
     for (void* p : ns->allocs) dfree(p, ns->stream);
     dfree(ns->d_limits, ns->stream);
-    cudaStreamSynchronize(ns->stream);
+    stream_wait(ns->stream);
     cudaStreamDestroy(ns->stream);
   }
   delete ns;
@@ -1783,7 +1783,7 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
     cudaMemcpyAsync(pRng, st, sizeof(st), cudaMemcpyHostToDevice, ns->stream);
     cudaMemsetAsync(pCnt, 0, kNumCounters * 8, ns->stream);
     cudaMemsetAsync(pSt, 0, 4, ns->stream);
-    CUDA_TRY(cudaStreamSynchronize(ns->stream));
+    CUDA_TRY(stream_wait(ns->stream));
     j.V = (const double*)pV;
     j.F = (const int32_t*)pF;
     j.entries = (const uint32_t*)pE;
@@ -1830,7 +1830,7 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
   CUDA_TRY(cudaMemcpyAsync(pEj, ej.data(), ej.size() * sizeof(EnergyJob), cudaMemcpyHostToDevice, ns->stream));
   launch_total_energy((EnergyJob*)pEj, (int)ej.size(), total_sites, ns->stream);
   launch_ns_jitter(ns->d_runs, n_runs, max_K, ns->stream);
-  cudaError_t e = cudaStreamSynchronize(ns->stream);
+  cudaError_t e = stream_wait(ns->stream);
   if (e != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, cudaGetErrorString(e)));
   // the per-site scratch is only needed at set-up
   dfree(pSite, ns->stream);
@@ -1840,7 +1840,7 @@ extern "C" int brawl_ns_create(const brawl_ns_desc* descs, int n_runs, brawl_ns*
   for (int r = 0; r < n_runs; ++r) {
     int32_t st = 0;
     cudaMemcpyAsync(&st, ns->runs[r].job.status, 4, cudaMemcpyDeviceToHost, ns->stream);
-    cudaStreamSynchronize(ns->stream);
+    stream_wait(ns->stream);
     if (st) return cleanup(fail(BRAWL_ESTATE, "walker initialisation failed on run " + std::to_string(r)));
   }
   *out = ns;
@@ -1862,7 +1862,7 @@ extern "C" int brawl_ns_iterate(brawl_ns* ns, int n_iter, double* limits) {
   // the device-side run state (iteration counters) is authoritative: read it back
   std::vector<NsRun> cur(n_runs);
   CUDA_TRY(cudaMemcpyAsync(cur.data(), ns->d_runs, n_runs * sizeof(NsRun), cudaMemcpyDeviceToHost, ns->stream));
-  CUDA_TRY(cudaStreamSynchronize(ns->stream));
+  CUDA_TRY(stream_wait(ns->stream));
   for (int r = 0; r < n_runs; ++r) {
     cur[r].limits = ns->d_limits + (size_t)r * n_iter;
     cur[r].n_iter = n_iter;
@@ -1872,7 +1872,7 @@ extern "C" int brawl_ns_iterate(brawl_ns* ns, int n_iter, double* limits) {
   CUDA_TRY(cudaGetLastError());
   if (limits)
     CUDA_TRY(cudaMemcpyAsync(limits, ns->d_limits, need, cudaMemcpyDeviceToHost, ns->stream));
-  CUDA_TRY(cudaStreamSynchronize(ns->stream));
+  CUDA_TRY(stream_wait(ns->stream));
   for (int r = 0; r < n_runs; ++r) {
     int32_t st = 0;
     CUDA_TRY(cudaMemcpy(&st, ns->runs[r].job.status, 4, cudaMemcpyDeviceToHost));
@@ -1898,7 +1898,7 @@ extern "C" int brawl_ns_walker_config(brawl_ns* ns, int run, int walker, int8_t*
   launch_unpack(g, R.walkers + (size_t)walker * g.n_sites, d_grid, ns->stream);
   cudaError_t e = cudaMemcpyAsync(config, d_grid, grid, cudaMemcpyDeviceToHost, ns->stream);
   dfree(d_grid, ns->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ns->stream);
+  if (e == cudaSuccess) e = stream_wait(ns->stream);
   if (e != cudaSuccess) return fail(BRAWL_ECUDA, cudaGetErrorString(e));
   return BRAWL_OK;
 }
@@ -1976,7 +1976,7 @@ int batch_genrand(brawl_batch* b, int c, int64_t n, double* out) {
   }
   st[kMTN] = (uint32_t)pos;
   CUDA_TRY(cudaMemcpyAsync(b->jobs[c].rng, st, sizeof(st), cudaMemcpyHostToDevice, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 }  // namespace
@@ -2082,7 +2082,7 @@ extern "C" int brawl_wl_create(const brawl_wl_desc* walkers, int n, int bins,
       dalloc(&wl->d_combined, (size_t)bins * sizeof(double), ws) != cudaSuccess)
     return cleanup(fail(BRAWL_ENOMEM, "exchange buffers"));
   cudaMemcpyAsync(wl->d_groups, wl->groups.data(), wl->groups.size() * sizeof(WlGroup), cudaMemcpyHostToDevice, ws);
-  if (cudaStreamSynchronize(ws) != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, "walker set-up"));
+  if (stream_wait(ws) != cudaSuccess) return cleanup(fail(BRAWL_ECUDA, "walker set-up"));
   *out = wl;
   return BRAWL_OK;
 }
@@ -2106,7 +2106,7 @@ extern "C" int brawl_wl_sweeps(brawl_wl* wl, int64_t n_trials, double wl_f, int 
   CUDA_TRY(cudaGetLastError());
   std::vector<WlWalker> res(n);
   CUDA_TRY(cudaMemcpyAsync(res.data(), wl->d_w, n * sizeof(WlWalker), cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   if (accepted)
     for (int c = 0; c < n; ++c) accepted[c] = res[c].accepted;
   int r = check_status(b);
@@ -2119,7 +2119,7 @@ extern "C" int brawl_wl_average(brawl_wl* wl) {
   CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), wl->w.size() * sizeof(WlWalker), cudaMemcpyHostToDevice, wl->b->stream));
   launch_wl_average(wl->d_groups, (int)wl->groups.size(), wl->d_w, wl->bins, 0, wl->b->stream);
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
+  CUDA_TRY(stream_wait(wl->b->stream));
   return BRAWL_OK;
 }
 
@@ -2147,7 +2147,7 @@ extern "C" int brawl_wl_replica_exchange(brawl_wl* wl, int* partner, int* exchan
     CUDA_TRY(cudaMemcpyAsync(partner, wl->d_partner, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   if (exchanged)
     CUDA_TRY(cudaMemcpyAsync(exchanged, wl->d_exchanged, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   if (n_accepted) *n_accepted = nacc;
   return BRAWL_OK;
 }
@@ -2160,7 +2160,7 @@ extern "C" int brawl_wl_flatness(brawl_wl* wl, double* flatness) {
   launch_wl_flatness(wl->d_w, n, wl->d_flat, b->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(flatness, wl->d_flat, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -2176,7 +2176,7 @@ extern "C" int brawl_wl_dos_combine(brawl_wl* wl, double* lng) {
   CUDA_TRY(cudaMemcpyAsync(&status, wl->d_nacc + 1, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   if (lng)
     CUDA_TRY(cudaMemcpyAsync(lng, wl->d_combined, (size_t)wl->bins * 8, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   if (status != 0) return fail(BRAWL_ESTATE, "a window has no overlap with the previous one");
   return BRAWL_OK;
 }
@@ -2186,7 +2186,7 @@ extern "C" int brawl_wl_reset_hist(brawl_wl* wl) {
   size_t total = 0;
   for (const WlWalker& W : wl->w) total += W.end - W.start + 1;
   CUDA_TRY(cudaMemsetAsync(wl->d_hist, 0, total * 8, wl->b->stream));
-  CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
+  CUDA_TRY(stream_wait(wl->b->stream));
   return BRAWL_OK;
 }
 
@@ -2252,7 +2252,7 @@ extern "C" int brawl_wl_enter_windows(brawl_wl* wl, double energy_min, double en
   launch_wl_enter(d_jobs, n, smem, s);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(jobs.data(), d_jobs, (size_t)n * sizeof(WlEnterJob), cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
+  CUDA_TRY(stream_wait(s));
   cleanup(BRAWL_OK);
   int rc = check_status(b);
   if (rc != BRAWL_OK) return rc;
@@ -2315,7 +2315,7 @@ extern "C" int brawl_wl_radial_enable(brawl_wl* wl, int wc_range, const double* 
   CUDA_TRY(cudaMemsetAsync(wl->d_rad_record, 0, (size_t)n * wl->bins * 4, s));
   CUDA_TRY(cudaMemsetAsync(wl->d_rad_rho, 0, (size_t)n * wl->bins * per * 8, s));
   CUDA_TRY(cudaMemsetAsync(wl->d_rad_steps, 0, (size_t)n * 4, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
+  CUDA_TRY(stream_wait(s));
   wl->rad_wc = wc_range;
   wl->rad_n_off = n_off;
   wl->rad_n_class = n_class;
@@ -2338,7 +2338,7 @@ extern "C" int brawl_wl_radial_set_done(brawl_wl* wl, const uint8_t* done) {
   bool all = true;
   for (int k = 0; k < wl->bins; ++k) all = all && done[k] != 0;
   CUDA_TRY(cudaMemcpyAsync(wl->d_rad_done, done, (size_t)wl->bins, cudaMemcpyHostToDevice, wl->b->stream));
-  CUDA_TRY(cudaStreamSynchronize(wl->b->stream));
+  CUDA_TRY(stream_wait(wl->b->stream));
   if (all)  // rho_saved: the walkers stop sampling
     for (WlWalker& W : wl->w) W.radial_record = nullptr;
   return BRAWL_OK;
@@ -2386,7 +2386,7 @@ extern "C" int brawl_wl_store_enable(brawl_wl* wl) {
   }
   CUDA_TRY(cudaMemsetAsync(wl->d_store, 0, total, s));             // config_per_bin = 0
   CUDA_TRY(cudaMemsetAsync(wl->d_store_open, 1, (size_t)n * wl->bins, s));  // config_store = .True.
-  CUDA_TRY(cudaStreamSynchronize(s));
+  CUDA_TRY(stream_wait(s));
   for (int c = 0; c < n; ++c) {
     wl->w[c].store = wl->d_store + off[c];
     wl->w[c].store_open = wl->d_store_open + (size_t)c * wl->bins;
@@ -2420,7 +2420,7 @@ extern "C" int brawl_wl_store_merge(brawl_wl* wl, const int* pick) {
   CUDA_TRY(cudaMemcpyAsync(wl->d_w, wl->w.data(), n * sizeof(WlWalker), cudaMemcpyHostToDevice, s));
   launch_wl_store_merge(wl->d_w, n, wl->bins, wl->d_pick, s);
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(s));
+  CUDA_TRY(stream_wait(s));
   return BRAWL_OK;
 }
 
@@ -2443,7 +2443,7 @@ extern "C" int brawl_wl_store_load(brawl_wl* wl, int c, int bin) {
   brawl_batch* b = wl->b;
   CUDA_TRY(cudaMemcpyAsync(b->jobs[c].lat, slot, (size_t)b->models[c].g.n_sites, cudaMemcpyDeviceToDevice,
                            b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -2458,7 +2458,7 @@ extern "C" int brawl_wl_store_get(brawl_wl* wl, int c, int bin, int8_t* config) 
   launch_unpack(g, slot, b->d_grid, b->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(config, b->d_grid, grid, cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -2512,7 +2512,7 @@ extern "C" int brawl_wl_set_windows(brawl_wl* wl, const int* start_idx, const in
   }
   wl->smem = smem;
   wl->all_D = all_D;
-  CUDA_TRY(cudaStreamSynchronize(s));
+  CUDA_TRY(stream_wait(s));
   return BRAWL_OK;
 }
 
@@ -2570,7 +2570,7 @@ extern "C" int brawl_wl_swap_configs(brawl_wl* wl, int a, int c) {
   CUDA_TRY(cudaMemcpyAsync(b->d_grid, b->jobs[a].lat, ga.n_sites, cudaMemcpyDeviceToDevice, b->stream));
   CUDA_TRY(cudaMemcpyAsync(b->jobs[a].lat, b->jobs[c].lat, ga.n_sites, cudaMemcpyDeviceToDevice, b->stream));
   CUDA_TRY(cudaMemcpyAsync(b->jobs[c].lat, b->d_grid, ga.n_sites, cudaMemcpyDeviceToDevice, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -2621,7 +2621,7 @@ void api_batch_beta(brawl_batch* b, int c, ChainJob& j, double beta) { set_beta(
 int api_batch_set_rng(brawl_batch* b, int c, const uint32_t state[625]) {
   if (!b || c < 0 || c >= (int)b->jobs.size()) return fail(BRAWL_EINVAL, "bad chain");
   CUDA_TRY(cudaMemcpyAsync(b->jobs[c].rng, state, (kMTN + 1) * 4, cudaMemcpyHostToDevice, b->stream));
-  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
 }
 
@@ -2641,6 +2641,33 @@ void api_ns_variant(brawl_ns* ns, int* max_z, bool* all_D) {
   *all_D = ns->all_D;
 }
 int api_last_error_set(int code, const std::string& msg) { return fail(code, msg); }
+namespace {
+struct WaitEvent {
+  cudaEvent_t e = nullptr;
+  ~WaitEvent() {
+    if (e) cudaEventDestroy(e);
+  }
+};
+thread_local bool tl_blocking = false;
+thread_local WaitEvent tl_wait;
+}  // namespace
+
+void set_blocking_waits(bool on) { tl_blocking = on; }
+
+cudaError_t stream_wait(cudaStream_t s) {
+  if (!tl_blocking) return cudaStreamSynchronize(s);
+  if (!tl_wait.e) {
+    const cudaError_t e = cudaEventCreateWithFlags(&tl_wait.e, cudaEventBlockingSync | cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      tl_wait.e = nullptr;
+      return cudaStreamSynchronize(s);
+    }
+  }
+  const cudaError_t e = cudaEventRecord(tl_wait.e, s);
+  if (e != cudaSuccess) return e;
+  return cudaEventSynchronize(tl_wait.e);
+}
+
 std::string api_last_error() { return g_err; }
 
 }  // namespace brawl

@@ -584,7 +584,7 @@ int setup_wl(Job& j) {
   brawl_batch* wb = api_wl_batch(j.wl);
   for (int k = 0; k < nw; ++k) SV_TRY(api_batch_set_rng(wb, k, rng[k].data()));
   SV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&j.d_estate), nw * sizeof(double), api_batch_stream(wb)));
-  SV_CUDA(cudaStreamSynchronize(api_batch_stream(wb)));
+  SV_CUDA(stream_wait(api_batch_stream(wb)));
   j.wl_energy.resize(nw);
   for (int k = 0; k < nw; ++k) {
     ChainSlot cs;
@@ -1004,6 +1004,7 @@ void end_one(brawl_server* S, const JobP& j, int status) {
 
 void worker(brawl_server* S) {
   cudaSetDevice(S->device);
+  set_blocking_waits(true);
   for (;;) {
     JobP j;
     int end_status = 0;
