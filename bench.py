@@ -385,11 +385,15 @@ def serving_leg(args) -> dict:
         "rounds": stats["rounds"],
         "busy_s_by_pipeline": {k: round(v["busy_s"], 2) for k, v in prof.items()},
     }
-    # ---- saturation phase
+    # ---- saturation phases: the mixed stream, then its anneal jobs alone
     n_sat = int(args.serve_sat_rate * args.serve_sat_seconds)
-    if n_sat > 0:
-        jobs = SV.stream_jobs(n_sat, master_seed=525252, L_range=(6, args.serve_L_max),
-                              sweeps_range=(100, args.serve_sweeps_max))
+    for key, kinds in (("saturation", None), ("saturation_anneal_only", ("anneal",))):
+        if n_sat <= 0:
+            break
+        jobs = SV.stream_jobs(n_sat if kinds is None else 3 * n_sat, master_seed=525252,
+                              L_range=(6, args.serve_L_max), sweeps_range=(100, args.serve_sweeps_max))
+        if kinds is not None:
+            jobs = [j for j in jobs if j["kind"] in kinds]
         arrivals = np.cumsum(rng.exponential(1.0 / args.serve_sat_rate, len(jobs)))
         util = UtilSampler(dev)
         series = []
@@ -413,7 +417,8 @@ def serving_leg(args) -> dict:
         samples = util.stop()
         lo = series[len(series) // 3]
         hi = series[-1]
-        out["saturation"] = {
+        out[key] = {
+            "jobs": "the mixed stream" if kinds is None else "the mixed stream's anneal jobs",
             "arrivals": f"Poisson, {args.serve_sat_rate} jobs/s for {args.serve_sat_seconds} s "
                         "(far above capacity: the queue grows)",
             "window_s": hi[0] - lo[0],

@@ -61,7 +61,7 @@ enum { kAnneal = 0, kWl = 1, kNs = 2, kKinds = 3 };
 // threads building admitted jobs' device objects and reading back ended
 // ones (a nested-sampling run's walker initialisation is one warp's
 // sequential work, so several run at once)
-constexpr int kWorkers = 32;
+constexpr int kWorkers = 8;
 // initial capacity of the pinned buffers: growing one (a pinned allocation)
 // waits for the whole device, so it should be rare
 constexpr size_t kPinnedEntries = 4096;
