@@ -233,11 +233,32 @@ enum LazyFold : int {
 
 constexpr int kLazyIlp = 8;  // chains per lane in flight
 
+// The species a chain's logged neighbour holds at its evaluation (before or
+// after the move).
+__device__ __forceinline__ int lazy_species(const LazyLog& L, int at, int s_before, int s_after,
+                                            bool after) {
+  const int code = (int)L.codes[at];
+  int s = code & 0x3f;
+  if (after) {
+    if (code & kLazyPartner) s = s_before;  // the partner now holds our old species
+    else if (code & kLazySelf) s = s_after;
+  }
+  return s;
+}
+
+// One logged neighbour's term V(cs, s, shell) of a chain (0 for a lane's
+// chain slot past the last chain: adding 0.0 to the unused sums).
+__device__ __forceinline__ double lazy_term(const LazyLog& L, const double* Vsh, int at, int cs,
+                                            int s_before, int s_after, bool after, bool on, int ns) {
+  if (!on) return 0.0;
+  return Vsh[(cs - 1) + ns * (lazy_species(L, at, s_before, s_after, after) - 1)];
+}
+
 // The exact energies of the n logged moves folded into e (the walker's
 // exact energy before the first of them).  All lanes; returns the same value
 // in every lane.
 static __device__ __noinline__ double lazy_flush(const Geom& g, const double* V, const int16_t* sstart,
-                                          LazyLog L, int n, double e, int fold, int lane) {
+                                                 LazyLog L, int n, double e, int fold, int lane) {
   const int z = g.z, nsh = g.nsh, ns = g.ns;
   const int nch = 4 * n;  // chains per shell: (move, evaluation)
   for (int sh = 0; sh < nsh; ++sh) {
@@ -261,18 +282,28 @@ static __device__ __noinline__ double lazy_flush(const Geom& g, const double* V,
         row[i] = m * 2 * z + (site2 ? z : 0) + k0;
         sum[i] = 0.0;
       }
-      for (int k = 0; k < len; ++k) {
+      int k = 0;
+      // the terms of four neighbours of every chain are loaded before
+      // their adds, so the loads overlap and the adds issue back to back
+      // (FP64 adds are the bound: one warp add every 64 cycles per
+      // sub-partition); each chain still adds its terms in list order
+      for (; k + 4 <= len; k += 4) {
+        double t[kLazyIlp][4];
 #pragma unroll
-        for (int i = 0; i < kLazyIlp; ++i) {
-          if (!on[i]) continue;
-          const int code = L.codes[row[i] + k];
-          int s = code & 0x3f;
-          if (after[i]) {
-            if (code & kLazyPartner) s = s_before[i];  // the partner now holds our old species
-            else if (code & kLazySelf) s = s_after[i];
-          }
-          sum[i] = __dadd_rn(sum[i], Vsh[(cs[i] - 1) + ns * (s - 1)]);
-        }
+        for (int i = 0; i < kLazyIlp; ++i)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) t[i][u] = lazy_term(L, Vsh, row[i] + k + u, cs[i], s_before[i], s_after[i],
+                                                          after[i], on[i], ns);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int i = 0; i < kLazyIlp; ++i) sum[i] = __dadd_rn(sum[i], t[i][u]);
+      }
+      for (; k < len; ++k) {
+#pragma unroll
+        for (int i = 0; i < kLazyIlp; ++i)
+          sum[i] = __dadd_rn(sum[i], lazy_term(L, Vsh, row[i] + k, cs[i], s_before[i], s_after[i], after[i],
+                                               on[i], ns));
       }
 #pragma unroll
       for (int i = 0; i < kLazyIlp; ++i) {
@@ -312,9 +343,15 @@ static __device__ __noinline__ double lazy_flush(const Geom& g, const double* V,
     L.pair[i] = __dadd_rn(e4[0], e4[nsh]);
   }
   __syncwarp();
-  for (int m = 0; m < n; ++m) {
-    const double pb = L.pair[2 * m], pa = L.pair[2 * m + 1];
-    e = fold == kFoldWangLandau ? __dadd_rn(__dsub_rn(e, pb), pa) : __dadd_rn(e, __dsub_rn(pa, pb));
+  if (fold == kFoldWangLandau) {
+    // e = (e - pair_before) + pair_after, two dependent adds per move
+    for (int m = 0; m < n; ++m) e = __dadd_rn(__dsub_rn(e, L.pair[2 * m]), L.pair[2 * m + 1]);
+  } else {
+    // e = e + (pair_after - pair_before): the differences are independent of
+    // e, so the lanes take them first and the chain is one add per move
+    for (int m = lane; m < n; m += 32) L.part[m] = __dsub_rn(L.pair[2 * m + 1], L.pair[2 * m]);
+    __syncwarp();
+    for (int m = 0; m < n; ++m) e = __dadd_rn(e, L.part[m]);
   }
   __syncwarp();
   return e;
