@@ -92,6 +92,7 @@ def load(rebuild: bool = False):
         "brawl_site_energy": ([vp, vp, vp], i),
         "brawl_pair_energy": ([vp, vp, vp, vp], i),
         "brawl_metropolis_run": ([vp, d, i64, i, vp], i),
+        "brawl_anneal_sweeps": ([vp, d, i64, i64, i, vp, vp], i),
         "brawl_lattice_shells": ([vp, i, vp], i),
         "brawl_radial_densities": ([vp, i, vp, vp], i),
         "brawl_counters": ([vp, vp], i),
@@ -168,6 +169,7 @@ def load(rebuild: bool = False):
         "brawl_batch_radial_densities": ([vp, i, i, vp, vp], i),
         "brawl_batch_sampling_reset": ([vp, i], i),
         "brawl_batch_energy_sample": ([vp, vp], i),
+        "brawl_batch_anneal_sweeps": ([vp, i64, i64, i, vp, vp], i),
         "brawl_batch_asro_sample": ([vp, i, vp, vp], i),
         "brawl_batch_temperature_stats": ([vp, i64, i64, d, d, i, vp, vp], i),
         "brawl_batch_asro_stats": ([vp, i64, vp, vp], i),
@@ -321,6 +323,18 @@ class Chain:
         _check(load().brawl_metropolis_run(self._h, float(beta), int(n_trials), int(bool(nbr_swap)),
                                            C.byref(acc)))
         return acc.value
+
+    def anneal_sweeps(self, beta: float, n_sweeps: int, sweep_trials: int, nbr_swap: bool = False,
+                      energies: bool = True):
+        """n_sweeps blocks of sweep_trials trials, the total energy after
+        each block (the annealing loop's samples); returns (energies or
+        None, accepted moves)."""
+        out = np.zeros(int(n_sweeps), dtype=np.float64) if energies else None
+        acc = C.c_int64()
+        _check(load().brawl_anneal_sweeps(self._h, float(beta), int(n_sweeps), int(sweep_trials),
+                                          int(bool(nbr_swap)), None if out is None else _ptr(out),
+                                          C.byref(acc)))
+        return out, acc.value
 
     def counters(self) -> dict:
         c = np.zeros(NUM_COUNTERS, dtype=np.int64)
@@ -569,6 +583,18 @@ class Batch:
         out = np.zeros(self.n, dtype=np.float64) if energies else None
         _check(load().brawl_batch_energy_sample(self._h, None if out is None else _ptr(out)))
         return out
+
+    def anneal_sweeps(self, n_sweeps: int, sweep_trials: int, accumulate: bool = False,
+                      energies: bool = True):
+        """n_sweeps blocks of sweep_trials trials on every chain, each
+        chain's total energy after every block (added to the sampling sums
+        with accumulate); returns (energies[n_sweeps, n] or None, accepted
+        moves per chain)."""
+        out = np.zeros((int(n_sweeps), self.n), dtype=np.float64) if energies else None
+        acc = np.zeros(self.n, dtype=np.int64)
+        _check(load().brawl_batch_anneal_sweeps(self._h, int(n_sweeps), int(sweep_trials), int(bool(accumulate)),
+                                                None if out is None else _ptr(out), _ptr(acc)))
+        return out, acc
 
     def asro_sample(self, c: int, shells, rho: bool = True) -> np.ndarray | None:
         """Chain c's radial_densities added to its sums; returns them."""

@@ -388,6 +388,18 @@ struct brawl_batch {
   double* d_rho_sum = nullptr;
   double* d_rho_stats = nullptr;
   unsigned long long* d_mask = nullptr;  // ASRO class masks (64)
+  // anneal blocks (brawl_batch_anneal_sweeps): 3n energy jobs (the live
+  // lattices, then two snapshot buffers), the snapshots (2 x total sites),
+  // the sampled energies (sweeps x n), and the stream the energies run on
+  unsigned char* d_snap = nullptr;
+  size_t snap_cap = 0;
+  EnergyJob* d_snap_jobs = nullptr;
+  int8_t* d_snap_lat = nullptr;
+  double* d_traj = nullptr;
+  size_t traj_rows = 0;
+  cudaStream_t energy_stream = nullptr;
+  cudaEvent_t ev_snap[2] = {nullptr, nullptr};
+  cudaEvent_t ev_free[2] = {nullptr, nullptr};
 };
 
 struct brawl_ctx {
@@ -552,6 +564,22 @@ int run_metropolis(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, b
   return BRAWL_OK;
 }
 
+// Every chain's uploaded job (b->d_jobs) once on `stream`: the halo chains
+// per class or in one launch, the others in one launch of the plain kernel.
+int launch_sweep(brawl_batch* b, cudaStream_t stream) {
+  const int n = (int)b->jobs.size();
+  const int nh = b->n_halo_launch;
+  if (nh > 0 && b->per_class)
+    TRY(launch_classes(b, stream, -1));
+  else if (nh > 0)
+    launch_halo_chains(b->d_jobs, nh, b->halo_smem, b->halo_min_z, b->halo_max_z, b->spec_nc, b->max_optin,
+                       stream);
+  if (n - nh > 0)
+    launch_metropolis(b->d_jobs + nh, n - nh, b->smem_lat, b->use_D, b->smem_bytes, b->max_z, stream);
+  CUDA_TRY(cudaGetLastError());
+  return BRAWL_OK;
+}
+
 int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accepted, bool serial,
                         cudaStream_t stream, bool wait) {
   const int n = (int)b->jobs.size();
@@ -568,8 +596,10 @@ int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accept
     CUDA_TRY(cudaStreamWaitEvent(stream, ev, 0));
     cudaEventDestroy(ev);
   }
-  const int nh = b->n_halo_launch;
-  if (serial) {
+  if (!serial) {
+    TRY(launch_sweep(b, stream));
+  } else {
+    const int nh = b->n_halo_launch;
     for (int k = 0; k < n; ++k) {
       if (k < nh)
         launch_halo_chains(b->d_jobs + k, 1, b->halo_smem, b->halo_min_z, b->halo_max_z, b->spec_nc, b->max_optin,
@@ -580,16 +610,6 @@ int run_metropolis_once(brawl_batch* b, const int64_t* n_trials, int64_t* accept
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(stream_wait(stream));
     }
-  } else {
-    if (nh > 0 && b->per_class)
-      TRY(launch_classes(b, stream, -1));
-    else if (nh > 0)
-      launch_halo_chains(b->d_jobs, nh, b->halo_smem, b->halo_min_z, b->halo_max_z, b->spec_nc,
-                         b->max_optin, stream);
-    if (n - nh > 0)
-      launch_metropolis(b->d_jobs + nh, n - nh, b->smem_lat, b->use_D, b->smem_bytes, b->max_z,
-                        stream);
-    CUDA_TRY(cudaGetLastError());
   }
   if (!wait) return BRAWL_OK;
   CUDA_TRY(stream_wait(stream));
@@ -810,9 +830,16 @@ int brawl_batch_destroy(brawl_batch* b) {
   if (b->stream) {
     for (const void* p : {(const void*)b->arena, (const void*)b->d_site_e, (const void*)b->d_grid,
                           (const void*)b->d_grids, (const void*)b->d_gjobs, (const void*)b->d_scratch,
-                          (const void*)b->d_alro, (const void*)b->d_alro_off, (const void*)b->d_samp})
+                          (const void*)b->d_alro, (const void*)b->d_alro_off, (const void*)b->d_samp,
+                          (const void*)b->d_snap, (const void*)b->d_traj})
       dfree(p, b->stream);
     stream_wait(b->stream);
+    if (b->energy_stream) {
+      stream_wait(b->energy_stream);
+      cudaStreamDestroy(b->energy_stream);
+    }
+    for (cudaEvent_t ev : {b->ev_snap[0], b->ev_snap[1], b->ev_free[0], b->ev_free[1]})
+      if (ev) cudaEventDestroy(ev);
     for (size_t k = 0; k < b->side.size(); ++k) {
       stream_wait(b->side[k]);
       cudaEventDestroy(b->ev_side[k]);
@@ -1351,12 +1378,128 @@ int brawl_batch_energy_sample(brawl_batch* b, double* energies) {
   if (!b->d_samp) return fail(BRAWL_EINVAL, "brawl_batch_sampling_reset first");
   const int n = (int)b->jobs.size();
   TRY(queue_batch_energy(b));
-  launch_energy_accumulate(b->d_energy, b->d_sums, n, b->stream);
+  launch_energy_accumulate(b->d_energy, b->d_sums, nullptr, n, b->stream);
   CUDA_TRY(cudaGetLastError());
   if (energies)
     CUDA_TRY(cudaMemcpyAsync(energies, b->d_energy, n * 8, cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(stream_wait(b->stream));
   return BRAWL_OK;
+}
+
+// The energy jobs of the live lattices and of the two snapshot buffers, the
+// site-energy scratch, the snapshots and n_rows rows of sampled energies;
+// returns the batch's total and largest site counts.
+static int ensure_anneal_block(brawl_batch* b, int64_t n_rows, int64_t& total_sites, int& max_sites) {
+  const int n = (int)b->jobs.size();
+  total_sites = 0;
+  max_sites = 0;
+  for (int c = 0; c < n; ++c) {
+    total_sites += b->models[c].g.n_sites;
+    max_sites = std::max(max_sites, (int)b->models[c].g.n_sites);
+  }
+  if ((size_t)total_sites * 8 > b->site_e_cap) {
+    dfree(b->d_site_e, b->stream);
+    b->d_site_e = nullptr;
+    b->site_e_cap = 0;
+    CUDA_TRY(dalloc(&b->d_site_e, (size_t)total_sites * 8, b->stream));
+    b->site_e_cap = (size_t)total_sites * 8;
+  }
+  const size_t jobs_bytes = ((size_t)3 * n * sizeof(EnergyJob) + 255) / 256 * 256;
+  const size_t need = jobs_bytes + 2 * (size_t)total_sites;
+  if (need > b->snap_cap) {
+    dfree(b->d_snap, b->stream);
+    b->d_snap = nullptr;
+    b->snap_cap = 0;
+    CUDA_TRY(dalloc(&b->d_snap, need, b->stream));
+    b->snap_cap = need;
+  }
+  b->d_snap_jobs = reinterpret_cast<EnergyJob*>(b->d_snap);
+  b->d_snap_lat = reinterpret_cast<int8_t*>(b->d_snap + jobs_bytes);
+  if ((size_t)n_rows > b->traj_rows) {
+    dfree(b->d_traj, b->stream);
+    b->d_traj = nullptr;
+    b->traj_rows = 0;
+    CUDA_TRY(dalloc(&b->d_traj, (size_t)n_rows * n * 8, b->stream));
+    b->traj_rows = (size_t)n_rows;
+  }
+  if (!b->energy_stream) {
+    CUDA_TRY(object_stream(&b->energy_stream));
+    for (cudaEvent_t* ev : {&b->ev_snap[0], &b->ev_snap[1], &b->ev_free[0], &b->ev_free[1]})
+      CUDA_TRY(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  }
+  std::vector<EnergyJob> ej((size_t)3 * n);
+  int64_t off = 0;
+  for (int c = 0; c < n; ++c) {
+    EnergyJob j;
+    j.g = b->models[c].g;
+    j.lat = b->jobs[c].lat;
+    j.V = b->jobs[c].V;
+    j.entries = b->jobs[c].entries;
+    j.shell_start = b->jobs[c].shell_start;
+    j.site_energy = b->d_site_e + off;
+    j.out = b->d_energy + c;
+    j.site_offset = off;
+    ej[c] = j;
+    for (int k = 0; k < 2; ++k) {
+      j.lat = b->d_snap_lat + (size_t)k * total_sites + off;
+      ej[(size_t)(1 + k) * n + c] = j;
+    }
+    off += j.g.n_sites;
+  }
+  CUDA_TRY(cudaMemcpyAsync(b->d_snap_jobs, ej.data(), ej.size() * sizeof(EnergyJob), cudaMemcpyHostToDevice,
+                           b->stream));
+  return BRAWL_OK;
+}
+
+int brawl_batch_anneal_sweeps(brawl_batch* b, int64_t n_sweeps, int64_t sweep_trials, int accumulate,
+                              double* energies, int64_t* accepted) {
+  if (!b || n_sweeps < 0 || sweep_trials < 0 || sweep_trials > kMaxLaunchTrials)
+    return fail(BRAWL_EINVAL, "bad argument");
+  const int n = (int)b->jobs.size();
+  if (n_sweeps > ((int64_t)1 << 28) / n) return fail(BRAWL_EINVAL, "too many sweeps for one block");
+  if (accumulate && !b->d_samp) return fail(BRAWL_EINVAL, "brawl_batch_sampling_reset first");
+  const bool sample = accumulate || energies;
+  for (int c = 0; c < n; ++c) {
+    b->jobs[c].n_trials = sweep_trials;
+    b->jobs[c].nbr_swap = b->nbr_swap[c];
+  }
+  TRY(upload_jobs(b));
+  int64_t total_sites = 0;
+  int max_sites = 0;
+  if (sample) TRY(ensure_anneal_block(b, std::max<int64_t>(n_sweeps, 1), total_sites, max_sites));
+  cudaStream_t ms = b->stream, es = b->energy_stream;
+  // sweep i's lattices go to snapshot buffer i % 2; its energies run on the
+  // energy stream while sweep i + 1 runs, and the buffer is written again
+  // (sweep i + 2) only after they have read it
+  for (int64_t i = 0; i < n_sweeps; ++i) {
+    TRY(launch_sweep(b, ms));
+    if (!sample) continue;
+    const int k = (int)(i & 1);
+    if (i >= 2) CUDA_TRY(cudaStreamWaitEvent(ms, b->ev_free[k], 0));
+    launch_lattice_snapshot(b->d_snap_jobs, b->d_snap_jobs + (size_t)(1 + k) * n, n, max_sites, ms);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(b->ev_snap[k], ms));
+    CUDA_TRY(cudaStreamWaitEvent(es, b->ev_snap[k], 0));
+    launch_total_energy(b->d_snap_jobs + (size_t)(1 + k) * n, n, total_sites, es);
+    launch_energy_accumulate(b->d_energy, accumulate ? b->d_sums : nullptr,
+                             energies ? b->d_traj + (size_t)i * n : nullptr, n, es);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(b->ev_free[k], es));
+  }
+  if (sample && n_sweeps > 0) {
+    CUDA_TRY(cudaStreamWaitEvent(ms, b->ev_free[(n_sweeps - 1) & 1], 0));
+    if (energies)
+      CUDA_TRY(cudaMemcpyAsync(energies, b->d_traj, (size_t)n_sweeps * n * 8, cudaMemcpyDeviceToHost, ms));
+  }
+  CUDA_TRY(stream_wait(ms));
+  std::vector<unsigned long long> cnt;
+  TRY(read_counters(b, cnt));
+  if (accepted)
+    for (int c = 0; c < n; ++c)
+      accepted[c] = (int64_t)(cnt[c * kNumCounters + kCntAccepted] -
+                              b->last_counters[c * kNumCounters + kCntAccepted]);
+  b->last_counters = cnt;
+  return check_status(b);
 }
 
 int brawl_batch_asro_sample(brawl_batch* b, int c, const double* shells, double* rho) {
@@ -1625,6 +1768,15 @@ int brawl_metropolis_run(brawl_ctx* ctx, double beta, int64_t n_trials, int nbr_
   set_beta(b->jobs[0], b->models[0], beta);
   b->nbr_swap[0] = nbr_swap ? 1 : 0;
   return run_metropolis(b, &n_trials, accepted, false, b->stream, true);
+}
+
+int brawl_anneal_sweeps(brawl_ctx* ctx, double beta, int64_t n_sweeps, int64_t sweep_trials, int nbr_swap,
+                        double* energies, int64_t* accepted) {
+  if (!ctx) return fail(BRAWL_EINVAL, "null argument");
+  brawl_batch* b = ctx->b;
+  set_beta(b->jobs[0], b->models[0], beta);
+  b->nbr_swap[0] = nbr_swap ? 1 : 0;
+  return brawl_batch_anneal_sweeps(b, n_sweeps, sweep_trials, 0, energies, accepted);
 }
 
 int brawl_lattice_shells(brawl_ctx* ctx, int wc_range, double* shells) {

@@ -121,7 +121,7 @@ __host__ __device__ inline HaloLayout halo_layout(const Geom& g, const HaloGeom&
 int lane_entries_for(int max_z);
 
 // Sampling reductions of the annealing loop on the device (sampling.cu).
-void launch_energy_accumulate(const double* d_e, double* d_sums, int n, cudaStream_t s);
+void launch_energy_accumulate(const double* d_e, double* d_sums, double* d_traj, int n, cudaStream_t s);
 void launch_acceptance_snapshot(const unsigned long long* d_counters, unsigned long long* d_acc0, int n,
                                 cudaStream_t s);
 void launch_asro_finish(const unsigned long long* d_counts, const unsigned long long* d_mask, int n_class,
@@ -268,6 +268,11 @@ struct EnergyJob {
 };
 void launch_total_energy(const EnergyJob* d_jobs, int n_jobs, int64_t total_sites,
                          cudaStream_t stream);
+// Every job's compact lattice (n_sites bytes) copied from src[c].lat to
+// dst[c].lat: the snapshot an energy on another stream reads while the
+// chains move on.
+void launch_lattice_snapshot(const EnergyJob* d_src, const EnergyJob* d_dst, int n_jobs, int max_sites,
+                             cudaStream_t stream);
 
 // Site energy of one site (nbr_energy), one thread.
 void launch_site_energy(const EnergyJob* d_job, int x, int y, int z, double* out,

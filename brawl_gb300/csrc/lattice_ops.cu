@@ -84,6 +84,26 @@ void launch_total_energy(const EnergyJob* d_jobs, int n_jobs, int64_t total_site
   sum_sites_kernel<<<(n_jobs + kSumWarps - 1) / kSumWarps, 32 * kSumWarps, 0, stream>>>(d_jobs, n_jobs);
 }
 
+// One block row per job (blockIdx.y), the sites strided over the row's
+// blocks.
+__global__ void lattice_snapshot_kernel(const EnergyJob* __restrict__ src, const EnergyJob* __restrict__ dst) {
+  const int c = blockIdx.y;
+  const int n = src[c].g.n_sites;
+  const int8_t* __restrict__ from = src[c].lat;
+  int8_t* __restrict__ to = const_cast<int8_t*>(dst[c].lat);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) to[i] = from[i];
+}
+
+void launch_lattice_snapshot(const EnergyJob* d_src, const EnergyJob* d_dst, int n_jobs, int max_sites,
+                             cudaStream_t stream) {
+  if (n_jobs <= 0) return;
+  BRAWL_CARVEOUT(lattice_snapshot_kernel);
+  const int bx = std::min(8, (max_sites + 255) / 256);
+  for (int base = 0; base < n_jobs; base += 65535)  // gridDim.y <= 65535
+    lattice_snapshot_kernel<<<dim3(bx, std::min(65535, n_jobs - base)), 256, 0, stream>>>(d_src + base,
+                                                                                        d_dst + base);
+}
+
 __global__ void one_site_energy_kernel(const EnergyJob* __restrict__ job, int x, int y, int z,
                                        double* out) {
   *out = site_energy_ref(job->g, job->lat, job->V, job->entries, job->shell_start, x, y, z);
@@ -256,6 +276,7 @@ void preload_lattice_kernels() {
   cudaFuncGetAttributes(&a, initial_setup_kernel);
   cudaFuncGetAttributes(&a, site_energies_kernel);
   cudaFuncGetAttributes(&a, sum_sites_kernel);
+  cudaFuncGetAttributes(&a, lattice_snapshot_kernel);
   cudaFuncGetAttributes(&a, pack_kernel);
   cudaFuncGetAttributes(&a, unpack_kernel);
   cudaFuncGetAttributes(&a, pack_batch_kernel);

@@ -19,14 +19,18 @@
 
 namespace brawl {
 
-// step_E += E, step_Esq += E * E (src/metropolis.F90:363-367)
+// step_E += E, step_Esq += E * E (src/metropolis.F90:363-367) when sums is
+// set; the energy also copied to a trajectory row when traj is set
 __global__ void energy_accumulate_kernel(const double* __restrict__ e, double* __restrict__ sums,
-                                         int n) {
+                                         double* __restrict__ traj, int n) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
   const double E = e[c];
-  sums[c] = __dadd_rn(sums[c], E);
-  sums[n + c] = __dadd_rn(sums[n + c], __dmul_rn(E, E));
+  if (sums) {
+    sums[c] = __dadd_rn(sums[c], E);
+    sums[n + c] = __dadd_rn(sums[n + c], __dmul_rn(E, E));
+  }
+  if (traj) traj[c] = E;
 }
 
 // the accepted-move counters at the start of the sampling loop
@@ -109,9 +113,9 @@ __global__ void asro_stats_kernel(int n, int m, const double* __restrict__ rho_s
   }
 }
 
-void launch_energy_accumulate(const double* d_e, double* d_sums, int n, cudaStream_t s) {
+void launch_energy_accumulate(const double* d_e, double* d_sums, double* d_traj, int n, cudaStream_t s) {
   BRAWL_CARVEOUT(energy_accumulate_kernel);
-  energy_accumulate_kernel<<<(n + 127) / 128, 128, 0, s>>>(d_e, d_sums, n);
+  energy_accumulate_kernel<<<(n + 127) / 128, 128, 0, s>>>(d_e, d_sums, d_traj, n);
 }
 
 void launch_acceptance_snapshot(const unsigned long long* d_counters, unsigned long long* d_acc0, int n,

@@ -24,6 +24,21 @@ def _f32_floor_div(a: int, b: int) -> int:
     return int(np.floor(np.float32(a) / np.float32(b)))
 
 
+def _block_end(m, i: int, n_sweeps: int, n_sweep_steps: int) -> int:
+    """The last sweep of the device block starting at sweep i: the first
+    sweep from i on after which ASRO or ALRO is sampled (those read the
+    configuration on the host), else the temperature's last sweep."""
+    j = i
+    while j < n_sweeps:
+        step_n = j * n_sweep_steps
+        if m.calculate_asro and step_n % m.n_sample_steps_asro == 0:
+            break
+        if m.calculate_alro and step_n % m.n_sample_steps_alro == 0:
+            break
+        j += 1
+    return j
+
+
 def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs: bool = True):
     """Runs the annealing on a chain whose configuration and stream are
     already set (initial_setup or a read configuration).  `metropolis` is a
@@ -72,11 +87,20 @@ def simulated_annealing(chain: Chain, metropolis, wc_range: int, record_configs:
         n_sweeps = m.n_mc_steps // m.n_sample_steps
         n_sweep_steps = m.n_mc_steps // n_sweeps
         accepted = 0
+        block_E = None
+        block_end = 0
         for i in range(1, n_sweeps + 1):
-            accepted += chain.metropolis(beta, n_sweep_steps, m.nbr_swap)
+            if i > block_end:
+                # the sweeps up to the next ASRO / ALRO sample run as one
+                # device block, their energies sampled on the device
+                block_end = _block_end(m, i, n_sweeps, n_sweep_steps)
+                block_E, acc = chain.anneal_sweeps(beta, block_end - i + 1, n_sweep_steps, m.nbr_swap,
+                                                   energies=bool(m.calculate_energies))
+                block_first = i
+                accepted += acc
             step_n = i * n_sweep_steps
             if m.calculate_energies:
-                current_energy = chain.total_energy()
+                current_energy = float(block_E[i - block_first])
                 step_E = step_E + current_energy
                 step_Esq = step_Esq + current_energy * current_energy
             if m.calculate_asro and step_n % m.n_sample_steps_asro == 0:
@@ -215,11 +239,20 @@ def simulated_annealing_ensemble(batch: Batch, metropolis, wc_range: int, record
                 o["initial_configs"].append(batch.config(c))
         n_sweeps = m.n_mc_steps // m.n_sample_steps
         n_sweep_steps = m.n_mc_steps // n_sweeps
+        block_E = None
+        block_end = 0
         for i in range(1, n_sweeps + 1):
-            batch.metropolis(n_sweep_steps)
+            if i > block_end:
+                # the sweeps up to the next ASRO / ALRO sample run as one
+                # device block, their energies sampled on the device
+                block_end = _block_end(m, i, n_sweeps, n_sweep_steps)
+                block_E, _ = batch.anneal_sweeps(block_end - i + 1, n_sweep_steps,
+                                                 accumulate=bool(m.calculate_energies),
+                                                 energies=bool(m.calculate_energies))
+                block_first = i
             step_n = i * n_sweep_steps
             if m.calculate_energies:
-                energy = batch.energy_sample()
+                energy = block_E[i - block_first]
             if m.calculate_asro and step_n % m.n_sample_steps_asro == 0:
                 asro = [batch.asro_sample(c, shells[c]) for c in range(n)]
             if m.calculate_alro and step_n % m.n_sample_steps_alro == 0:

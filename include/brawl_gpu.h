@@ -116,6 +116,16 @@ int brawl_pair_energy(brawl_ctx *ctx, const int idx1[4], const int idx2[4], doub
  * their accept results, i.e. what the reference adds to `acceptance`. */
 int brawl_metropolis_run(brawl_ctx *ctx, double beta, int64_t n_trials, int nbr_swap,
                          int64_t *accepted);
+/* The sweep loop of metropolis_simulated_annealing with its energy samples
+ * (src/metropolis.F90:348-367): n_sweeps blocks of sweep_trials trials at
+ * inverse temperature beta, and after each block the chain's total_energy,
+ * written to energies[n_sweeps] (may be NULL: no energies).  The blocks run
+ * back to back on the device; each block's energy is taken from a copy of
+ * the lattice while the next block runs.  accepted (may be NULL) receives
+ * the accepted moves of all blocks.  Trajectory and results are what
+ * n_sweeps pairs of brawl_metropolis_run + brawl_total_energy give. */
+int brawl_anneal_sweeps(brawl_ctx *ctx, double beta, int64_t n_sweeps, int64_t sweep_trials, int nbr_swap,
+                        double *energies, int64_t *accepted);
 
 /* lattice_shells (src/analytics.f90:205-275) of the current config. */
 int brawl_lattice_shells(brawl_ctx *ctx, int wc_range, double *shells);
@@ -238,6 +248,14 @@ int brawl_batch_set_configs(brawl_batch *batch, const int8_t *configs);
  * gets them in the layout of brawl_batch_radial_densities). */
 int brawl_batch_sampling_reset(brawl_batch *batch, int wc_range);
 int brawl_batch_energy_sample(brawl_batch *batch, double *energies);
+/* brawl_anneal_sweeps for every chain of a batch (each at its own beta and
+ * nbr_swap): n_sweeps blocks of sweep_trials trials per chain; after each
+ * block every chain's total_energy goes to energies[sweep * n + chain]
+ * (when not NULL) and, with accumulate = 1, into the sampling sums as
+ * brawl_batch_energy_sample adds it.  accepted[n] (may be NULL) receives
+ * each chain's accepted moves over all blocks. */
+int brawl_batch_anneal_sweeps(brawl_batch *batch, int64_t n_sweeps, int64_t sweep_trials, int accumulate,
+                              double *energies, int64_t *accepted);
 int brawl_batch_asro_sample(brawl_batch *batch, int chain, const double *shells, double *rho);
 /* The temperature's results (src/metropolis.F90:410-428): per_chain[3n] =
  * energies_of_T (n), C_of_T (n), acceptance_of_T (n), computed on the

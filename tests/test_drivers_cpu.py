@@ -26,6 +26,15 @@ class OracleChain:
     def total_energy(self):
         return self.mod.total_energy(self.cfg)
 
+    def anneal_sweeps(self, beta, n_sweeps, sweep_trials, nbr_swap=False, energies=True):
+        E = np.zeros(n_sweeps) if energies else None
+        acc = 0
+        for i in range(n_sweeps):
+            acc += self.metropolis(beta, sweep_trials, nbr_swap)
+            if energies:
+                E[i] = self.total_energy()
+        return E, acc
+
     def config(self):
         return self.cfg.copy()
 

@@ -576,3 +576,53 @@ def test_classes_run_their_own_depths_and_autotune_keeps_state():
     acc2 = b.metropolis(np.array([e[0] - h for e, h in zip(expect, half)]))
     for k, (t, cfg, a, c) in enumerate(expect):
         assert acc1[k] + acc2[k] == a and np.array_equal(b.config(k), cfg), Ls[k]
+
+
+def test_anneal_sweeps_equal_per_sweep_calls():
+    """brawl_anneal_sweeps / brawl_batch_anneal_sweeps (sweeps back to back,
+    each sweep's energy taken from a snapshot on another stream) give the
+    energies, accepted counts, configurations and streams of one
+    metropolis call + one total_energy call per sweep; with accumulate the
+    sampling sums are brawl_batch_energy_sample's."""
+    rng = np.random.default_rng(71)
+    V = random_V(rng, 2, 2)
+    setup = B.Setup("fcc", 4, 4, 4, 2, 2)
+    beta = 1.0 / (700.0 * B.K_B_IN_RY)
+    a, b_ = B.Chain(setup, V), B.Chain(setup, V)
+    for ch in (a, b_):
+        ch.seed(4242)
+        ch.initial_setup(conc_vector(2), equi_numbers(setup.n_atoms, 2))
+    sweep = setup.n_atoms
+    E_ref, acc_ref = [], 0
+    for _ in range(9):
+        acc_ref += a.metropolis(beta, sweep)
+        E_ref.append(a.total_energy())
+    E, acc = b_.anneal_sweeps(beta, 9, sweep)
+    assert acc == acc_ref and np.array_equal(E, np.array(E_ref))
+    assert np.array_equal(a.config(), b_.config()) and np.array_equal(a.rng_state(), b_.rng_state())
+    E0, acc0 = b_.anneal_sweeps(beta, 3, sweep, energies=False)
+    acc_ref = sum(a.metropolis(beta, sweep) for _ in range(3))
+    assert E0 is None and acc0 == acc_ref and np.array_equal(a.config(), b_.config())
+
+    # a batch of two classes (different L) with their own betas, sums on the device
+    V4 = random_V(rng, 4, 6)
+    chains = []
+    for r, L in enumerate([4, 5, 4]):
+        chains.append(dict(setup=B.Setup("bcc", L, L, L, 4, 6), V=V4, seed=110179 + 11 * r,
+                           beta=1.0 / ((400.0 + 300.0 * r) * B.K_B_IN_RY), species_concentrations=conc_vector(4)))
+    p2, q2 = B.Batch(chains), B.Batch(chains)
+    q2.set_class_depths([2, 1])  # per-class launches, the L = 4 class two trials per round
+    n = min(c["setup"].n_atoms for c in chains)
+    for x in (p2, q2):
+        x.sampling_reset(0)
+    E_ref, acc_ref = [], np.zeros(3, dtype=np.int64)
+    for _ in range(6):
+        acc_ref += p2.metropolis(np.full(3, n))
+        E_ref.append(p2.energy_sample())
+    E, acc = q2.anneal_sweeps(6, n, accumulate=True)
+    assert np.array_equal(E, np.array(E_ref)) and np.array_equal(acc, acc_ref)
+    for k in range(3):
+        assert np.array_equal(p2.config(k), q2.config(k))
+    s_p = p2.temperature_stats(6, 6 * n, 500.0, 500.0 * B.K_B_IN_RY, True)
+    s_q = q2.temperature_stats(6, 6 * n, 500.0, 500.0 * B.K_B_IN_RY, True)
+    assert np.array_equal(s_p[0], s_q[0]) and np.array_equal(s_p[1], s_q[1])
