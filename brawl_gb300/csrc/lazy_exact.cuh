@@ -254,107 +254,164 @@ __device__ __forceinline__ double lazy_term(const LazyLog& L, const double* Vsh,
   return Vsh[(cs - 1) + ns * (lazy_species(L, at, s_before, s_after, after) - 1)];
 }
 
-// The exact energies of the n logged moves folded into e (the walker's
-// exact energy before the first of them).  All lanes; returns the same value
-// in every lane.
-static __device__ __noinline__ double lazy_flush(const Geom& g, const double* V, const int16_t* sstart,
-                                                 LazyLog L, int n, double e, int fold, int lane) {
+// bar.sync on named barrier `id` for `count` threads (a multiple of 32):
+// the warps of a block that share a deferred-energy log meet there.
+__device__ __forceinline__ void named_barrier(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// The site energies of the n logged moves, summed by `nthreads` threads
+// (this one is tid), ILP chains per thread in flight.  Chain c = 4 m + ev is
+// evaluation ev of move m (site 1 before, site 2 before, site 1 after, site
+// 2 after); it adds each shell's terms in list order from 0.0 and the shell
+// sums left to right (nbr_energy).  The four chains of a move sit in four
+// neighbouring lanes (c = tid mod 4), so the pair energies site 1 + site 2
+// (pair_energy) are taken through shuffles and written to L.pair[2 m +
+// after]; for the nested fold the differences pair_after - pair_before go to
+// L.part[m].
+template <int ILP>
+__device__ __forceinline__ void lazy_sites(const Geom& g, const double* V, const int16_t* sstart,
+                                           const LazyLog& L, int n, int fold, int tid, int nthreads) {
   const int z = g.z, nsh = g.nsh, ns = g.ns;
-  const int nch = 4 * n;  // chains per shell: (move, evaluation)
-  for (int sh = 0; sh < nsh; ++sh) {
-    const int k0 = sstart[sh], len = sstart[sh + 1] - k0;
-    const double* Vsh = V + ns * ns * sh;
-    for (int c0 = 0; c0 < nch; c0 += 32 * kLazyIlp) {
-      double sum[kLazyIlp];
-      int row[kLazyIlp], cs[kLazyIlp], s_before[kLazyIlp], s_after[kLazyIlp];
-      bool on[kLazyIlp], after[kLazyIlp];
+  const int nch = 4 * n;
+  for (int c0 = 0; c0 < nch; c0 += nthreads * ILP) {
+    int row[ILP], cs[ILP], s_before[ILP], s_after[ILP];
+    bool on[ILP], after[ILP];
+    double site[ILP];
 #pragma unroll
-      for (int i = 0; i < kLazyIlp; ++i) {
-        const int c = c0 + 32 * i + lane;
-        on[i] = c < nch;
-        const int m = on[i] ? c >> 2 : 0, ev = c & 3;
-        const bool site2 = ev & 1;
-        after[i] = ev >= 2;
-        const int sa = L.spec[2 * m], sb = L.spec[2 * m + 1];
-        s_before[i] = site2 ? sb : sa;  // the site's own species before the move
-        s_after[i] = site2 ? sa : sb;
-        cs[i] = after[i] ? s_after[i] : s_before[i];
-        row[i] = m * 2 * z + (site2 ? z : 0) + k0;
-        sum[i] = 0.0;
-      }
+    for (int i = 0; i < ILP; ++i) {
+      const int c = c0 + nthreads * i + tid;
+      on[i] = c < nch;
+      const int m = on[i] ? c >> 2 : 0, ev = c & 3;
+      const bool site2 = ev & 1;
+      after[i] = ev >= 2;
+      const int sa = L.spec[2 * m], sb = L.spec[2 * m + 1];
+      s_before[i] = site2 ? sb : sa;  // the site's own species before the move
+      s_after[i] = site2 ? sa : sb;
+      cs[i] = after[i] ? s_after[i] : s_before[i];
+      row[i] = m * 2 * z + (site2 ? z : 0);
+      site[i] = 0.0;
+    }
+    for (int sh = 0; sh < nsh; ++sh) {
+      const int k0 = sstart[sh], len = sstart[sh + 1] - k0;
+      const double* Vsh = V + ns * ns * sh;
+      double sum[ILP];
+#pragma unroll
+      for (int i = 0; i < ILP; ++i) sum[i] = 0.0;
       int k = 0;
       // the terms of four neighbours of every chain are loaded before
-      // their adds, so the loads overlap and the adds issue back to back
-      // (FP64 adds are the bound: one warp add every 64 cycles per
-      // sub-partition); each chain still adds its terms in list order
+      // their adds, so the loads overlap and the adds issue back to back;
+      // each chain still adds its terms in list order
       for (; k + 4 <= len; k += 4) {
-        double t[kLazyIlp][4];
+        double t[ILP][4];
 #pragma unroll
-        for (int i = 0; i < kLazyIlp; ++i)
+        for (int i = 0; i < ILP; ++i)
 #pragma unroll
-          for (int u = 0; u < 4; ++u) t[i][u] = lazy_term(L, Vsh, row[i] + k + u, cs[i], s_before[i], s_after[i],
-                                                          after[i], on[i], ns);
+          for (int u = 0; u < 4; ++u)
+            t[i][u] = lazy_term(L, Vsh, row[i] + k0 + k + u, cs[i], s_before[i], s_after[i], after[i], on[i], ns);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
-          for (int i = 0; i < kLazyIlp; ++i) sum[i] = __dadd_rn(sum[i], t[i][u]);
+          for (int i = 0; i < ILP; ++i) sum[i] = __dadd_rn(sum[i], t[i][u]);
       }
       for (; k < len; ++k) {
 #pragma unroll
-        for (int i = 0; i < kLazyIlp; ++i)
-          sum[i] = __dadd_rn(sum[i], lazy_term(L, Vsh, row[i] + k, cs[i], s_before[i], s_after[i], after[i],
-                                               on[i], ns));
+        for (int i = 0; i < ILP; ++i)
+          sum[i] = __dadd_rn(sum[i], lazy_term(L, Vsh, row[i] + k0 + k, cs[i], s_before[i], s_after[i],
+                                               after[i], on[i], ns));
       }
+      // site energy: shell 1 + shell 2 + ... left to right
 #pragma unroll
-      for (int i = 0; i < kLazyIlp; ++i) {
-        const int c = c0 + 32 * i + lane;
-        if (on[i]) L.part[c * nsh + sh] = sum[i];
-      }
+      for (int i = 0; i < ILP; ++i) site[i] = sh == 0 ? sum[i] : __dadd_rn(site[i], sum[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < ILP; ++i) {
+      const int c = c0 + nthreads * i + tid;
+      const int ev = c & 3;
+      const double pr = __dadd_rn(site[i], __shfl_down_sync(kFull, site[i], 1));  // site 1 + site 2
+      if (on[i] && (ev & 1) == 0) L.pair[2 * (c >> 2) + (ev >> 1)] = pr;
+      const double pr_after = __shfl_down_sync(kFull, pr, 2);
+      if (fold == kFoldNested && on[i] && ev == 0) L.part[c >> 2] = __dsub_rn(pr_after, pr);
     }
   }
-  __syncwarp();
-  // site energies: shell 1 + shell 2 + ... left to right
-  for (int c0 = 0; c0 < nch; c0 += 32 * kLazyIlp) {
-    double acc[kLazyIlp];
-#pragma unroll
-    for (int i = 0; i < kLazyIlp; ++i) {
-      const int c = c0 + 32 * i + lane;
-      acc[i] = c < nch ? L.part[c * nsh] : 0.0;
-    }
-    for (int sh = 1; sh < nsh; ++sh) {
-#pragma unroll
-      for (int i = 0; i < kLazyIlp; ++i) {
-        const int c = c0 + 32 * i + lane;
-        if (c < nch) acc[i] = __dadd_rn(acc[i], L.part[c * nsh + sh]);
-      }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int i = 0; i < kLazyIlp; ++i) {
-      const int c = c0 + 32 * i + lane;
-      if (c < nch) L.part[c * nsh] = acc[i];
-    }
-  }
-  __syncwarp();
-  // pair energies: site 1 + site 2, before and after
-  for (int i = lane; i < 2 * n; i += 32) {
-    const int m = i >> 1, aft = i & 1;
-    const double* e4 = L.part + (size_t)(4 * m + 2 * aft) * nsh;
-    L.pair[i] = __dadd_rn(e4[0], e4[nsh]);
-  }
-  __syncwarp();
+}
+
+// lazy_sites with as many chains per thread as the log needs (1 to MaxIlp
+// in flight; more chains loop).  Out of line: flushes are rare next to the
+// steps.  One warp wants 8 chains per lane to keep its FP64 pipe busy;
+// four warps need no more than 4 (fewer registers).
+template <int MaxIlp>
+static __device__ __noinline__ void lazy_sites_any(const Geom& g, const double* V, const int16_t* sstart,
+                                                   LazyLog L, int n, int fold, int tid, int nthreads) {
+  const int per = (4 * n + nthreads - 1) / nthreads;
+  if (per <= 1) lazy_sites<1>(g, V, sstart, L, n, fold, tid, nthreads);
+  else if (per <= 2 || MaxIlp == 2) lazy_sites<2>(g, V, sstart, L, n, fold, tid, nthreads);
+  else if (per <= 4 || MaxIlp == 4) lazy_sites<4>(g, V, sstart, L, n, fold, tid, nthreads);
+  else lazy_sites<MaxIlp>(g, V, sstart, L, n, fold, tid, nthreads);
+}
+
+// The walker's energy e folded with the n moves' pair energies (one warp;
+// every lane returns the same value).
+static __device__ __noinline__ double lazy_fold(LazyLog L, int n, double e, int fold) {
   if (fold == kFoldWangLandau) {
     // e = (e - pair_before) + pair_after, two dependent adds per move
     for (int m = 0; m < n; ++m) e = __dadd_rn(__dsub_rn(e, L.pair[2 * m]), L.pair[2 * m + 1]);
   } else {
-    // e = e + (pair_after - pair_before): the differences are independent of
-    // e, so the lanes take them first and the chain is one add per move
-    for (int m = lane; m < n; m += 32) L.part[m] = __dsub_rn(L.pair[2 * m + 1], L.pair[2 * m]);
-    __syncwarp();
+    // e = e + (pair_after - pair_before): the differences were taken in
+    // parallel, so the chain is one add per move
     for (int m = 0; m < n; ++m) e = __dadd_rn(e, L.part[m]);
   }
   __syncwarp();
   return e;
+}
+
+// The exact energies of the n logged moves folded into e (the walker's
+// exact energy before the first of them), by one warp.  All lanes; returns
+// the same value in every lane.
+__device__ __forceinline__ double lazy_flush(const Geom& g, const double* V, const int16_t* sstart,
+                                             const LazyLog& L, int n, double e, int fold, int lane) {
+  lazy_sites_any<kLazyIlp>(g, V, sstart, L, n, fold, lane, 32);
+  __syncwarp();
+  return lazy_fold(L, n, e, fold);
+}
+
+// The same with the helper warps of the block: warp 0 posts the move count
+// in ctl[1] and meets the helpers at barrier 1, every thread sums its share
+// of the chains, barrier 2 closes, and warp 0 folds.  With one warp
+// (nthreads = 32) it is lazy_flush.
+__device__ __forceinline__ double lazy_flush_block(const Geom& g, const double* V, const int16_t* sstart,
+                                                   const LazyLog& L, int n, double e, int fold, int lane,
+                                                   int nthreads, volatile int* ctl) {
+  if (nthreads == 32) return lazy_flush(g, V, sstart, L, n, e, fold, lane);
+  if (lane == 0) {
+    ctl[0] = 1;
+    ctl[1] = n;
+  }
+  named_barrier(1, nthreads);
+  lazy_sites_any<4>(g, V, sstart, L, n, fold, lane, nthreads);
+  named_barrier(2, nthreads);
+  return lazy_fold(L, n, e, fold);
+}
+
+// The helper warps' side of lazy_flush_block (threads tid >= 32): wait at
+// barrier 1 for a flush (ctl[0] = 1) or the end (ctl[0] = 0), sum this
+// thread's chains, meet at barrier 2.
+__device__ __forceinline__ void lazy_helper_loop(const Geom& g, const double* V, const int16_t* sstart,
+                                                 const LazyLog& L, int fold, int tid, int nthreads,
+                                                 volatile int* ctl) {
+  for (;;) {
+    named_barrier(1, nthreads);
+    if (ctl[0] == 0) return;
+    lazy_sites_any<4>(g, V, sstart, L, ctl[1], fold, tid, nthreads);
+    named_barrier(2, nthreads);
+  }
+}
+
+// Warp 0's end of the helpers' loop.
+__device__ __forceinline__ void lazy_helpers_release(int lane, int nthreads, volatile int* ctl) {
+  if (nthreads == 32) return;
+  if (lane == 0) ctl[0] = 0;
+  named_barrier(1, nthreads);
 }
 
 }  // namespace brawl

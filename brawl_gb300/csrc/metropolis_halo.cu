@@ -70,6 +70,87 @@ __device__ __noinline__ int halo_exact_decision(const ChainJob* __restrict__ Jg,
   return acc | 2 | (st.fp64 ? 4 : 0) | (st.cr ? 8 : 0);
 }
 
+// The species of the neighbour at entry e of a site at padded index `base`
+// (relative to the staged lattice) with parity par, through the halo's
+// padded offsets (the plan's arithmetic, for any entry).
+__device__ __forceinline__ int halo_nbr_species(uint32_t e, int base, int par, int SZ, int SY, bool bcc) {
+  extern __shared__ int8_t s_i8[];
+  int dx, dy, dz, sh;
+  unpack_entry(e, dx, dy, dz, sh);
+  const int ddx = (par + dx) >> 1;
+  const int ddy = bcc ? ((par + dy) >> 1) : dy;
+  return s_i8[base + dz * SZ + ddy * SY + ddx];
+}
+
+// halo_exact_decision for a pair that is not near (the pairs halo_delta
+// takes): no neighbour of either site is the other, so every neighbour
+// holds the same species before and after the swap and is read through
+// the padded offsets.  Lane c < 4 nsh adds, in list order from 0.0, the
+// terms of shell c % nsh of evaluation c / nsh (site 1 before, site 2
+// before, site 1 after, site 2 after); the shell sums are then added in
+// shell order and the two sites' energies summed (nbr_energy and
+// pair_energy, src/bw_hamiltonian.f90:99-114) -- the values and order of
+// exact_pair_energies, so the same doubles.  The path runs on about one
+// trial in fifty to a thousand, so its code is kept short (rolled loops):
+// it is fetched cold each time.  The next four terms are loaded before the
+// adds of the current four.
+static __device__ __noinline__ int halo_exact_far(const ChainJob* __restrict__ Jg, const double* V,
+                                                  const uint32_t* ents, const int16_t* sstart, int lat_off,
+                                                  int SZ, int SY, int bcc, int ns, int nsh, int pa, int pb,
+                                                  int par_a, int par_b, int sa, int sb, uint32_t wu, int lane) {
+  const int nc = 4 * nsh;
+  double part[2] = {0.0, 0.0};
+#pragma unroll 1
+  for (int r = 0; r < 2; ++r) {
+    const int c = lane + 32 * r;
+    double sum = 0.0;
+    if (c < nc) {
+      const int ev = c / nsh, sh = c - ev * nsh;
+      const bool on2 = ev & 1, after = ev >= 2;
+      const int base = lat_off + (on2 ? pb : pa);
+      const int par = on2 ? par_b : par_a;
+      const int cs = (on2 != after) ? sb : sa;
+      // Vr[ns * s] = V(cs, s, sh) for the neighbour species s (1-based)
+      const double* Vr = V + (cs - 1) + ns * ns * sh - ns;
+      const int k1 = sstart[sh + 1];
+      double t[4] = {0.0, 0.0, 0.0, 0.0};
+      int n_prev = 0;  // terms held in t
+#pragma unroll 1
+      for (int k = sstart[sh];; k += 4) {
+        double x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          x[u] = k + u < k1 ? Vr[ns * halo_nbr_species(ents[k + u], base, par, SZ, SY, bcc)] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (u < n_prev) sum = __dadd_rn(sum, t[u]);
+        if (k >= k1) break;
+        n_prev = min(4, k1 - k);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t[u] = x[u];
+      }
+    }
+    part[r] = sum;
+  }
+  double e[4];
+#pragma unroll 1
+  for (int ev = 0; ev < 4; ++ev) {
+    double acc = 0.0;
+#pragma unroll 1
+    for (int sh = 0; sh < nsh; ++sh) {
+      const int c = ev * nsh + sh;
+      const double v = c < 32 ? __shfl_sync(kFull, part[0], c) : __shfl_sync(kFull, part[1], c - 32);
+      acc = sh == 0 ? v : __dadd_rn(acc, v);
+    }
+    e[ev & 3] = acc;
+  }
+  const double delta_e = __dsub_rn(__dadd_rn(e[2], e[3]), __dadd_rn(e[0], e[1]));
+  if (delta_e < 0.0) return 1;
+  DecideStats st = {0u, 0u};
+  const int acc = u_lt_exp(wu, __dmul_rn(-Jg->beta, delta_e), st);
+  return acc | 2 | (st.fp64 ? 4 : 0) | (st.cr ? 8 : 0);
+}
+
 // Log-domain acceptance thresholds: the uphill decision as two integer
 // compares of the fixed-point energy change against bounds taken from the
 // acceptance word (no exponential of the change).  The reference accepts an uphill move iff u < exp(-beta dE_ref)
@@ -213,7 +294,8 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
       // latency; a neighbouring pair (which the fast sum assumes away) takes
       // the general sum instead
       int dE = halo_delta<NJ, FULL>(g, lat_off, D_abs, P, pa, pb, par_a, par_b, p.sa, p.sb, lane);
-      if (pair_near_flat(g, H, p.ax, p.ay, p.az, p.bx, p.by, p.bz)) {
+      const bool near = pair_near_flat(g, H, p.ax, p.ay, p.az, p.bx, p.by, p.bz);
+      if (near) {
         dE = halo_delta_general(Jg, (int)L.ents, I_off, L.F_off, hl, p.ax, p.ay, p.az,
                                 p.az * g.sz + Ya * g.sy + Xa, p.bx, p.by, p.bz,
                                 p.bz * g.sz + Yb * g.sy + Xb, p.sa, p.sb, lane);
@@ -229,9 +311,11 @@ __global__ void __launch_bounds__(32) metropolis_halo_kernel(const ChainJob* __r
       }
       if (accept < 0) {
         ++b_exact;
-        const int r = halo_exact_decision(Jg, hl, V, ents, sstart, p.ax, p.ay, p.az,
-                                          p.az * g.sz + Ya * g.sy + Xa, p.bx, p.by, p.bz,
-                                          p.bz * g.sz + Yb * g.sy + Xb, p.sa, p.sb, lane, wu);
+        const int r = near ? halo_exact_decision(Jg, hl, V, ents, sstart, p.ax, p.ay, p.az,
+                                                 p.az * g.sz + Ya * g.sy + Xa, p.bx, p.by, p.bz,
+                                                 p.bz * g.sz + Yb * g.sy + Xb, p.sa, p.sb, lane, wu)
+                           : halo_exact_far(Jg, V, ents, sstart, lat_off, H.SZ, H.SY, bcc, g.ns, g.nsh, pa,
+                                            pb, par_a, par_b, p.sa, p.sb, wu, lane);
         accept = r & 1;
         consumed = (r & 2) ? n_base + 1 : n_base;
         c_fp64 += (r >> 2) & 1;

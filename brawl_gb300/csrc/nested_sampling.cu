@@ -97,13 +97,20 @@ __device__ __forceinline__ long long gap_up(double limit, double E, int S) {
 constexpr int kRedraws = 32;
 static_assert(3 * kRedraws <= kRingMirror, "redraw words must fit the ring's mirror");
 
+// Warps per run: warp 0 walks; the others join only the deferred-energy
+// flushes, whose FP64 sums are the step's largest cost (each sub-partition
+// of an SM has its own FP64 pipe, so four warps sum four times as fast).
+constexpr int kNsWarps = 4;
+
 template <int NJ, bool kUseD>
-__global__ void __launch_bounds__(32, 1) ns_iterate_kernel(NsRun* __restrict__ runs) {
+__global__ void __launch_bounds__(32 * kNsWarps, 1) ns_iterate_kernel(NsRun* __restrict__ runs) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_ctl[2];  // the flushes' command and move count (lazy_flush_block)
   NsRun& R = runs[blockIdx.x];
   const ChainJob& J = R.job;
   const Geom g = J.g;
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int nthreads = blockDim.x;
   const unsigned long long t_start = global_ns();
   const int n = g.n_sites;
   const int nV = g.ns * g.ns * g.nsh;
@@ -118,6 +125,11 @@ __global__ void __launch_bounds__(32, 1) ns_iterate_kernel(NsRun* __restrict__ r
   int8_t* lat = reinterpret_cast<int8_t*>(smem + WLy.lat);
   double* vbuf = reinterpret_cast<double*>(smem + WLy.vbuf);
   const LazyLog LG = lazy_layout(g, smem + WLy.lazy, R.lazy_cap);
+  if (threadIdx.x >= 32) {
+    // a helper warp: flushes only, until warp 0 releases it
+    lazy_helper_loop(g, V, sstart, LG, kFoldNested, threadIdx.x, nthreads, s_ctl);
+    return;
+  }
   const double q = ldexp(1.0, -R.S);
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
@@ -201,7 +213,7 @@ __global__ void __launch_bounds__(32, 1) ns_iterate_kernel(NsRun* __restrict__ r
     auto flush = [&]() {
       if (n_log == 0) return;
       const double E0 = E;
-      E = lazy_flush(g, V, sstart, LG, n_log, E, kFoldNested, lane);
+      E = lazy_flush_block(g, V, sstart, LG, n_log, E, kFoldNested, lane, nthreads, s_ctl);
       if (!in_quanta(E, E0, Dlo - Rs, Dhi + Rs, q)) status = kStatusBandViolated;
       n_log = 0;
       rebase();
@@ -314,6 +326,7 @@ __global__ void __launch_bounds__(32, 1) ns_iterate_kernel(NsRun* __restrict__ r
     if (lane == 0) R.energies[imax] = E;
     __syncwarp();
   }
+  lazy_helpers_release(lane, nthreads, s_ctl);
   ring_writeback(mt, tbuf, ring, J.rng, lane);
   if (lane == 0) {
     R.extra_steps = extra_steps;
@@ -350,7 +363,7 @@ static void launch_ns_nj(NsRun* d_runs, int n_runs, uint32_t smem_bytes, cudaStr
   cudaFuncSetAttribute(ns_iterate_kernel<NJ, kUseD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes);
   BRAWL_CARVEOUT(ns_iterate_kernel<NJ, kUseD>);
-  ns_iterate_kernel<NJ, kUseD><<<n_runs, 32, smem_bytes, stream>>>(d_runs);
+  ns_iterate_kernel<NJ, kUseD><<<n_runs, 32 * kNsWarps, smem_bytes, stream>>>(d_runs);
 }
 
 template <bool kUseD>
