@@ -114,13 +114,19 @@ __device__ __noinline__ void wl_store_config(const Geom& g, const int8_t* lat, i
   }
 }
 
+// Warps per walker: warp 0 walks; the others join only the deferred-energy
+// flushes (each sub-partition of an SM has its own FP64 pipe).
+constexpr int kWlWarps = 4;
+
 template <int NJ, bool kUseD>
-__global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ walkers) {
+__global__ void __launch_bounds__(32 * kWlWarps, 1) wl_sweep_kernel(WlWalker* __restrict__ walkers) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_ctl[2];  // the flushes' command and move count (lazy_flush_block)
   WlWalker& W = walkers[blockIdx.x];
   const ChainJob& J = W.job;
   const Geom g = J.g;
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int nthreads = blockDim.x;
   const unsigned long long t_start = global_ns();
   const int nV = g.ns * g.ns * g.nsh;
   const int nb = W.end - W.start + 1;
@@ -140,6 +146,11 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   int8_t* lat = reinterpret_cast<int8_t*>(smem + WLy.lat);
   double* vbuf = reinterpret_cast<double*>(smem + WLy.vbuf);
   const LazyLog LG = lazy_layout(g, smem + WLy.lazy, W.lazy_cap);
+  if (threadIdx.x >= 32) {
+    // a helper warp: flushes only, until warp 0 releases it
+    lazy_helper_loop(g, V, sstart, LG, kFoldWangLandau, threadIdx.x, nthreads, s_ctl);
+    return;
+  }
   for (int i = lane; i < kMTN; i += 32) mt[i] = J.rng[i];
   for (int i = lane; i < nV; i += 32) V[i] = J.V[i];
   for (int i = lane; i < WLy.nI - WLy.F_off; i += 32) F[i] = J.F[i];
@@ -219,7 +230,7 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
   auto flush = [&]() {
     if (n_log == 0) return;
     const double e0 = e_ex;
-    e_ex = lazy_flush(g, V, sstart, LG, n_log, e_ex, kFoldWangLandau, lane);
+    e_ex = lazy_flush_block(g, V, sstart, LG, n_log, e_ex, kFoldWangLandau, lane, nthreads, s_ctl);
     if (!in_quanta(e_ex, e0, Dlo - Rs, Dhi + Rs, q)) status = kStatusBandViolated;
     n_log = 0;
     rebase();
@@ -363,6 +374,7 @@ __global__ void __launch_bounds__(32, 1) wl_sweep_kernel(WlWalker* __restrict__ 
     ring_consume(ring, consumed);
   }
   flush();
+  lazy_helpers_release(lane, nthreads, s_ctl);
   const double e_un = e_ex;
 
   __syncwarp();
@@ -561,7 +573,7 @@ template <int NJ, bool kUseD>
 static void launch_wl_nj(WlWalker* d_walkers, int n, uint32_t smem, cudaStream_t stream) {
   cudaFuncSetAttribute(wl_sweep_kernel<NJ, kUseD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   BRAWL_CARVEOUT(wl_sweep_kernel<NJ, kUseD>);
-  wl_sweep_kernel<NJ, kUseD><<<n, 32, smem, stream>>>(d_walkers);
+  wl_sweep_kernel<NJ, kUseD><<<n, 32 * kWlWarps, smem, stream>>>(d_walkers);
 }
 
 template <bool kUseD>
