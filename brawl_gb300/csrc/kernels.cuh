@@ -219,36 +219,105 @@ struct InitJob {
 };
 void launch_initial_setup(const InitJob* d_jobs, int n_jobs, cudaStream_t stream);
 
-// The site-by-site draw loop of initial_setup for one configuration, on the
-// warp's stream (mt in shared memory at position pos); check is shared
-// scratch of kMaxSpecies counters.  Returns false when a quota can never be
-// met (guards against a corrupted job; the host validates counts).
+// The site-by-site draw loop of initial_setup for one configuration
+// (src/initialise.F90:434-617), on the warp's stream (mt in shared memory at
+// position pos); check is shared scratch of kMaxSpecies counters.  Every
+// word of the stream is one draw: species l + 1 when it falls in the
+// interval of species l whose count is below its quota (the last such l,
+// as the reference's loop over l leaves it), else no species and the site
+// draws again.  Accepted words fill the sites in order.
+//
+// The warp decides 32 consecutive words at once.  While no word in the
+// batch falls in two intervals and no quota can fill inside the batch
+// (check + the batch's words of that species <= count), every word's fate
+// is known from the counts at the batch's start: the accepted words take
+// the next sites in order (a ballot and a prefix count).  A batch where a
+// quota fills, or a word sits on two intervals, is decided word by word.
+// Returns false when a quota can never be met (guards against a corrupted
+// job; the host validates counts).
 __device__ inline bool initial_setup_warp(const InitJob& J, int8_t* lat, uint32_t* mt, int& pos,
                                           int64_t* check, unsigned long long& draws, int lane) {
   if (lane < kMaxSpecies) check[lane] = 0;
   __syncwarp();
   const int ns = J.ns;
-  const unsigned long long limit = draws + (unsigned long long)J.n_sites * 4096ull + 1000000ull;
-  for (int site = 0; site < J.n_sites; ++site) {
-    int s = 0;
-    while (s == 0) {
-      const uint32_t w = __shfl_sync(kFull, mt_peek(mt, pos, 1, lane), 0);
-      pos += 1;
-      ++draws;
-      const int64_t wl = (int64_t)w;
-      for (int l = 0; l < ns; ++l) {
+  const int n_sites = J.n_sites;
+  const unsigned long long limit = draws + (unsigned long long)n_sites * 4096ull + 1000000ull;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int site = 0;
+  while (site < n_sites) {
+    // the next n <= 32 words, none past the end of the current block
+    const int avail = kMTN - pos;
+    const int n = avail > 0 ? min(32, avail) : 32;
+    const uint32_t w = mt_peek(mt, pos, n, lane);
+    const int64_t wl = (int64_t)w;
+    int cand = 0, hits = 0;
+    if (lane < n)
+      for (int l = 0; l < ns; ++l)
         if (wl >= J.lo_w[l] && wl <= J.hi_w[l]) {
-          if (check[l] < J.counts[l]) {
-            s = l + 1;
+          cand = l + 1;
+          ++hits;
+        }
+    bool fast = !__any_sync(kFull, hits > 1);
+    // a candidate whose quota is already full is a plain rejection; one
+    // whose quota fills inside the batch needs the word-by-word pass
+    bool open = false;
+    if (cand > 0) open = check[cand - 1] < J.counts[cand - 1];
+    unsigned acc = __ballot_sync(kFull, open);
+    int need_mine = 0;  // lane l < ns: accepted words of species l + 1 in the batch
+    for (int l = 0; l < ns; ++l) {
+      const int c = __popc(__ballot_sync(kFull, open && cand == l + 1));
+      if (lane == l) need_mine = c;
+    }
+    if (lane < ns && check[lane] + need_mine > J.counts[lane]) fast = false;
+    fast = __all_sync(kFull, fast);
+    int consumed = n;
+    if (fast) {
+      const int r = n_sites - site;
+      if (__popc(acc) >= r) {
+        // the configuration ends inside the batch: its r-th accepted word
+        // is the last one consumed (the words after it are not drawn)
+        unsigned m = acc;
+        for (int k = 1; k < r; ++k) m &= m - 1u;
+        const int last = __ffs(m) - 1;
+        consumed = last + 1;
+        acc &= (last == 31) ? 0xffffffffu : ((1u << (last + 1)) - 1u);
+      }
+      const bool mine = (acc >> lane) & 1u;
+      if (mine) lat[site + __popc(acc & lt_mask)] = (int8_t)cand;
+      int add = 0;
+      for (int l = 0; l < ns; ++l) {
+        const int c = __popc(__ballot_sync(kFull, mine && cand == l + 1));
+        if (lane == l) add = c;
+      }
+      __syncwarp();
+      if (lane < ns) check[lane] += add;
+      site += __popc(acc);
+    } else {
+      for (int k = 0; k < n; ++k) {
+        const int64_t wk = (int64_t)__shfl_sync(kFull, w, k);
+        int s = 0;
+        for (int l = 0; l < ns; ++l)
+          if (wk >= J.lo_w[l] && wk <= J.hi_w[l] && check[l] < J.counts[l]) s = l + 1;
+        __syncwarp();
+        if (s > 0) {
+          if (lane == 0) {
+            check[s - 1] += 1;
+            lat[site] = (int8_t)s;
+          }
+          ++site;
+          if (site == n_sites) {
+            consumed = k + 1;
             __syncwarp();
-            if (lane == 0) check[l] += 1;
-            __syncwarp();
+            break;
           }
         }
+        __syncwarp();
       }
-      if (draws > limit) return false;
     }
-    if (lane == 0) lat[site] = (int8_t)s;
+    __syncwarp();
+    pos += consumed;
+    draws += (unsigned long long)consumed;
+    if (draws > limit) return false;
   }
   __syncwarp();
   return true;
