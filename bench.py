@@ -799,7 +799,7 @@ def main() -> int:
     ap.add_argument("--serve-rate", type=float, default=10.0)
     ap.add_argument("--serve-L-max", type=int, default=32)
     ap.add_argument("--serve-sweeps-max", type=int, default=2000)
-    ap.add_argument("--serve-sat-rate", type=float, default=80.0)
+    ap.add_argument("--serve-sat-rate", type=float, default=250.0)
     ap.add_argument("--serve-sat-seconds", type=float, default=45.0)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--walker-legs", default="wl,ns",

@@ -345,6 +345,7 @@ struct brawl_server {
   bool stop = false;
   size_t used = 0;
   int admitted = 0;         // jobs in set-up, ready, resident or ending
+  int admitted_kind[4] = {0, 0, 0, 0};  // the same by job kind (BRAWL_JOB_*)
   int64_t rounds = 0, ended = 0;
   std::thread th;
   std::vector<std::thread> workers;
@@ -413,6 +414,7 @@ void finish(brawl_server* S, const JobP& j, int status) {
   std::lock_guard<std::mutex> lk(S->mu);
   S->used -= j->footprint;
   S->admitted -= 1;
+  S->admitted_kind[kind_index(j->d.kind)] -= 1;
   j->res.status = status;
   j->res.t_finish = S->now();
   j->res.n_values = (int)j->values.size();
@@ -988,11 +990,32 @@ void fail_pipe(brawl_server* S, Pipe& P, int rc) {
 // arrival order while the slot count and the device-memory budget allow (a
 // job larger than the budget is admitted alone) and build their device
 // objects on the objects' own streams, so the pipelines keep running.
-bool admissible(brawl_server* S) {
-  if (S->queue.empty()) return false;
-  if (S->admitted >= S->o.max_active) return false;
-  return S->admitted == 0 || S->used + S->queue.front()->footprint <= S->o.hbm_budget;
+// Wang-Landau and nested-sampling jobs have their own resident caps: past
+// a few hundred resident walks their rounds lengthen faster than the work
+// they add (on a mixed stream at 250 jobs/s: 4.8e8 trials/s with 256
+// resident jobs, 3.6e8 with 1024, 1.5e8 uncapped), while anneal chains keep
+// gaining up to thousands.  A queued job of a kind at its cap waits; the
+// first later job of another kind is admitted instead.
+int kind_cap(const brawl_server* S, int kind) {
+  if (kind == BRAWL_JOB_WL) return S->o.max_active_wl;
+  if (kind == BRAWL_JOB_NS) return S->o.max_active_ns;
+  return S->o.max_active;
 }
+
+// The queue index of the next job to admit, or -1.
+long admissible_index(brawl_server* S) {
+  if (S->queue.empty() || S->admitted >= S->o.max_active) return -1;
+  for (size_t q = 0; q < S->queue.size(); ++q) {
+    const JobP& j = S->queue[q];
+    const int k = j->d.kind;
+    if (S->admitted_kind[kind_index(k)] >= kind_cap(S, k)) continue;
+    if (S->admitted == 0 || S->used + j->footprint <= S->o.hbm_budget) return (long)q;
+    return -1;  // the budget: wait for memory, in arrival order
+  }
+  return -1;
+}
+
+bool admissible(brawl_server* S) { return admissible_index(S) >= 0; }
 
 void end_one(brawl_server* S, const JobP& j, int status) {
   if (status == BRAWL_OK) {
@@ -1020,10 +1043,12 @@ void worker(brawl_server* S) {
       } else if (S->stop) {
         return;
       } else {
-        j = S->queue.front();
-        S->queue.pop_front();
+        const long q = admissible_index(S);
+        j = S->queue[(size_t)q];
+        S->queue.erase(S->queue.begin() + q);
         S->used += j->footprint;
         S->admitted += 1;
+        S->admitted_kind[kind_index(j->d.kind)] += 1;
         j->res.t_admit = S->now();
       }
     }
@@ -1161,6 +1186,8 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
     S->o.hbm_budget = free_b / 10 * 6;
   }
   if (S->o.max_active <= 0) S->o.max_active = 4096;
+  if (S->o.max_active_wl <= 0) S->o.max_active_wl = 128;
+  if (S->o.max_active_ns <= 0) S->o.max_active_ns = 128;
   if (!(S->o.round_ms > 0.0)) S->o.round_ms = 20.0;
   if (S->o.max_trials < 0) S->o.max_trials = 0;
   if (S->o.max_iterations < 0) S->o.max_iterations = 0;

@@ -32,7 +32,8 @@ EAGAIN, ETIMEDOUT = 7, 4
 
 class _Opts(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("round_ms", C.c_double),
-                ("max_trials", C.c_int64), ("max_iterations", C.c_int)]
+                ("max_trials", C.c_int64), ("max_iterations", C.c_int), ("max_active_wl", C.c_int),
+                ("max_active_ns", C.c_int)]
 
 
 class _JobDesc(C.Structure):
@@ -63,8 +64,9 @@ class Server:
     """A brawl_server: submit jobs, wait for them, read their values."""
 
     def __init__(self, hbm_budget: int = 0, max_active: int = 0, round_ms: float = 0.0,
-                 max_trials: int = 0, max_iterations: int = 0):
-        o = _Opts(hbm_budget, max_active, round_ms, max_trials, max_iterations)
+                 max_trials: int = 0, max_iterations: int = 0, max_active_wl: int = 0,
+                 max_active_ns: int = 0):
+        o = _Opts(hbm_budget, max_active, round_ms, max_trials, max_iterations, max_active_wl, max_active_ns)
         h = C.c_void_p()
         _check(load().brawl_serve_create(C.byref(o), C.byref(h)))
         self._h = h
