@@ -308,26 +308,14 @@ def _mean_util(samples, t_lo, t_hi):
     return float(np.mean(v)) / 100.0 if v else None
 
 
-def serving_leg(args) -> dict:
-    """The serving stream through the continuous-batching loop
-    (brawl_serve_*), on the mixed workload's ranges: fcc/bcc, L in [6, 32],
-    2-5 species, 2-6 shells, anneals of 100-2000 sweeps, Wang-Landau windows
-    and nested-sampling runs.  Two phases.
-    latency: Poisson arrivals at args.serve_rate jobs/s (below capacity),
-      latency = finish - submit per job, p50/p99 overall and by kind, the
-      device's busy fraction while jobs arrive;
-    saturation: arrivals far above capacity for args.serve_sat_seconds;
-      throughput = work the scheduler handed out per second once the resident
-      set has filled (trials; Wang-Landau summed over walkers; nested
-      sampling walk steps), and the busy fraction over the same window."""
-    from brawl_gb300 import serving as SV
-    dev = torch_device_index()
-    out = {}
-    # ---- latency phase
-    jobs = SV.stream_jobs(args.serve_jobs, master_seed=424242, L_range=(6, args.serve_L_max),
+def _serve_latency(args, SV, dev, rate: float, n_jobs: int) -> dict:
+    """Poisson arrivals of the seeded mixed stream at `rate` jobs/s; latency
+    = finish - submit per job, p50/p99 overall and by kind, the device's
+    busy fraction while jobs arrive."""
+    jobs = SV.stream_jobs(n_jobs, master_seed=424242, L_range=(6, args.serve_L_max),
                           sweeps_range=(100, args.serve_sweeps_max))
     rng = np.random.default_rng(99)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, len(jobs)))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(jobs)))
     util = UtilSampler(dev)
     with SV.Server() as srv:
         ids = []
@@ -364,14 +352,14 @@ def serving_leg(args) -> dict:
     trials = sum(SV.job_trials(j) for j, r in zip(jobs, res) if r["status"] == 0 and j["kind"] != "ns")
     ns_steps = sum(int(r["trials"]) for j, r in zip(jobs, res) if r["status"] == 0 and j["kind"] == "ns")
     counts = {k: sum(1 for j in jobs if j["kind"] == k) for k in ("anneal", "wl", "ns")}
-    out["latency"] = {
+    return {
         "stream": f"{len(jobs)} jobs (of the 10^4 of the full stream) of the seeded mixed stream: "
                   f"fcc/bcc, L in [6,{args.serve_L_max}], 2-5 species (Dirichlet composition), "
                   f"2-6 shells, V uniform +-0.05 eV; anneal 100-{args.serve_sweeps_max} sweeps over "
                   "4 temperatures, WL window (4 walkers, 256 bins, 20 one-sweep calls), NS run "
                   "(64 walkers, 100 iterations of one-sweep walks)",
         "jobs_by_kind": counts,
-        "arrivals": f"Poisson, {args.serve_rate} jobs/s over {arrivals[-1]:.0f} s",
+        "arrivals": f"Poisson, {rate} jobs/s over {arrivals[-1]:.0f} s",
         "jobs_ok": len(ok), "jobs_failed": failed,
         "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
         "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
@@ -385,7 +373,38 @@ def serving_leg(args) -> dict:
         "rounds": stats["rounds"],
         "busy_s_by_pipeline": {k: round(v["busy_s"], 2) for k, v in prof.items()},
     }
+
+
+def serving_leg(args) -> dict:
+    """The serving stream through the continuous-batching loop
+    (brawl_serve_*), on the mixed workload's ranges: fcc/bcc, L in [6, 32],
+    2-5 species, 2-6 shells, anneals of 100-2000 sweeps, Wang-Landau windows
+    and nested-sampling runs.  Two phases.
+    latency: Poisson arrivals at args.serve_rate jobs/s (below capacity),
+      latency = finish - submit per job, p50/p99 overall and by kind, the
+      device's busy fraction while jobs arrive;
+    saturation: arrivals far above capacity for args.serve_sat_seconds;
+      throughput = work the scheduler handed out per second once the resident
+      set has filled (trials; Wang-Landau summed over walkers; nested
+      sampling walk steps), and the busy fraction over the same window."""
+    from brawl_gb300 import serving as SV
+    dev = torch_device_index()
+    out = {}
+    # ---- latency phase
+    out["latency"] = _serve_latency(args, SV, dev, args.serve_rate, args.serve_jobs)
+    # ---- optional latency curve: the same stream at other arrival rates
+    rates = [float(x) for x in args.serve_rate_sweep.split(",") if x.strip()]
+    if rates:
+        curve = []
+        for r in rates:
+            L = _serve_latency(args, SV, dev, r, args.serve_sweep_jobs)
+            curve.append({"rate_jobs_per_s": r, "jobs": L["jobs_ok"], "p50_s": L["p50_s"], "p99_s": L["p99_s"],
+                          "p50_by_kind_s": L["p50_by_kind_s"], "p99_by_kind_s": L["p99_by_kind_s"],
+                          "p99_queue_s": L["p99_queue_s"], "trials_per_s": L["trials_per_s"],
+                          "gpu_busy_while_arriving": L["gpu_busy_while_arriving"]})
+        out["latency_curve"] = curve
     # ---- saturation phases: the mixed stream, then its anneal jobs alone
+    rng = np.random.default_rng(99)
     n_sat = int(args.serve_sat_rate * args.serve_sat_seconds)
     for key, kinds in (("saturation", None), ("saturation_anneal_only", ("anneal",))):
         if n_sat <= 0:
@@ -800,6 +819,9 @@ def main() -> int:
     ap.add_argument("--serve-L-max", type=int, default=32)
     ap.add_argument("--serve-sweeps-max", type=int, default=2000)
     ap.add_argument("--serve-sat-rate", type=float, default=250.0)
+    ap.add_argument("--serve-rate-sweep", default="",
+                    help="comma-separated arrival rates (jobs/s) for a latency curve (empty: none)")
+    ap.add_argument("--serve-sweep-jobs", type=int, default=300)
     ap.add_argument("--serve-sat-seconds", type=float, default=45.0)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--walker-legs", default="wl,ns",

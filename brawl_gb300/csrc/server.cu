@@ -990,12 +990,14 @@ void fail_pipe(brawl_server* S, Pipe& P, int rc) {
 // arrival order while the slot count and the device-memory budget allow (a
 // job larger than the budget is admitted alone) and build their device
 // objects on the objects' own streams, so the pipelines keep running.
-// Wang-Landau and nested-sampling jobs have their own resident caps: past
-// a few hundred resident walks their rounds lengthen faster than the work
-// they add (on a mixed stream at 250 jobs/s: 4.8e8 trials/s with 256
-// resident jobs, 3.6e8 with 1024, 1.5e8 uncapped), while anneal chains keep
-// gaining up to thousands.  A queued job of a kind at its cap waits; the
-// first later job of another kind is admitted instead.
+// Wang-Landau and nested-sampling jobs have their own resident caps: a
+// walker or run on a large lattice holds a whole SM (its shared memory) for
+// a long round, and past a few dozen of them the anneal chains lose more
+// SMs than the walks add work (on a mixed stream at 250 jobs/s, 45 s:
+// 7.3e8 trials/s with 32 of each kind resident, 6.8e8 with 64, 2.5e8 with
+// 128), while anneal chains keep gaining up to thousands.  A queued job of
+// a kind at its cap waits; the first later job of another kind is admitted
+// instead.
 int kind_cap(const brawl_server* S, int kind) {
   if (kind == BRAWL_JOB_WL) return S->o.max_active_wl;
   if (kind == BRAWL_JOB_NS) return S->o.max_active_ns;
@@ -1186,8 +1188,8 @@ int brawl_serve_create(const brawl_server_opts* opts, brawl_server** out) {
     S->o.hbm_budget = free_b / 10 * 6;
   }
   if (S->o.max_active <= 0) S->o.max_active = 4096;
-  if (S->o.max_active_wl <= 0) S->o.max_active_wl = 128;
-  if (S->o.max_active_ns <= 0) S->o.max_active_ns = 128;
+  if (S->o.max_active_wl <= 0) S->o.max_active_wl = 64;
+  if (S->o.max_active_ns <= 0) S->o.max_active_ns = 64;
   if (!(S->o.round_ms > 0.0)) S->o.round_ms = 20.0;
   if (S->o.max_trials < 0) S->o.max_trials = 0;
   if (S->o.max_iterations < 0) S->o.max_iterations = 0;

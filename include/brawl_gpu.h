@@ -466,8 +466,8 @@ typedef struct brawl_server_opts {
                                    per round (0: none) */
     int max_iterations;         /* cap on a nested-sampling job's iterations per
                                    round (0: none) */
-    int max_active_wl;          /* resident Wang-Landau jobs at most (0: 128) */
-    int max_active_ns;          /* resident nested-sampling jobs at most (0: 128);
+    int max_active_wl;          /* resident Wang-Landau jobs at most (0: 64) */
+    int max_active_ns;          /* resident nested-sampling jobs at most (0: 64);
                                    queued jobs of a kind at its cap wait while
                                    later jobs of other kinds are admitted */
 } brawl_server_opts;
