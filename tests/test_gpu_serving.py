@@ -185,3 +185,27 @@ def test_serving_budget_queues_jobs_and_reports_bad_jobs():
         assert r["status"] == 0
         vals, _ = _oracle(narrow)
         assert np.array_equal(srv.values(jid, r["n_values"]), vals)
+
+
+def test_serving_kind_caps_admit_past_a_capped_kind():
+    """With one resident nested-sampling job allowed, the second and third
+    wait for the first to end while the anneal jobs queued behind them are
+    admitted at once; every job still equals the oracle's run."""
+    jobs = _jobs()
+    ns = [j for j in jobs if j["kind"] == "ns"]
+    ns.append(_job("ns", "fcc", 2, 2, 2, 33, ns_walkers=12, ns_steps=16, ns_iter=12))
+    anneals = [j for j in jobs if j["kind"] == "anneal"]
+    order = ns + anneals
+    with S.Server(max_active_ns=1, max_iterations=2) as srv:
+        ids = [srv.submit(j) for j in order]
+        res = [_collect(srv, i) for i in ids]
+    r_ns, r_an = res[:len(ns)], res[len(ns):]
+    # at most one nested-sampling job resident at a time, in arrival order
+    for a, b in zip(r_ns, r_ns[1:]):
+        assert b["t_admit"] >= a["t_finish"]
+    # the anneals did not wait behind the capped kind
+    assert all(r["t_admit"] < r_ns[1]["t_admit"] for r in r_an)
+    for job, r in zip(order, res):
+        vals, cfg = _oracle(job)
+        assert np.array_equal(r["values"], vals), job["kind"]
+        assert np.array_equal(r["config"], cfg), job["kind"]
