@@ -295,15 +295,20 @@ __device__ inline bool initial_setup_warp(const InitJob& J, int8_t* lat, uint32_
     } else {
       for (int k = 0; k < n; ++k) {
         const int64_t wk = (int64_t)__shfl_sync(kFull, w, k);
+        // every species whose interval holds the word and whose quota is
+        // open takes the site in turn and uses up one of its quota (a word
+        // on the boundary of two intervals uses up both); the last one keeps it
         int s = 0;
+        unsigned taken = 0u;
         for (int l = 0; l < ns; ++l)
-          if (wk >= J.lo_w[l] && wk <= J.hi_w[l] && check[l] < J.counts[l]) s = l + 1;
+          if (wk >= J.lo_w[l] && wk <= J.hi_w[l] && check[l] < J.counts[l]) {
+            s = l + 1;
+            taken |= 1u << l;
+          }
         __syncwarp();
         if (s > 0) {
-          if (lane == 0) {
-            check[s - 1] += 1;
-            lat[site] = (int8_t)s;
-          }
+          if (lane < ns && ((taken >> lane) & 1u)) check[lane] += 1;
+          if (lane == 0) lat[site] = (int8_t)s;
           ++site;
           if (site == n_sites) {
             consumed = k + 1;

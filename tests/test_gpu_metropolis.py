@@ -626,3 +626,66 @@ def test_anneal_sweeps_equal_per_sweep_calls():
     s_p = p2.temperature_stats(6, 6 * n, 500.0, 500.0 * B.K_B_IN_RY, True)
     s_q = q2.temperature_stats(6, 6 * n, 500.0, 500.0 * B.K_B_IN_RY, True)
     assert np.array_equal(s_p[0], s_q[0]) and np.array_equal(s_p[1], s_q[1])
+
+
+def _temper(y):
+    y ^= y >> 11
+    y ^= (y << 7) & 0x9D2C5680
+    y ^= (y << 15) & 0xEFC60000
+    y ^= y >> 18
+    return y & 0xFFFFFFFF
+
+
+def _untemper(y):
+    """The mt19937 state word whose tempered output is y."""
+    y ^= y >> 18
+    y ^= (y << 15) & 0xEFC60000
+    t = y
+    for _ in range(5):
+        t = y ^ ((t << 7) & 0x9D2C5680)
+    y = t & 0xFFFFFFFF
+    t = y
+    for _ in range(3):
+        t = y ^ (t >> 11)
+    return t & 0xFFFFFFFF
+
+
+def test_initial_setup_on_interval_boundaries():
+    """A stream word on the boundary of two species' intervals: every species
+    whose quota is open takes the site in turn and uses up one of its quota
+    (src/initialise.F90's loop over l), the last one keeping it.  With one
+    side already full the word is an ordinary draw (device equals the
+    oracle, word for word); with both open a quota is used up twice, the
+    configuration can never be completed (the reference loops forever) and
+    the device reports the chain at its draw limit."""
+    for x in (0, 1, 0x80000000, 0x12345678, 0xFFFFFFFF):
+        assert _temper(_untemper(x)) == x
+    rng = np.random.default_rng(17)
+    setup = B.Setup("fcc", 2, 2, 2, 2, 1)  # 32 sites
+    V = random_V(rng, 2, 1)
+    base = O.OracleRng(4321).state_words()
+    # species 1 holds [0, 2^27], species 2 [2^27, 2^32 - 1] (1 : 31 atoms)
+    nums = np.array([1, 31], dtype=np.int64)
+    st = base.copy()
+    st[0] = _untemper(100)            # species 1: its only atom
+    st[1] = _untemper(1 << 27)        # the boundary, species 1 already full
+    st[624] = 0
+    mod = O.OracleModel("fcc", 2, 2, 2, V)
+    r = O.OracleRng(1)
+    r.set_state_words(st)
+    cfg, conc_o = mod.initial_setup(r, np.array([0.0, 0.5, 0.5]), nums)
+    ch = B.Chain(setup, V)
+    ch.set_rng_state(st)
+    conc_g = ch.initial_setup(np.array([0.0, 0.5, 0.5]), nums)
+    assert np.array_equal(ch.config(), cfg) and np.array_equal(conc_g, conc_o)
+    assert np.array_equal(ch.genrand(8), np.array([r.uniform() for _ in range(8)]))
+    # both quotas open at the boundary word (16 : 16, boundary 2^31), drawn
+    # first or in the middle of a 32-word batch
+    for at in (0, 5):
+        st = base.copy()
+        st[at] = _untemper(1 << 31)
+        st[624] = 0
+        ch = B.Chain(setup, V)
+        ch.set_rng_state(st)
+        with pytest.raises(B.BrawlError):
+            ch.initial_setup(np.array([0.0, 0.5, 0.5]), np.array([16, 16], dtype=np.int64))
