@@ -481,3 +481,29 @@ def test_wang_landau_driver_performance_gates_the_optimiser(monkeypatch):
     # no pre-sampling: no store, no reloads
     W, out = _run_driver(monkeypatch, pre_sample=False)
     assert not W.enabled and not any(x[0] == "load" for x in W.log if not isinstance(x, str))
+
+
+def test_sweep_blocks_end_at_host_side_samples():
+    """The annealing drivers run the sweeps between host-side samples as one
+    device block: a block ends at the first sweep after which ASRO or ALRO
+    is sampled, else at the temperature's last sweep."""
+    m = I.MetropolisParams(mode="simulated_annealing", n_mc_steps=10 * 8, n_sample_steps=8,
+                           calculate_energies=True, calculate_asro=True, n_sample_steps_asro=3 * 8,
+                           n_sample_steps_trajectory=8, T=300.0, T_steps=1, delta_T=0.0)
+
+    def blocks(m, n_sweeps=10, step=8):
+        out, i = [], 1
+        while i <= n_sweeps:
+            e = M._block_end(m, i, n_sweeps, step)
+            out.append((i, e))
+            i = e + 1
+        return out
+
+    assert blocks(m) == [(1, 3), (4, 6), (7, 9), (10, 10)]
+    m.calculate_asro = False
+    assert blocks(m) == [(1, 10)]
+    m.calculate_alro = True
+    m.n_sample_steps_alro = 4 * 8
+    assert blocks(m) == [(1, 4), (5, 8), (9, 10)]
+    m.calculate_asro = True
+    assert blocks(m) == [(1, 3), (4, 4), (5, 6), (7, 8), (9, 9), (10, 10)]
