@@ -692,6 +692,7 @@ def _wl_windows_run(args, setup, V, conc) -> dict:
         "trials_per_s": 128 * 10_000 * calls / loop_s,
         "ln_f_reached": rec[-1]["wl_f"] if rec else 1.0,
         "calls_per_halving": c_k,
+        "seconds_at_halving": [round(float(r["seconds"]), 2) for r in rec],
         "seconds_to_ln_f_1e-6_extrapolated": est,
         "extrapolation": "calls per halving fitted as a*r^k on the measured halvings; "
                          "the halvings up to 2^-20 < 1e-6 at the run's seconds per call",
