@@ -469,6 +469,29 @@ struct CompactLat {
   __device__ __forceinline__ int operator()(int i) const { return p[i]; }
 };
 
+// The pair energies from the (evaluation, shell) partial sums, sum c = ev
+// * nsh + sh in lane c of part[0] (c < 32) or lane c - 32 of part[1]: lane
+// ev < 4 adds the shell sums of evaluation ev in shell order (site 1
+// before, site 2 before, site 1 after, site 2 after; nbr_energy's shell 1 +
+// shell 2 + ...), all four at once, then e_un = e(site 1) + e(site 2)
+// before and e_sw the same after (pair_energy).  Every lane returns both.
+__device__ __forceinline__ void combine_pair_energies(const double part[2], int nsh, int lane, double& e_un,
+                                                      double& e_sw) {
+  const int ev = lane & 3;
+  double acc = 0.0;
+  for (int sh = 0; sh < nsh; ++sh) {
+    const int c = ev * nsh + sh;
+    const double v0 = __shfl_sync(kFull, part[0], c & 31);
+    const double v1 = __shfl_sync(kFull, part[1], c & 31);
+    const double v = c < 32 ? v0 : v1;
+    acc = sh == 0 ? v : __dadd_rn(acc, v);
+  }
+  // lane 0: e(site 1 before) + e(site 2 before); lane 2: the same after
+  const double pair = __dadd_rn(acc, __shfl_down_sync(kFull, acc, 1));
+  e_un = __shfl_sync(kFull, pair, 0);
+  e_sw = __shfl_sync(kFull, pair, 2);
+}
+
 template <class Lat>
 __device__ inline void exact_pair_energies(const Geom& g, const Lat& lat, const double* V,
                                            const uint32_t* ents, const int16_t* sstart,
@@ -503,19 +526,7 @@ __device__ inline void exact_pair_energies(const Geom& g, const Lat& lat, const 
       part[r] = sum;
     }
   }
-  double e[4];
-#pragma unroll
-  for (int ev = 0; ev < 4; ++ev) {
-    double acc = 0.0;
-    for (int sh = 0; sh < nsh; ++sh) {
-      const int c = ev * nsh + sh;
-      double v = c < 32 ? __shfl_sync(kFull, part[0], c) : __shfl_sync(kFull, part[1], c - 32);
-      acc = sh == 0 ? v : __dadd_rn(acc, v);
-    }
-    e[ev] = acc;
-  }
-  e_un = __dadd_rn(e[0], e[1]);
-  e_sw = __dadd_rn(e[2], e[3]);
+  combine_pair_energies(part, nsh, lane, e_un, e_sw);
 }
 
 // The same sums with the terms staged first: every (evaluation, neighbour)
@@ -574,19 +585,7 @@ __device__ inline void exact_pair_energies_staged(const Geom& g, const Lat& lat,
       part[r] = sum;
     }
   }
-  double e[4];
-#pragma unroll
-  for (int ev = 0; ev < 4; ++ev) {
-    double acc = 0.0;
-    for (int sh = 0; sh < nsh; ++sh) {
-      const int c = ev * nsh + sh;
-      double v = c < 32 ? __shfl_sync(kFull, part[0], c) : __shfl_sync(kFull, part[1], c - 32);
-      acc = sh == 0 ? v : __dadd_rn(acc, v);
-    }
-    e[ev] = acc;
-  }
-  e_un = __dadd_rn(e[0], e[1]);
-  e_sw = __dadd_rn(e[2], e[3]);
+  combine_pair_energies(part, nsh, lane, e_un, e_sw);
   __syncwarp();  // vbuf is reused by the next call
 }
 

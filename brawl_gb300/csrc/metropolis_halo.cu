@@ -132,19 +132,9 @@ static __device__ __noinline__ int halo_exact_far(const ChainJob* __restrict__ J
     }
     part[r] = sum;
   }
-  double e[4];
-#pragma unroll 1
-  for (int ev = 0; ev < 4; ++ev) {
-    double acc = 0.0;
-#pragma unroll 1
-    for (int sh = 0; sh < nsh; ++sh) {
-      const int c = ev * nsh + sh;
-      const double v = c < 32 ? __shfl_sync(kFull, part[0], c) : __shfl_sync(kFull, part[1], c - 32);
-      acc = sh == 0 ? v : __dadd_rn(acc, v);
-    }
-    e[ev & 3] = acc;
-  }
-  const double delta_e = __dsub_rn(__dadd_rn(e[2], e[3]), __dadd_rn(e[0], e[1]));
+  double e_un, e_sw;
+  combine_pair_energies(part, nsh, lane, e_un, e_sw);
+  const double delta_e = __dsub_rn(e_sw, e_un);
   if (delta_e < 0.0) return 1;
   DecideStats st = {0u, 0u};
   const int acc = u_lt_exp(wu, __dmul_rn(-Jg->beta, delta_e), st);
