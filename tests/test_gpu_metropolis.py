@@ -603,6 +603,14 @@ def test_anneal_sweeps_equal_per_sweep_calls():
     E0, acc0 = b_.anneal_sweeps(beta, 3, sweep, energies=False)
     acc_ref = sum(a.metropolis(beta, sweep) for _ in range(3))
     assert E0 is None and acc0 == acc_ref and np.array_equal(a.config(), b_.config())
+    # neighbour swaps (monte_carlo_step_nbr)
+    E_ref, acc_ref = [], 0
+    for _ in range(4):
+        acc_ref += a.metropolis(beta, sweep, nbr_swap=True)
+        E_ref.append(a.total_energy())
+    E, acc = b_.anneal_sweeps(beta, 4, sweep, nbr_swap=True)
+    assert acc == acc_ref and np.array_equal(E, np.array(E_ref))
+    assert np.array_equal(a.config(), b_.config()) and np.array_equal(a.rng_state(), b_.rng_state())
 
     # a batch of two classes (different L) with their own betas, sums on the device
     V4 = random_V(rng, 4, 6)
